@@ -1,0 +1,455 @@
+"""Device models on the Newton hot path, as vectorized element groups.
+
+Each class mirrors a voltax element (same terminals, internal unknowns and
+parameter names; log-space storage of positive quantities):
+
+* `Resistor`, `Capacitor`      -- voltax/elements/passive.py:13-59
+* `Conductance`                -- voltax/elements/behavioral.py:29-99
+* `VoltageSource`, `CurrentSource` -- voltax/elements/sources.py:58-115
+* `MOSProcess`, `EKVMOSFET`    -- voltax/elements/mosfet.py:26-205
+
+The physics itself is evaluated by the CUDA device kernels
+(``voltax_gb300/csrc/devices.cuh``). On the host an element only knows its
+nodes, its parameters (float64 torch tensors, ``(N,)`` or ``(B, N)`` for a
+batch of B circuit instances) and how to turn them into the kernel's
+per-device parameter rows (`gpu_params`). Those rows are computed with torch
+ops, so gradients flow from the kernel's parameter VJP back to the user's
+parameters through ordinary torch autograd.
+"""
+
+from __future__ import annotations
+
+from typing import Any, Sequence
+
+import numpy as np
+import torch
+
+from .signals import Constant, Signal, as_signal
+
+_F64 = torch.float64
+VT_300K = 0.025852
+"""Thermal voltage kT/q at 300 K (voltax/elements/semiconductor.py:13)."""
+
+# kernel codes of the device table (must match csrc/vxg_types.h)
+KIND_CONDUCTANCE = 0
+KIND_CAPACITOR = 1
+KIND_VSOURCE = 2
+KIND_ISOURCE = 3
+KIND_EKV = 4
+
+
+def _t(x) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(_F64)
+    return torch.as_tensor(np.asarray(x, dtype=np.float64))
+
+
+def positive_log(x) -> torch.Tensor:
+    """``log(x)``, validating that `x` is positive (voltax/element.py:40-45)."""
+    x = _t(x)
+    if not x.requires_grad and bool(torch.any(x <= 0)):
+        raise ValueError(f"expected a positive value, got {x}")
+    return torch.log(x)
+
+
+def _is_single(nodes: Sequence[Any]) -> bool:
+    return len(nodes) > 0 and isinstance(nodes[0], (int, str, np.integer))
+
+
+class Element:
+    """A vectorized group of ``N`` devices of one type (voltax/element.py:66-131).
+
+    Subclasses declare ``terminals``, ``n_internal``, ``internal_names``,
+    ``shared`` (fields common to all devices), ``fields`` (per-device
+    parameter tensors) and the kernel ``kind``.
+    """
+
+    terminals: tuple[str, ...] = ()
+    n_internal: int = 0
+    internal_names: tuple[str, ...] = ()
+    shared: tuple[str, ...] = ()
+    fields: tuple[str, ...] = ()
+    static: tuple[str, ...] = ()
+    local: bool = True
+    kind: int = -1
+    has_charges: bool = False
+
+    nodes: tuple[tuple[Any, ...], ...]
+
+    # ------------------------------------------------------------ structure
+    @property
+    def size(self) -> int:
+        return len(self.nodes)
+
+    def node_array(self) -> np.ndarray:
+        return np.asarray(self.nodes, dtype=np.int64).reshape(self.size, -1)
+
+    def with_nodes(self, nodes) -> "Element":
+        new = object.__new__(type(self))
+        new.__dict__.update(self.__dict__)
+        new.nodes = tuple(tuple(d) for d in nodes)
+        return new
+
+    @staticmethod
+    def _devices(nodes) -> tuple[tuple[Any, ...], ...]:
+        if _is_single(nodes):
+            return (tuple(nodes),)
+        return tuple(tuple(d) for d in nodes)
+
+    def _per_device(self, value) -> torch.Tensor:
+        value = _t(value)
+        if value.ndim == 0:
+            return value.expand(self.size).clone()
+        if value.shape[-1] != self.size:
+            raise ValueError(f"expected a scalar or shape (..., {self.size}) value, "
+                             f"got {tuple(value.shape)}")
+        return value
+
+    def _log_per_device(self, value) -> torch.Tensor:
+        return self._per_device(positive_log(value))
+
+    # ------------------------------------------------------------ parameters
+    def param_tensors(self) -> dict[str, torch.Tensor]:
+        return {f: getattr(self, f) for f in self.fields}
+
+    def batch_size(self) -> int:
+        """Instances in the parameters' leading axis (1 when unbatched)."""
+        sizes = {p.shape[0] for p in self._all_params() if p.ndim == 2}
+        if len(sizes) > 1:
+            raise ValueError(f"inconsistent batch sizes {sizes}")
+        return sizes.pop() if sizes else 1
+
+    def _all_params(self) -> list[torch.Tensor]:
+        return list(self.param_tensors().values())
+
+    def get(self, field: str, index=slice(None)):
+        return getattr(self, field)[..., index]
+
+    def set(self, index: int, **values) -> "Element":
+        """Copy with device `index`'s parameters replaced (physical units;
+        log-space fields handled as in voltax/element.py:143-163)."""
+        out = self.with_nodes(self.nodes)
+        for key, value in values.items():
+            log_attr = f"log_{key.rstrip('_')}"
+            if log_attr in self.fields:
+                attr, value = log_attr, torch.log(_t(value))
+            elif key in self.fields:
+                attr, value = key, _t(value)
+            else:
+                settable = sorted(f.removeprefix("log_") for f in self.fields)
+                raise AttributeError(f"{type(self).__name__} has no per-device "
+                                     f"parameter {key!r}; settable: {settable}")
+            new = getattr(out, attr).clone()
+            new[..., index] = value
+            setattr(out, attr, new)
+        return out
+
+    def gpu_params(self) -> list[torch.Tensor]:
+        """Kernel parameter rows, each ``(N,)`` or ``(B, N)`` float64."""
+        raise NotImplementedError
+
+    def group_key(self) -> tuple:
+        """Elements with equal keys can be fused (voltax/element.py:218-242)."""
+        static = tuple((s, getattr(self, s)) for s in self.static)
+        shared = tuple(id(getattr(self, s)) for s in self.shared)
+        return (type(self), static, shared)
+
+
+def concatenate(elements: Sequence[Element]) -> Element:
+    """Fuse same-type elements into one group (voltax/element.py:198-215)."""
+    first = elements[0]
+    if len(elements) == 1:
+        return first
+    out = first.with_nodes([d for e in elements for d in e.nodes])
+    for f in first.fields:
+        xs = [getattr(e, f) for e in elements]
+        batched = max(x.ndim for x in xs) == 2
+        if batched:
+            B = max(x.shape[0] for x in xs if x.ndim == 2)
+            xs = [x if x.ndim == 2 else x.expand(B, x.shape[-1]) for x in xs]
+        setattr(out, f, torch.cat(xs, dim=-1))
+    if hasattr(first, "value") and isinstance(first.value, Signal):
+        sigs = [e.value for e in elements]
+        params = []
+        for i in range(len(first.value.fields)):
+            xs = [s.params()[i] for s in sigs]
+            batched = max(x.ndim for x in xs) == 2
+            if batched:
+                B = max(x.shape[0] for x in xs if x.ndim == 2)
+                xs = [x if x.ndim == 2 else x.expand(B, x.shape[-1]) for x in xs]
+            params.append(torch.cat(xs, dim=-1))
+        out.value = first.value.replace_params(params)
+    return out
+
+
+# =============================================================================
+# Linear two-terminal elements
+# =============================================================================
+
+
+class Resistor(Element):
+    """Linear resistor, ``i = (v_p - v_n) exp(-log_r)`` (passive.py:13-38)."""
+
+    terminals = ("p", "n")
+    fields = ("log_r",)
+    kind = KIND_CONDUCTANCE
+
+    def __init__(self, nodes, r):
+        self.nodes = self._devices(nodes)
+        self.log_r = self._log_per_device(r)
+
+    @property
+    def r(self):
+        return torch.exp(self.log_r)
+
+    @property
+    def g(self):
+        return torch.exp(-self.log_r)
+
+    def gpu_params(self):
+        return [torch.exp(-self.log_r)]
+
+
+class Conductance(Element):
+    """Linear conductance ``i = g(theta) (v_p - v_n)`` with a chosen map from
+    ``theta`` to ``g`` (behavioral.py:29-99): log, softplus, sigmoid, linear."""
+
+    terminals = ("p", "n")
+    fields = ("theta",)
+    static = ("transform", "g_min", "g_max")
+    kind = KIND_CONDUCTANCE
+
+    def __init__(self, nodes, g, transform: str = "log", g_min: float = 0.0,
+                 g_max: float = 1.0):
+        if transform not in ("log", "softplus", "sigmoid", "linear"):
+            raise ValueError(f"unknown transform {transform!r}")
+        self.nodes = self._devices(nodes)
+        self.transform, self.g_min, self.g_max = transform, g_min, g_max
+        self.theta = self._per_device(self.to_theta(g))
+
+    def to_theta(self, g):
+        g = _t(g)
+        if self.transform == "log":
+            return torch.log(g)
+        if self.transform == "softplus":
+            y = g - self.g_min
+            return y + torch.log(-torch.expm1(-y))
+        if self.transform == "sigmoid":
+            u = (g - self.g_min) / (self.g_max - self.g_min)
+            return torch.log(u) - torch.log1p(-u)
+        return g
+
+    @property
+    def g(self):
+        th = self.theta
+        if self.transform == "log":
+            return torch.exp(th)
+        if self.transform == "softplus":
+            return self.g_min + torch.logaddexp(th, torch.zeros_like(th))
+        if self.transform == "sigmoid":
+            return self.g_min + (self.g_max - self.g_min) * torch.sigmoid(th)
+        return th
+
+    def set(self, index, **values):
+        if "g" in values:
+            values["theta"] = self.to_theta(values.pop("g"))
+        if "r" in values:
+            values["theta"] = self.to_theta(1.0 / _t(values.pop("r")))
+        return super().set(index, **values)
+
+    def gpu_params(self):
+        return [self.g]
+
+
+class Capacitor(Element):
+    """Linear capacitor, ``q = c (v_p - v_n)`` (passive.py:41-59)."""
+
+    terminals = ("p", "n")
+    fields = ("log_c",)
+    kind = KIND_CAPACITOR
+    has_charges = True
+
+    def __init__(self, nodes, c):
+        self.nodes = self._devices(nodes)
+        self.log_c = self._log_per_device(c)
+
+    @property
+    def c(self):
+        return torch.exp(self.log_c)
+
+    def gpu_params(self):
+        return [torch.exp(self.log_c)]
+
+
+# =============================================================================
+# Sources
+# =============================================================================
+
+
+class _Source(Element):
+    terminals = ("p", "n")
+    fields = ()
+
+    def _init_source(self, nodes, value):
+        self.nodes = self._devices(nodes)
+        sig = as_signal(value)
+        single = _is_single(nodes)
+        self.value = sig.map(lambda x: x.reshape(1) if single and x.ndim == 0
+                             else self._per_device(x))
+
+    @property
+    def static(self):  # waveform type decides the kernel branch
+        return ("wave_kind",)
+
+    @property
+    def wave_kind(self) -> int:
+        return self.value.kind
+
+    def _all_params(self):
+        return self.value.params()
+
+    def with_dc(self, values) -> "_Source":
+        out = self.with_nodes(self.nodes)
+        out.value = Constant(self._per_device(values))
+        return out
+
+    def set(self, index, **values):
+        out = self.with_nodes(self.nodes)
+        out.value = self.value.map(lambda x: x.clone())
+        for key in [k for k in values if k in self.value.fields and k != "value"]:
+            getattr(out.value, key)[..., index] = _t(values.pop(key))
+        if "value" in values:
+            dc = _t(values.pop("value"))
+            if isinstance(out.value, Constant):
+                v = out.value.value.clone()
+                if dc.ndim == 1 and v.ndim == 1 and dc.shape[0] != v.shape[0]:
+                    v = v.expand(dc.shape[0], v.shape[0]).clone()
+                    v[:, index] = dc
+                else:
+                    v[..., index] = dc
+                out.value = Constant(v)
+            elif self.size == 1:
+                out.value = Constant(dc.reshape(-1) if dc.ndim else dc.reshape(1))
+            else:
+                raise TypeError("set(value=...) on a batched non-DC source")
+        if values:
+            raise AttributeError(f"unknown source parameters {sorted(values)}")
+        return out
+
+    def gpu_params(self):
+        return self.value.params()
+
+
+class VoltageSource(_Source):
+    """Independent voltage source ``v_p - v_n = value(t)``; internal unknown
+    ``i`` flows p -> n through the source (sources.py:58-87)."""
+
+    n_internal = 1
+    internal_names = ("i",)
+    kind = KIND_VSOURCE
+
+    def __init__(self, nodes, value: Signal | Any = 0.0):
+        self._init_source(nodes, value)
+
+
+class CurrentSource(_Source):
+    """Independent current source driving ``value(t)`` from p to n through
+    the source (sources.py:90-115)."""
+
+    kind = KIND_ISOURCE
+
+    def __init__(self, nodes, value: Signal | Any = 0.0):
+        self._init_source(nodes, value)
+
+
+# =============================================================================
+# EKV MOSFET
+# =============================================================================
+
+
+class MOSProcess:
+    """Shared technology parameters (mosfet.py:26-87)."""
+
+    def __init__(self, kp=400e-6, vth=0.4, n=1.3, lam=0.04, vt=VT_300K, gamma=0.0,
+                 phi=0.7, cox=8.6e-3, cov=0.3e-9):
+        self.log_kp = positive_log(kp)
+        self.vth, self.n, self.lam, self.vt = _t(vth), _t(n), _t(lam), _t(vt)
+        self.gamma, self.phi = _t(gamma), _t(phi)
+        self.log_cox = positive_log(cox)
+        self.log_cov = positive_log(cov)
+
+    @classmethod
+    def nmos(cls, **overrides) -> "MOSProcess":
+        return cls(**{"kp": 400e-6, **overrides})
+
+    @classmethod
+    def pmos(cls, **overrides) -> "MOSProcess":
+        return cls(**{"kp": 200e-6, **overrides})
+
+    @property
+    def kp(self):
+        return torch.exp(self.log_kp)
+
+    @property
+    def cox(self):
+        return torch.exp(self.log_cox)
+
+    @property
+    def cov(self):
+        return torch.exp(self.log_cov)
+
+
+class EKVMOSFET(Element):
+    """EKV 2.6-style MOSFET (mosfet.py:155-205); terminals ``(d, g, s, b)``.
+
+    Kernel parameter rows (all per device): sign, i_spec = 2 n kp (W/L) vt^2,
+    vth, dvth, n, vt, lam, c_ox = cox W L, cov W.
+    """
+
+    terminals = ("d", "g", "s", "b")
+    shared = ("process",)
+    fields = ("log_w", "log_l", "dvth")
+    static = ("polarity",)
+    kind = KIND_EKV
+    has_charges = True
+
+    def __init__(self, nodes, w=1e-6, l=0.13e-6, process: MOSProcess | None = None,
+                 polarity: str = "n", dvth=0.0):
+        if polarity not in ("n", "p"):
+            raise ValueError(f"polarity must be 'n' or 'p', got {polarity!r}")
+        self.nodes = self._devices(nodes)
+        self.polarity = polarity
+        self.log_w = self._log_per_device(w)
+        self.log_l = self._log_per_device(l)
+        self.dvth = self._per_device(dvth)
+        if process is None:
+            process = MOSProcess.nmos() if polarity == "n" else MOSProcess.pmos()
+        self.process = process
+
+    @property
+    def w(self):
+        return torch.exp(self.log_w)
+
+    @property
+    def l(self):
+        return torch.exp(self.log_l)
+
+    @property
+    def sign(self) -> float:
+        return 1.0 if self.polarity == "n" else -1.0
+
+    def gpu_params(self):
+        p = self.process
+        w, l = self.w, self.l
+        i_spec = 2 * p.n * p.kp * (w / l) * p.vt ** 2
+        shape = i_spec.shape
+
+        def full(x):
+            return _t(x).expand(shape)
+
+        return [full(self.sign), i_spec, full(p.vth), self.dvth.expand(shape),
+                full(p.n), full(p.vt), full(p.lam), p.cox * w * l, p.cov * w]
+
+
+ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
+                 EKVMOSFET)

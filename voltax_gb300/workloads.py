@@ -1,0 +1,112 @@
+"""Seeded synthetic circuits of the benchmark workloads.
+
+All draws use ``numpy.random.default_rng(seed)``.
+
+* `power_grid(n)`: n x n resistive mesh; segment conductance
+  ``exp(N(0, 0.3))`` S (median 1 S), a sink ``U(0, 1 mA)`` at every node,
+  1.0 V pads at the 4 corners and at every 25th node of a clockwise walk of
+  the border starting at the top-left corner (100 x 100: 19 pads, 10,019
+  unknowns). Structure follows voltax/benchmarks/benchmark_power_grid.py:30-66.
+* `ring_oscillator(stages)`: CMOS ring of EKV inverters (NMOS w=1u, PMOS
+  w=2u, l=0.13u), VDD 1.2 V, 5 fF per stage; `ring_initial_state` gives the
+  alternating rail pattern with a 0.1 V kick on node 0.
+* `mirror_adder_mc(instances)`: 4-bit ripple-carry adder of 28-transistor
+  mirror full adders, per-device ``dvth ~ N(0, 30 mV)`` and
+  ``log W += N(0, 0.05)``; A and B step 0000 -> 1111 with 20 ps edges.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .builder import CircuitBuilder
+from .library import cmos
+from .signals import Step
+
+VDD = 1.2
+
+
+def grid_pads(n: int, every: int = 25) -> list[tuple[int, int]]:
+    """Pad sites: corners plus every `every`-th node of the border walk."""
+    walk = ([(0, j) for j in range(n)] + [(i, n - 1) for i in range(1, n)]
+            + [(n - 1, j) for j in range(n - 2, -1, -1)]
+            + [(i, 0) for i in range(n - 2, 0, -1)])
+    sites = {walk[p] for p in range(0, len(walk), every)}
+    sites |= {(0, 0), (0, n - 1), (n - 1, 0), (n - 1, n - 1)}
+    return sorted(sites)
+
+
+def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
+               sink_max: float = 1e-3, vpad: float = 1.0):
+    rng = np.random.default_rng(seed)
+    b = CircuitBuilder()
+    node = lambda i, j: f"n{i}_{j}"  # noqa: E731
+    edges = []
+    for i in range(n):
+        for j in range(n):
+            if j + 1 < n:
+                edges.append((node(i, j), node(i, j + 1)))
+            if i + 1 < n:
+                edges.append((node(i, j), node(i + 1, j)))
+    g = np.exp(rng.normal(0.0, sigma, len(edges)))
+    for k, (a, c) in enumerate(edges):
+        b.resistor(a, c, 1.0 / g[k], name=f"R{k}")
+    sinks = rng.uniform(0.0, sink_max, n * n)
+    for p in range(n * n):
+        b.isource(node(p // n, p % n), "0", sinks[p], name=f"I{p}")
+    for k, (i, j) in enumerate(grid_pads(n)):
+        b.vsource(node(i, j), "0", vpad, name=f"Vpad{k}")
+    return b.build()
+
+
+def ring_oscillator(stages: int = 101, cload: float = 5e-15):
+    b = CircuitBuilder()
+    b.vsource("vdd", "0", VDD, name="Vdd")
+    nodes = [f"n{k}" for k in range(stages)]
+    cmos.ring_oscillator(b, nodes, "vdd", wn=1e-6, wp=2e-6)
+    for nd in nodes:
+        b.capacitor(nd, "0", cload)
+    return b.build(), nodes
+
+
+def ring_initial_state(circuit, nodes, kick: float = 0.1) -> torch.Tensor:
+    """Alternating rails (node k at VDD for odd k) with node 0 at `kick`."""
+    v = {"vdd": VDD, **{nd: VDD * (k % 2) for k, nd in enumerate(nodes)}}
+    v[nodes[0]] = kick
+    return circuit.state(v=v)
+
+
+def mirror_adder(bits: int = 4, edge: float = 20e-12, delay: float = 50e-12,
+                 cload: float = 1e-15):
+    """One nominal adder; inputs A, B step 0 -> VDD at `delay`, cin = 0."""
+    b = CircuitBuilder()
+    b.vsource("vdd", "0", VDD, name="Vdd")
+    a = [f"a{i}" for i in range(bits)]
+    c = [f"b{i}" for i in range(bits)]
+    for nd in a + c:
+        b.vsource(nd, "0", Step(0.0, VDD, delay, edge), name=f"V{nd}")
+    s = [f"s{i}" for i in range(bits)]
+    cmos.mirror_ripple_adder(b, a, c, "0", s, "co", "vdd")
+    for nd in s + ["co"]:
+        b.capacitor(nd, "0", cload)
+    return b.build()
+
+
+def mirror_adder_mc(instances: int = 4096, seed: int = 0, bits: int = 4,
+                    sigma_vth: float = 0.03, sigma_logw: float = 0.05):
+    """`mirror_adder` with a leading instance axis on the MOSFET parameters."""
+    c = mirror_adder(bits)
+    rng = np.random.default_rng(seed)
+    for name in sorted(c.elements):
+        el = c.elements[name]
+        if not hasattr(el, "dvth"):
+            continue
+        n = el.size
+        new = el.with_nodes(el.nodes)
+        new.dvth = torch.as_tensor(rng.normal(0.0, sigma_vth, (instances, n)))
+        new.log_w = el.log_w + torch.as_tensor(rng.normal(0.0, sigma_logw,
+                                                          (instances, n)))
+        new.log_l = el.log_l.expand(instances, n).clone()
+        c = c.replace(name, new)
+    return c
