@@ -1,0 +1,193 @@
+"""Device physics in torch float64 on the CPU (oracle).
+
+Each element group becomes a `GroupModel` with ``currents(v, x, t) -> (I,
+F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
+
+* Resistor            voltax/elements/passive.py:37-38
+* Capacitor           voltax/elements/passive.py:58-59
+* Conductance         voltax/elements/behavioral.py:78-99
+* VoltageSource       voltax/elements/sources.py:85-87
+* CurrentSource       voltax/elements/sources.py:110-112
+* EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
+                      ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
+* Constant/Step/Pulse voltax/signals.py:58-114
+
+`local_jacobian` forms each device's ``(T+K) x (T+K)`` block of
+``cf * d(I,F)/du + cq * d(Q,P)/du`` by forward-mode AD, one seed per local
+unknown, as voltax/sparse.py:200-249 does with ``jax.jvp``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+F64 = torch.float64
+
+
+def _np(x):
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().to(F64)
+    return torch.as_tensor(np.asarray(x, dtype=np.float64))
+
+
+def _inst(x, b):
+    """Instance `b` of a parameter that may carry a leading instance axis."""
+    x = _np(x)
+    return x[b] if x.ndim == 2 else x
+
+
+def softplus(x):
+    return torch.logaddexp(x, torch.zeros_like(x))
+
+
+def signal_value(sig, t, b):
+    """Waveform value per device (voltax/signals.py:58-114)."""
+    name = type(sig).__name__
+    g = lambda f: _inst(getattr(sig, f), b)  # noqa: E731
+    t = torch.as_tensor(t, dtype=F64)
+    if name == "Constant":
+        return g("value")
+    if name == "Step":
+        v0, v1, delay, rise = g("v0"), g("v1"), g("delay"), g("rise")
+        frac = torch.clamp((t - delay) / rise, 0.0, 1.0)
+        return v0 + (v1 - v0) * frac
+    if name == "Pulse":
+        v1, v2, delay = g("v1"), g("v2"), g("delay")
+        rise, fall, width, period = g("rise"), g("fall"), g("width"), g("period")
+        tc = torch.remainder(t - delay, period)
+        up = torch.clamp(tc / (rise + 1e-30), 0.0, 1.0)
+        t_fall_end = rise + width + fall
+        down = torch.clamp((t_fall_end - tc) / (fall + 1e-30), 0.0, 1.0)
+        value = v1 + (v2 - v1) * torch.minimum(up, down)
+        return torch.where(t < delay, v1, value)
+    raise NotImplementedError(name)
+
+
+class GroupModel:
+    """One element group of one circuit instance."""
+
+    def __init__(self, el, b: int = 0):
+        self.el, self.b = el, b
+        self.name = type(el).__name__
+        self.T = len(el.terminals)
+        self.K = el.n_internal
+        self.has_charges = self.name in ("Capacitor", "EKVMOSFET")
+
+    # ---------------------------------------------------------------- physics
+    def currents(self, v, x, t):
+        el, b, name = self.el, self.b, self.name
+        if name == "Resistor":
+            i = (v[..., 0] - v[..., 1]) * torch.exp(-_inst(el.log_r, b))
+            return torch.stack([i, -i], -1), None
+        if name == "Conductance":
+            th = _inst(el.theta, b)
+            if el.transform == "log":
+                g = torch.exp(th)
+            elif el.transform == "softplus":
+                g = el.g_min + softplus(th)
+            elif el.transform == "sigmoid":
+                g = el.g_min + (el.g_max - el.g_min) * torch.sigmoid(th)
+            else:
+                g = th
+            i = g * (v[..., 0] - v[..., 1])
+            return torch.stack([i, -i], -1), None
+        if name == "Capacitor":
+            return None, None
+        if name == "VoltageSource":
+            i = x[..., 0]
+            val = signal_value(el.value, t, b)
+            return torch.stack([i, -i], -1), ((v[..., 0] - v[..., 1]) - val)[..., None]
+        if name == "CurrentSource":
+            i = torch.broadcast_to(signal_value(el.value, t, b), v.shape[:1])
+            return torch.stack([i, -i], -1), None
+        if name == "EKVMOSFET":
+            s = self._sign()
+            vd, vg, vs, vb = (s * v[..., k] for k in range(4))
+            ids = self._drain_current(vd, vg, vs, vb)
+            zero = torch.zeros_like(ids)
+            return s * torch.stack([ids, zero, -ids, zero], -1), None
+        raise NotImplementedError(name)
+
+    def charges(self, v, x):
+        el, b, name = self.el, self.b, self.name
+        if name == "Capacitor":
+            q = torch.exp(_inst(el.log_c, b)) * (v[..., 0] - v[..., 1])
+            return torch.stack([q, -q], -1), None
+        if name == "EKVMOSFET":
+            p = el.process
+            s = self._sign()
+            vd, vg, vs, vb = (s * v[..., k] for k in range(4))
+            i_f, i_r = self._inversion(vd, vg, vs, vb)
+            xf, xr = torch.sqrt(0.25 + i_f), torch.sqrt(0.25 + i_r)
+            w, l = torch.exp(_inst(el.log_w, b)), torch.exp(_inst(el.log_l, b))
+            cox, n, vt = torch.exp(_np(p.log_cox)), _np(p.n), _np(p.vt)
+            c_ox = cox * w * l
+            scale = c_ox * n * vt
+            ssum = xf + xr
+            q_d = -scale * ((4 / 15) * (3 * xr**3 + 6 * xr**2 * xf + 4 * xr * xf**2
+                                        + 2 * xf**3) / ssum**2 - 0.5)
+            q_s = -scale * ((4 / 15) * (3 * xf**3 + 6 * xf**2 * xr + 4 * xf * xr**2
+                                        + 2 * xr**3) / ssum**2 - 0.5)
+            q_i = q_d + q_s
+            q_b = -(n - 1) / n * (c_ox * (vg - vb) + q_i)
+            q_g = -(q_i + q_b)
+            intrinsic = torch.stack([q_d, q_g, q_s, q_b], -1)
+            cov = torch.exp(_np(p.log_cov)) * w
+            q_gs, q_gd = cov * (vg - vs), cov * (vg - vd)
+            overlap = torch.stack([-q_gd, q_gs + q_gd, -q_gs, torch.zeros_like(q_gs)], -1)
+            return s * (intrinsic + overlap), None
+        return None, None
+
+    def _sign(self):
+        return 1.0 if self.el.polarity == "n" else -1.0
+
+    def _inversion(self, vd, vg, vs, vb):
+        el, b = self.el, self.b
+        p = el.process
+        vth, n, vt = _np(p.vth), _np(p.n), _np(p.vt)
+        vp = (vg - vb - vth - _inst(el.dvth, b)) / n
+        i_f = softplus((vp - (vs - vb)) / (2 * vt)) ** 2
+        i_r = softplus((vp - (vd - vb)) / (2 * vt)) ** 2
+        return i_f, i_r
+
+    def _drain_current(self, vd, vg, vs, vb):
+        el, b = self.el, self.b
+        p = el.process
+        i_f, i_r = self._inversion(vd, vg, vs, vb)
+        w, l = torch.exp(_inst(el.log_w, b)), torch.exp(_inst(el.log_l, b))
+        n, vt, lam = _np(p.n), _np(p.vt), _np(p.lam)
+        i_spec = 2 * n * torch.exp(_np(p.log_kp)) * (w / l) * vt**2
+        vds = vd - vs
+        soft_abs = torch.sqrt(vds * vds + 1e-3 * 1e-3) - 1e-3
+        return i_spec * (i_f - i_r) * (1.0 + lam * soft_abs)
+
+    # ------------------------------------------------------------ local blocks
+    def outputs(self, u, t, cf, cq):
+        """``cf * currents + cq * charges`` of all devices, ``u`` (N, T+K)."""
+        n, T, k = u.shape[0], self.T, self.K
+
+        def part(A, B):
+            A = torch.zeros((n, T), dtype=F64) if A is None else torch.broadcast_to(A, (n, T))
+            B = torch.zeros((n, k), dtype=F64) if (B is None or k == 0) else B
+            return torch.cat([A, B], 1)
+
+        v, x = u[:, :T], u[:, T:]
+        out = torch.zeros((n, T + k), dtype=F64)
+        if cf != 0:
+            out = out + cf * part(*self.currents(v, x, t))
+        if cq != 0:
+            out = out + cq * part(*self.charges(v, x))
+        return out
+
+    def local_jacobian(self, u, t, cf, cq):
+        """``(N, m, m)`` blocks ``d out[d, i] / d u[d, j]`` by forward-mode AD
+        (one seed per local unknown, all devices at once)."""
+        n, m = u.shape
+        cols = []
+        for j in range(m):
+            seed = torch.zeros((n, m), dtype=F64)
+            seed[:, j] = 1.0
+            _, tan = torch.func.jvp(lambda uu: self.outputs(uu, t, cf, cq), (u,), (seed,))
+            cols.append(tan)
+        return torch.stack(cols, -1)  # (N, out i, in j)
