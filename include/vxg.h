@@ -1,0 +1,241 @@
+/*
+ * vxg.h -- C ABI of the GB300 (sm_103a) Newton inner loop for voltax circuits.
+ *
+ * Plain C types only: host descriptors hold host pointers, every array an
+ * entry point reads or writes at call time is a caller-owned DEVICE buffer,
+ * `stream` is a cudaStream_t passed as void*. Every call returns an int
+ * status (VXG_OK = 0); no C++ exception crosses this boundary. A handle may
+ * be used from several threads at once when each thread passes its own
+ * stream and its own workspace.
+ *
+ * Batches: `batch` instances share one topology. Per-instance arrays are
+ * instance-major with the strides given in each comment (S = state size,
+ * nnz = pattern entries, work = panel length of the handle). A topology may
+ * itself hold `n_seg` independent sub-circuits (an uneven batch concatenated
+ * into one block-diagonal system); Newton convergence, damping and gmin are
+ * then per segment. Instance index of (b, s) = b * n_seg + s.
+ */
+#ifndef VXG_H
+#define VXG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------ */
+enum {
+  VXG_OK = 0,
+  VXG_ERR_INVALID = 1,   /* bad argument or descriptor                      */
+  VXG_ERR_CUDA = 2,      /* a CUDA runtime call failed (see vxg_last_error) */
+  VXG_ERR_TOO_LARGE = 3, /* a supernode exceeds the shared-memory kernels   */
+  VXG_ERR_ALLOC = 4      /* vxg_create could not allocate its tables        */
+};
+
+/* ---- per-instance Newton status bits (written to `status`) ------------- */
+enum {
+  VXG_ST_CONVERGED = 1, /* |dz| <= atol + rtol |z|, undamped, finite    */
+  VXG_ST_NONFINITE = 2, /* the iterate or the factorization went non-finite */
+  VXG_ST_MAXITER = 4    /* the iteration limit was reached              */
+};
+
+/* ---- numeric formats of the factorization ------------------------------ */
+enum {
+  VXG_F64 = 0, /* plain form: FP64 panels, FP64 solves                       */
+  VXG_F32 = 1  /* chosen form: FP32 panels and solves + FP64 refinement     */
+};
+
+/* ---- device kinds (kernel parameter rows in brackets) ------------------ */
+enum {
+  VXG_KIND_CONDUCTANCE = 0, /* Resistor / Conductance    [g]                    */
+  VXG_KIND_CAPACITOR = 1,   /* Capacitor                 [c]                    */
+  VXG_KIND_VSOURCE = 2,     /* VoltageSource             [waveform rows]        */
+  VXG_KIND_ISOURCE = 3,     /* CurrentSource             [waveform rows]        */
+  VXG_KIND_EKV = 4          /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w] */
+};
+enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
+
+/* ---- Newton residual forms --------------------------------------------- */
+enum {
+  VXG_MODE_DC = 0,   /* f(z,t) + gmin v                                   */
+  VXG_MODE_BE = 1,   /* (q(z) - q(z_prev))/h + f(z,t) + gmin v            */
+  VXG_MODE_TRAP = 2  /* (q(z) - q(z_prev))/h + (f(z,t) + f(z_prev,t_prev))/2 + gmin v */
+};
+
+#define VXG_MAX_GROUPS 32
+
+/* One element group (voltax/circuit.py:30-159 layout, voltax/element.py:66-131). */
+typedef struct {
+  int32_t kind, n, T, K; /* device kind, devices, terminals, internals per device */
+  int32_t wave;          /* VXG_WAVE_* for sources, else -1                       */
+  int32_t n_params;      /* parameter rows the kernel reads                        */
+  int32_t int_offset;    /* state index of device 0's first internal unknown       */
+  const int32_t* nodes;  /* host (n*T) node indices, -1 = ground                   */
+} vxg_group_desc;
+
+/* Topology + symbolic plan, all host arrays (copied by vxg_create).
+ * Replaces the Structure/Plan objects of voltax/sparse.py:73-133, 381-535. */
+typedef struct {
+  int32_t size, n_nodes; /* S, number of node voltages (first entries of z) */
+  int64_t nnz;
+  const int64_t* indptr;  /* S+1 */
+  const int32_t* indices; /* nnz, sorted within rows */
+  const int32_t* rows;    /* nnz, row of each entry */
+  const int64_t* tptr;    /* S+1, column-major view of the pattern ... */
+  const int64_t* tent;    /* nnz, ... entry ids per column (ascending) */
+  const int64_t* diag;    /* S, entry id of each diagonal */
+  int32_t n_groups;
+  const vxg_group_desc* groups;
+  /* stamping: canonical-order gathers of device contributions */
+  int64_t n_res_slots;    /* sum over groups of n*(T+K) */
+  const int64_t* res_ptr; /* S+1 */
+  const int64_t* res_src; /* slot ids, ascending within each row */
+  int64_t n_jac_slots;    /* sum over groups of n*(T+K)^2 */
+  const int64_t* jac_ptr; /* nnz+1 */
+  const int64_t* jac_src; /* slot ids, ascending within each entry */
+  /* independent sub-circuits (segments) inside the topology */
+  int32_t n_seg;
+  const int32_t* seg_ptr;  /* n_seg+1 unknown offsets */
+  const int32_t* seg_of;   /* S: segment of each unknown */
+  /* supernodes: unpadded panels F11 (k*k) | F12 (k*r) | F21 (r*k) */
+  int32_t n_sn;
+  const int32_t* sn_k;
+  const int32_t* sn_r;
+  const int64_t* sn_panel;    /* panel offset of F11 */
+  const int64_t* sn_piv_ptr;  /* n_sn+1 into sn_piv */
+  const int32_t* sn_piv;      /* pivot unknowns of each supernode (sorted) */
+  const int64_t* sn_bord_ptr; /* n_sn+1 into sn_bord */
+  const int32_t* sn_bord;     /* border unknowns of each supernode (sorted) */
+  int64_t work;               /* panel length */
+  const int64_t* a_pos;       /* nnz: panel slot of each pattern entry */
+  /* elimination levels */
+  int32_t n_levels;
+  const int64_t* lv_ptr;     /* n_levels+1 into lv_sn */
+  const int32_t* lv_sn;      /* supernodes of each level */
+  const int64_t* lv_schur_off; /* per lv_sn entry: offset of its r*r block */
+  const int64_t* lv_bord_off;  /* per lv_sn entry: offset of its r contributions */
+  const int64_t* lv_schur_len; /* n_levels */
+  const int64_t* lv_bord_len;  /* n_levels */
+  const int64_t* lv_st_ptr;  /* n_levels+1 into schur targets */
+  const int64_t* st_tgt;     /* panel slots receiving Schur updates */
+  const int64_t* st_ptr;     /* (#targets + 1) into st_src */
+  const int64_t* st_src;     /* level-scratch indices, ascending */
+  const int64_t* lv_bt_ptr;  /* n_levels+1 into border targets */
+  const int32_t* bt_tgt;     /* unknowns receiving border updates */
+  const int64_t* bt_ptr;     /* (#targets + 1) into bt_src */
+  const int64_t* bt_src;     /* level border-contribution indices, ascending */
+} vxg_topology_desc;
+
+/* Parameter rows of one group for one call (device memory). Row p of
+ * instance b, device d is params[p*row_stride + b*batch_stride + d]. */
+typedef struct {
+  const double* params;
+  int64_t row_stride;
+  int64_t batch_stride; /* 0: shared by all instances */
+} vxg_group_params;
+
+typedef struct {
+  int32_t max_steps;  /* Newton iterations (voltax Options.max_steps)   */
+  double rtol, atol;  /* convergence test                                */
+  double max_dv;      /* damping: largest node-voltage update            */
+  int32_t precision;  /* VXG_F64 or VXG_F32                              */
+  int32_t refine;     /* FP64 refinement sweeps per solve (VXG_F32)     */
+} vxg_newton_opts;
+
+typedef struct vxg_handle vxg_handle;
+
+/* Last CUDA error text of this thread (static storage). */
+const char* vxg_last_error(void);
+
+/* Upload a topology + plan. Replaces voltax's host-side Structure/Plan
+ * caching (voltax/sparse.py:150-193, 412-535); the symbolic analysis itself
+ * runs on the host before this call. */
+int vxg_create(const vxg_topology_desc* desc, vxg_handle** out);
+int vxg_destroy(vxg_handle* h);
+
+/* Bytes of caller-owned scratch for `batch` instances at `precision`. */
+int vxg_workspace_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes);
+/* Bytes of a factor buffer (panels of all instances) at `precision`. */
+int vxg_factor_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes);
+
+/* Device evaluation and stamping at state z (B x S) and time t:
+ *   f_out (B x S) = f(z, t), q_out (B x S) = q(z)        (either may be NULL)
+ *   data_out (B x nnz) = cf df/dz + cq dq/dz + gmin on node diagonals (or NULL)
+ * gmin: device array (B*n_seg) or NULL for the scalar gmin_scalar.
+ * Replaces Circuit.f/q (voltax/circuit.py:196-226), sparse.jacobian
+ * (voltax/sparse.py:220-249) and _add_gmin (voltax/analysis.py:359-360). */
+int vxg_eval(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+             const double* z, double t, double cf, double cq, const double* gmin,
+             double gmin_scalar, double* f_out, double* q_out, double* data_out,
+             void* workspace, void* stream);
+
+/* Numeric refactorization of data (B x nnz, FP64) under the plan into
+ * factors (vxg_factor_size bytes): per supernode W = F11^-1 (Gauss-Jordan
+ * with partial pivoting inside the block), Ub = W F12, Lb = F21 W, Schur
+ * updates of ancestors in a fixed order. Replaces sparse.factor
+ * (voltax/sparse.py:543-572). */
+int vxg_factor(const vxg_handle* h, int32_t batch, int32_t precision, const double* data,
+               void* factors, void* workspace, void* stream);
+
+/* x = A^-1 b (or A^-T b) with factors from vxg_factor; b, x are B x S FP64
+ * (may alias). With VXG_F32 and data != NULL, `refine` FP64 refinement sweeps
+ * r = b - A x follow the first solve. Replaces sparse.solve
+ * (voltax/sparse.py:575-595). */
+int vxg_solve(const vxg_handle* h, int32_t batch, int32_t precision, const void* factors,
+              const double* data, const double* b, double* x, int32_t transpose,
+              int32_t refine, void* workspace, void* stream);
+
+/* y = A x (transpose: A^T x), FP64, B x S. Structure.matvec (voltax/sparse.py:130-133). */
+int vxg_spmv(const vxg_handle* h, int32_t batch, const double* data, const double* x,
+             double* y, int32_t transpose, void* stream);
+
+/* gdata = -g[rows] * x[indices] (B x nnz): the data cotangent of spsolve
+ * (voltax/sparse.py:614-618). */
+int vxg_spsolve_gdata(const vxg_handle* h, int32_t batch, const double* g, const double* x,
+                      double* gdata, void* stream);
+
+/* One damped Newton solve per instance (voltax/analysis.py:208-233) with the
+ * residual of `mode` (voltax/analysis.py:333-378). z (B x S) holds the guess
+ * and receives the result; z_prev (B x S) and t_prev are read for BE/TRAP.
+ * converged, iters (B*n_seg int32) are written. Instances that converge are
+ * frozen while others iterate (vmap semantics). If factors != NULL the
+ * factors of the final Jacobian, at the returned z, are left there (for the
+ * adjoint). */
+int vxg_newton(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+               int32_t mode, double t, double t_prev, const double* z_prev,
+               const double* gmin, double gmin_scalar, const vxg_newton_opts* opts,
+               double* z, int32_t* converged, int32_t* iters, void* factors,
+               void* workspace, void* stream);
+
+/* vxg_newton restricted to the instances with mask[i] != 0 (B*n_seg int32,
+ * device); the others keep z, converged and iters untouched. Used for gmin
+ * stepping of a batch, where only the instances that failed the direct
+ * attempt continue (voltax/analysis.py:236-266 under jax.vmap). */
+int vxg_newton_masked(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                      int32_t mode, double t, double t_prev, const double* z_prev,
+                      const double* gmin, double gmin_scalar, const vxg_newton_opts* opts,
+                      double* z, int32_t* converged, int32_t* iters, const int32_t* mask,
+                      void* workspace, void* stream);
+
+/* Fused transient: for n_t time points ts (host), starting from z0 (B x S),
+ * one vxg_newton per step with guess z_prev (voltax/analysis.py:434-480).
+ * z_out: n_t x B x S (row 0 = z0); converged, iters: n_t x B*n_seg. */
+int vxg_transient(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                  int32_t mode, int32_t n_t, const double* ts, const double* z0,
+                  double gmin_scalar, const vxg_newton_opts* opts, double* z_out,
+                  int32_t* converged, int32_t* iters, void* workspace, void* stream);
+
+/* Parameter VJP of the residual: for each group g and parameter row p,
+ * grads[g][p*row_stride + b*batch_stride + d] += -sum_i lam[i] d r_i/d param
+ * with r = cf f(z,t) + cq q(z) (voltax/analysis.py:282-288, the
+ * eqx.filter_vjp of the residual). grads has the layout of params. */
+int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                  const double* z, double t, double cf, double cq, const double* lam,
+                  double* const* grads, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VXG_H */

@@ -1,0 +1,246 @@
+"""GPU parity against the CPU oracle, through the C ABI.
+
+* stamping: f, q and the CSR Jacobian equal the oracle; bit for bit on
+  linear circuits (same device values, same canonical summation order), to
+  1e-12 relative on EKV circuits (analytic vs forward-mode derivatives), and
+  bitwise reproducible run to run (voltax tests/test_sparse.py:174-189);
+* factor/solve: real and transposed solves equal dense LAPACK for plans with
+  leaf 1, 2 and 16, in FP64 and in FP32 + FP64 refinement
+  (voltax tests/test_sparse.py:208-230);
+* analyses: DC and transient node voltages within 1e-9 relative of the
+  oracle, the same convergence flags and the same Newton iteration counts
+  (voltax tests/test_sparse.py:264-295);
+* adjoints: spsolve and dc gradients equal dense / finite differences
+  (voltax tests/test_sparse.py:245-261, 336-353).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from oracle import analysis as oa  # noqa: E402
+from oracle import stamp as ost  # noqa: E402
+import voltax_gb300 as vx  # noqa: E402
+from voltax_gb300 import sparse, symbolic, workloads  # noqa: E402
+from voltax_gb300.builder import CircuitBuilder  # noqa: E402
+from voltax_gb300.library import cmos  # noqa: E402
+
+
+def rc_ladder(R1=1e3, R2=2e3, C1=1e-9, C2=0.5e-9, Rload=1e4):
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.resistor("in", "a", R1, name="R1")
+    b.resistor("a", "out", R2, name="R2")
+    b.resistor("out", "0", Rload, name="Rload")
+    b.capacitor("a", "0", C1, name="C1")
+    b.capacitor("out", "0", C2, name="C2")
+    return b.build()
+
+
+CIRCUITS = {
+    "rc_ladder": rc_ladder,
+    "grid": lambda: workloads.power_grid(10, seed=3),
+    "adder": lambda: workloads.mirror_adder(2),
+    "ring": lambda: workloads.ring_oscillator(9)[0],
+}
+LINEAR = ("rc_ladder", "grid")
+
+
+def rel(a, b, floor=1e-3):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if a.size else 0.0
+
+
+@pytest.mark.parametrize("name", list(CIRCUITS))
+def test_stamping_matches_oracle(name):
+    c = CIRCUITS[name]()
+    st = symbolic.structure(c)
+    z = np.random.default_rng(0).uniform(-0.5, 1.5, c.size)
+    t = 0.3e-9
+    zt = torch.as_tensor(z)
+    f_gpu = c.f(zt, t).cpu().numpy()
+    q_gpu = c.q(zt).cpu().numpy()
+    f_ref, q_ref = ost.f(c, z, t), ost.q(c, z)
+    for cf, cq in ((1.0, 0.0), (0.0, 1.0), (0.5, 1e9)):
+        J = sparse.jacobian(c, zt, t, cf, cq, structure=st).cpu().numpy()
+        J2 = sparse.jacobian(c, zt, t, cf, cq, structure=st).cpu().numpy()
+        J_ref = ost.jacobian(c, st, z, t, cf, cq)
+        assert np.array_equal(J, J2), "stamping is not bitwise reproducible"
+        if name in LINEAR:
+            assert np.array_equal(J, J_ref), "linear stamps differ from the canonical sum"
+        else:
+            scale = np.abs(J_ref).max()
+            np.testing.assert_allclose(J, J_ref, rtol=1e-12, atol=1e-14 * scale)
+    if name in LINEAR:
+        assert np.array_equal(f_gpu, f_ref) and np.array_equal(q_gpu, q_ref)
+    else:
+        np.testing.assert_allclose(f_gpu, f_ref, rtol=1e-12, atol=1e-15 * np.abs(f_ref).max())
+        np.testing.assert_allclose(q_gpu, q_ref, rtol=1e-12, atol=1e-15 * np.abs(q_ref).max())
+
+
+@pytest.mark.parametrize("name,leaf", [("grid", 1), ("grid", 16), ("adder", 1),
+                                       ("adder", 16), ("ring", 2), ("rc_ladder", 16)])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_factor_solve_matches_dense(name, leaf, precision):
+    c = CIRCUITS[name]()
+    st = symbolic.structure(c)
+    plan = symbolic.make_plan(st, leaf)
+    z = np.random.default_rng(0).uniform(-0.5, 1.5, c.size)
+    G = ost.add_gmin(ost.jacobian(c, st, z, 0.0), st, c.n_nodes, 1e-12)
+    C = ost.jacobian(c, st, z, 0.0, 0.0, 1.0)
+    rhs = np.random.default_rng(1).standard_normal(c.size)
+    for A in (G, G + C / 1e-9):
+        dense = st.to_scipy(A).toarray()
+        fac = sparse.factor(plan, torch.as_tensor(A), precision)
+        for tr in (False, True):
+            x = sparse.solve(plan, fac, torch.as_tensor(rhs), tr).cpu().numpy()
+            ref = np.linalg.solve(dense.T if tr else dense, rhs)
+            np.testing.assert_allclose(x, ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+
+
+def _oracle_dc(c):
+    st = symbolic.structure(c)
+    return oa.dc(oa.System(c, st, st.plan))
+
+
+@pytest.mark.parametrize("name", ["rc_ladder", "grid", "adder"])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_dc_matches_oracle(name, precision):
+    c = CIRCUITS[name]()
+    sol = vx.dc(c, options=vx.Options(precision=precision))
+    z_ref, ok_ref, it_ref = _oracle_dc(c)
+    assert bool(sol.converged) == ok_ref
+    assert rel(sol.z.cpu().numpy(), z_ref) < 1e-9
+    if precision == "f64":
+        assert int(sol.iterations) == it_ref
+
+
+def test_cmos_full_adder_needs_gmin_stepping():
+    """voltax tests/test_analysis.py:138-149 on the GPU."""
+    b = CircuitBuilder()
+    b.vsource("vdd", "0", 1.2)
+    for n in ["a", "c"]:
+        b.vsource(n, "0", 0.0)
+    cmos.full_adder(b, "a", "c", "0", "s", "co", "vdd")
+    c = b.build()
+    plain = vx.dc(c, options=vx.Options(gmin_steps=0))
+    rescued = vx.dc(c)
+    assert not bool(plain.converged)
+    assert bool(rescued.converged)
+    z_ref, ok_ref, it_ref = _oracle_dc(c)
+    assert ok_ref and rel(rescued.z.cpu().numpy(), z_ref) < 1e-9
+    assert float(rescued.v("s")) < 0.01 and float(rescued.v("co")) < 0.01
+
+
+def test_singular_circuit_fails_check():
+    b = CircuitBuilder()
+    b.vsource("a", "0", 1.0)
+    b.vsource("a", "0", 2.0)
+    b.resistor("a", "0", 1e3)
+    with pytest.raises(RuntimeError, match="did not converge"):
+        vx.dc(b.build()).check()
+
+
+@pytest.mark.parametrize("method", ["be", "trap"])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_ring_transient_matches_oracle(method, precision):
+    c, nodes = workloads.ring_oscillator(9)
+    z0 = workloads.ring_initial_state(c, nodes)
+    ts = np.linspace(0.0, 60e-12, 31)
+    sol = vx.transient(c, ts, ic=z0, method=method, options=vx.Options(precision=precision))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic=z0.numpy(), method=method)
+    assert bool(sol.converged.all()) and okr.all()
+    v, vr = sol.z.cpu().numpy(), zr
+    assert np.max(np.abs(v[:, : c.n_nodes] - vr[:, : c.n_nodes])) < 1e-9
+    if precision == "f64":
+        assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+def test_rc_ladder_recorded_values_on_gpu():
+    """voltax tests/test_analysis.py:33-39 through the GPU path."""
+    c = rc_ladder()
+    sol = vx.transient(c, np.linspace(0, 1e-5, 101), ic="zero")
+    np.testing.assert_allclose(sol.z[-1].cpu().numpy(),
+                               [1.0, 0.921635241, 0.766714055, -7.83647588e-05], atol=1e-8)
+
+
+def test_batched_mc_matches_per_instance_oracle():
+    c = workloads.mirror_adder_mc(6, seed=1, bits=2)
+    ts = np.linspace(0, 200e-12, 21)
+    sol = vx.transient(c, ts, ic="dc", method="be", options=vx.Options(precision="f32"))
+    assert sol.z.shape == (6, len(ts), c.size)
+    st = symbolic.structure(c)
+    for b in (0, 5):
+        sys_b = oa.System(c, st, st.plan, b)
+        zr, okr, _ = oa.transient(sys_b, ts, ic="dc", method="be")
+        assert okr.all() and bool(sol.converged[b].all())
+        assert np.max(np.abs(sol.z[b].cpu().numpy() - zr)) < 1e-9
+
+
+def test_spsolve_gradients_match_dense():
+    c = workloads.power_grid(6, seed=2)
+    st = symbolic.structure(c)
+    A = ost.add_gmin(ost.jacobian(c, st, np.zeros(c.size), 0.0), st, c.n_nodes, 1e-12)
+    rhs = np.random.default_rng(2).standard_normal(c.size)
+    data = torch.tensor(A, device="cuda", requires_grad=True)
+    b = torch.tensor(rhs, device="cuda", requires_grad=True)
+    x = sparse.spsolve(st, data, b)
+    torch.sin(x).sum().backward()
+    dense = torch.tensor(st.to_scipy(A).toarray(), requires_grad=True)
+    bd = torch.tensor(rhs, requires_grad=True)
+    xd = torch.linalg.solve(dense, bd)
+    torch.sin(xd).sum().backward()
+    rows, cols = torch.as_tensor(st.rows), torch.as_tensor(st.indices)
+    np.testing.assert_allclose(data.grad.cpu().numpy(), dense.grad[rows, cols].numpy(),
+                               rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(b.grad.cpu().numpy(), bd.grad.numpy(), rtol=1e-7)
+
+
+def test_dc_gradient_of_power_grid_matches_finite_differences():
+    """voltax tests/test_sparse.py:336-353: d v(worst) / d log r."""
+    c = workloads.power_grid(8, seed=4)
+    el = c.elements["Resistor"]
+    log_r = el.log_r.clone().requires_grad_(True)
+    el2 = el.with_nodes(el.nodes)
+    el2.log_r = log_r
+    c2 = c.replace("Resistor", el2)
+    sol = vx.dc(c2)
+    worst = int(torch.argmin(sol.v().detach()))
+    sol.z[worst].backward()
+    g = log_r.grad.numpy()
+    k = int(np.argmax(np.abs(g)))
+    eps = 1e-5
+
+    def v_at(delta):
+        e3 = el.with_nodes(el.nodes)
+        lr = el.log_r.clone()
+        lr[k] += delta
+        e3.log_r = lr
+        return float(vx.dc(c.replace("Resistor", e3)).z[worst])
+
+    fd = (v_at(eps) - v_at(-eps)) / (2 * eps)
+    assert np.isclose(g[k], fd, rtol=1e-6)
+    # and against the oracle adjoint lam = J^-T e_worst, dv/dlog_r = -lam^T dF/dlog_r
+    st = symbolic.structure(c)
+    sys_o = oa.System(c, st, st.plan)
+    z_ref, _, _ = oa.dc(sys_o)
+    e = np.zeros(c.size)
+    e[worst] = 1.0
+    lam = oa.dc_adjoint(sys_o, z_ref, e)
+    nodes = el.node_array()
+    v = np.concatenate([z_ref, [0.0]])
+    lv = np.concatenate([lam, [0.0]])
+    dv = v[nodes[:, 0]] - v[nodes[:, 1]]
+    gref = -(lv[nodes[:, 0]] - lv[nodes[:, 1]]) * dv * (-np.exp(-el.log_r.numpy()))
+    np.testing.assert_allclose(g, gref, rtol=1e-8, atol=1e-12 * np.abs(gref).max())
+
+
+def test_f32_refined_matches_f64_on_power_grid():
+    c = workloads.power_grid(40, seed=7)
+    s64 = vx.dc(c, options=vx.Options(precision="f64"))
+    s32 = vx.dc(c, options=vx.Options(precision="f32"))
+    assert bool(s64.converged) and bool(s32.converged)
+    assert rel(s32.z.cpu().numpy(), s64.z.cpu().numpy()) < 1e-9

@@ -1,0 +1,300 @@
+"""Drop-in for ``voltax.dc`` / ``voltax.transient`` on the GPU
+(voltax/analysis.py).
+
+`dc` runs damped Newton with the gmin-stepping fallback
+(voltax/analysis.py:208-266, 410-431); `transient` runs backward Euler or
+trapezoidal steps, each a Newton solve warm-started from the previous state
+(voltax/analysis.py:434-480). The Newton loop, stamping, refactorization and
+solves run in ``libvxg.so``; this module only sequences the gmin stages and
+packs arguments.
+
+Differentiation: `dc` is differentiable in every element parameter (torch
+autograd). The backward pass is the implicit-function adjoint of
+voltax/analysis.py:282-288 -- one transposed solve ``J^T lam = g`` at the
+root, then the parameter VJP ``-lam^T dF/dp`` on the GPU -- and it reuses the
+factors of the Jacobian at the returned root instead of re-forming them.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .runtime import engine_for, stream_ptr
+from .symbolic import structure
+
+SPARSE_THRESHOLD = 200
+
+
+@dataclass(frozen=True)
+class Options:
+    """Newton settings (voltax/analysis.py:50-89) plus the factorization
+    format: ``precision="f64"`` is the plain FP64 form; ``"f32"`` factors in
+    FP32 and recovers FP64 accuracy with `refine` refinement sweeps against
+    the FP64 residual. `solver` is accepted for compatibility: every solve
+    uses the supernodal GPU factorization (a circuit of at most ``2 * leaf``
+    unknowns is one dense supernode)."""
+
+    max_steps: int = 100
+    rtol: float = 1e-6
+    atol: float = 1e-9
+    max_dv: float = 1.0
+    gmin: float = 1e-12
+    gmin_steps: int = 10
+    gmin_start: float = 1e-2
+    direct_steps: int = 25
+    solver: str = "auto"
+    sparse_threshold: int = SPARSE_THRESHOLD
+    precision: str = "f64"
+    refine: int = 2
+
+    def __post_init__(self):
+        if self.solver not in ("auto", "dense", "sparse"):
+            raise ValueError("solver must be 'auto', 'dense' or 'sparse', "
+                             f"got {self.solver!r}")
+        if self.precision not in ("f64", "f32"):
+            raise ValueError(f"precision must be 'f64' or 'f32', got {self.precision!r}")
+
+    def native(self, max_steps: int | None = None) -> L.NewtonOpts:
+        return L.NewtonOpts(self.max_steps if max_steps is None else max_steps, self.rtol,
+                            self.atol, self.max_dv,
+                            L.VXG_F32 if self.precision == "f32" else L.VXG_F64,
+                            self.refine)
+
+
+class Solution:
+    """Result of `dc` or `transient` (voltax/analysis.py:92-139).
+
+    ``z``: ``(S,)`` / ``(T, S)`` for one circuit, ``(B, S)`` / ``(B, T, S)``
+    for a batch of B instances; ``converged`` and ``iterations`` likewise
+    without the state axis.
+    """
+
+    def __init__(self, t, z, converged, layout, iterations=None):
+        self.t, self.z, self.converged, self.layout = t, z, converged, layout
+        self.iterations = iterations
+
+    def v(self, node: str | None = None):
+        if node is None:
+            return self.z[..., : self.layout.n_nodes]
+        idx = self.layout.node(node)
+        return torch.zeros(self.z.shape[:-1], dtype=self.z.dtype,
+                           device=self.z.device) if idx < 0 else self.z[..., idx]
+
+    def i(self, device: str, which: str | None = None):
+        return self.z[..., self.layout.internal(device, which)]
+
+    def check(self) -> "Solution":
+        bad = ~(self.converged.bool() & torch.all(torch.isfinite(self.z), dim=-1))
+        if bool(torch.any(bad)):
+            where = ""
+            if bad.ndim and torch.is_tensor(self.t) and self.t.ndim:
+                flat = bad.reshape(-1, bad.shape[-1]).any(0) if bad.ndim > 1 else bad
+                where = f" at t={float(self.t[int(torch.argmax(flat.int()))])}"
+            raise RuntimeError(
+                f"Newton did not converge{where}. Common causes: a node without "
+                "a DC path to ground, a loop of voltage sources/inductors, or "
+                "time steps too coarse for an edge (see docs: Analyses).")
+        return self
+
+    def __getitem__(self, name: str):
+        if "." in name:
+            device, which = name.rsplit(".", 1)
+            return self.i(device, which)
+        return self.v(name)
+
+
+# =============================================================================
+# Newton through the C ABI
+# =============================================================================
+
+
+class _Call:
+    """Arguments shared by the native Newton calls of one analysis."""
+
+    def __init__(self, circuit, options: Options):
+        self.c, self.o = circuit, options
+        self.st = structure(circuit)
+        self.eng = engine_for(self.st, circuit)
+        self.B = circuit.batch
+        self.params, self.keep, self.rows = self.eng.pack_params(circuit, self.B)
+        self.prec = L.VXG_F32 if options.precision == "f32" else L.VXG_F64
+        self.ws = self.eng.workspace(self.B, self.prec)
+        self.n_inst = self.B * self.eng.n_seg
+        dev = self.eng.device
+        self.conv = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
+        self.iters = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
+
+    def newton(self, mode, z, t, t_prev=0.0, z_prev=None, gmin=None, max_steps=None,
+               mask=None, factors=None):
+        o = self.o.native(max_steps)
+        gmin_t = None
+        gmin_s = self.o.gmin
+        if torch.is_tensor(gmin):
+            gmin_t = gmin.to(self.eng.device, torch.float64).contiguous()
+        elif gmin is not None:
+            gmin_s = float(gmin)
+        args = (self.eng.handle, self.B, self.params, mode, float(t), float(t_prev),
+                None if z_prev is None else z_prev.data_ptr(),
+                None if gmin_t is None else gmin_t.data_ptr(), gmin_s, C.byref(o),
+                z.data_ptr(), self.conv.data_ptr(), self.iters.data_ptr())
+        if mask is None:
+            L.check(self.eng.lib.vxg_newton(*args, None if factors is None else
+                                            factors.data_ptr(), self.ws.data_ptr(),
+                                            stream_ptr()), "vxg_newton")
+        else:
+            L.check(self.eng.lib.vxg_newton_masked(*args, mask.data_ptr(), self.ws.data_ptr(),
+                                                   stream_ptr()), "vxg_newton_masked")
+        return self.conv.clone(), self.iters.clone()
+
+
+def _gmin_stepping(call: _Call, t, guess: torch.Tensor, factors=None):
+    """voltax/analysis.py:236-266 for a batch: instances that fail the
+    direct attempt run the gmin stages; the others stay frozen."""
+    o = call.o
+    z = guess.clone()
+    conv, iters = call.newton(L.VXG_MODE_DC, z, t, gmin=o.gmin,
+                              max_steps=o.direct_steps if o.gmin_steps else None)
+    total = iters.clone()
+    if o.gmin_steps and not bool(conv.all()):
+        failed = (conv == 0).to(torch.int32)
+        seg_of = torch.as_tensor(call.eng.tables.seg_of, device=z.device, dtype=torch.long)
+        restart = failed.bool().reshape(call.B, -1)[:, seg_of]  # (B, S) per unknown
+        z = torch.where(restart, guess, z).contiguous()
+        gmins = np.concatenate([[o.gmin], np.logspace(np.log10(o.gmin_start),
+                                                      np.log10(o.gmin), o.gmin_steps)])
+        for k in range(1, o.gmin_steps + 1):
+            conv_k, it_k = call.newton(L.VXG_MODE_DC, z, t, gmin=gmins[k], mask=failed)
+            total = total + torch.where(failed.bool(), it_k, torch.zeros_like(it_k))
+            conv = torch.where(failed.bool(), conv_k, conv)
+    data = None
+    if factors is not None:  # factors of J at the returned root (adjoint)
+        data = _refactor(call, z, t, factors)
+    return z, conv, total, data
+
+
+def _refactor(call: _Call, z, t, factors):
+    eng = call.eng
+    data = torch.empty((call.B, eng.nnz), dtype=torch.float64, device=eng.device)
+    L.check(eng.lib.vxg_eval(eng.handle, call.B, call.params, z.data_ptr(), float(t), 1.0, 0.0,
+                             None, call.o.gmin, None, None, data.data_ptr(), call.ws.data_ptr(),
+                             stream_ptr()), "vxg_eval")
+    L.check(eng.lib.vxg_factor(eng.handle, call.B, call.prec, data.data_ptr(),
+                               factors.data_ptr(), call.ws.data_ptr(), stream_ptr()),
+            "vxg_factor")
+    return data
+
+
+class _DCRoot(torch.autograd.Function):
+    """z* = root of f(z, t) + gmin v; backward by the implicit function
+    theorem with the factors at z*."""
+
+    @staticmethod
+    def forward(ctx, call, t, guess, *rows):
+        fac = call.eng.factor_buffer(call.B, call.prec)
+        z, conv, iters, data = _gmin_stepping(call, t, guess, factors=fac)
+        ctx.call, ctx.t, ctx.fac, ctx.data = call, t, fac, data
+        ctx.conv, ctx.iters = conv, iters
+        ctx.save_for_backward(z)
+        ctx.mark_non_differentiable(conv, iters)
+        return z, conv, iters
+
+    @staticmethod
+    def backward(ctx, gz, _gc, _gi):
+        (z,) = ctx.saved_tensors
+        call = ctx.call
+        eng = call.eng
+        gz = gz.contiguous()
+        lam = torch.empty_like(gz)
+        data = ctx.data if call.prec == L.VXG_F32 else None
+        L.check(eng.lib.vxg_solve(eng.handle, call.B, call.prec, ctx.fac.data_ptr(),
+                                  None if data is None else data.data_ptr(), gz.data_ptr(),
+                                  lam.data_ptr(), 1, call.o.refine if data is not None else 0,
+                                  call.ws.data_ptr(), stream_ptr()), "vxg_solve")
+        grads_out = []
+        bufs = []
+        for name, rows in zip(eng.tables.group_names, call.rows):
+            n = call.c.elements[name].size
+            bufs.append(torch.zeros((len(rows), call.B, n), dtype=torch.float64,
+                                    device=eng.device))
+        ptrs = (C.c_void_p * max(len(bufs), 1))(*[b.data_ptr() for b in bufs])
+        L.check(eng.lib.vxg_param_vjp(eng.handle, call.B, call.params, z.data_ptr(),
+                                      float(ctx.t), 1.0, 0.0, lam.data_ptr(), ptrs,
+                                      stream_ptr()), "vxg_param_vjp")
+        for rows, buf in zip(call.rows, bufs):
+            for r, row in enumerate(rows):
+                g = buf[r]
+                grads_out.append(g.sum(0) if row.ndim == 1 else g)
+        return (None, None, None, *grads_out)
+
+
+def _flat_rows(call):
+    return [row for rows in call.rows for row in rows]
+
+
+def dc(circuit, t: float = 0.0, guess=None, options: Options = Options()) -> Solution:
+    """DC operating point: ``f(z, t) + gmin v = 0`` (voltax/analysis.py:410-431).
+
+    Differentiable in the circuit's parameters (torch autograd)."""
+    call = _Call(circuit, options)
+    S, B = call.eng.S, call.B
+    if guess is None:
+        g = torch.zeros((B, S), dtype=torch.float64, device=call.eng.device)
+    else:
+        g = torch.as_tensor(guess, dtype=torch.float64, device=call.eng.device)
+        g = g.reshape(-1, S).expand(B, S).contiguous()
+    rows = _flat_rows(call)
+    if any(r.requires_grad for r in rows):
+        z, conv, iters = _DCRoot.apply(call, float(t), g, *rows)
+    else:
+        z, conv, iters, _ = _gmin_stepping(call, float(t), g)
+    single = circuit.batch == 1
+    shape = (call.eng.n_seg,) if call.eng.n_seg > 1 else ()
+    conv = conv.reshape(B, *shape).bool()
+    iters = iters.reshape(B, *shape)
+    if single:
+        z, conv, iters = z[0], conv[0], iters[0]
+    return Solution(torch.as_tensor(t, dtype=torch.float64), z, conv, circuit.layout, iters)
+
+
+def transient(circuit, ts, ic="dc", method: str = "be",
+              options: Options = Options()) -> Solution:
+    """Transient analysis on the time grid `ts` (voltax/analysis.py:434-480)."""
+    if method not in ("be", "trap"):
+        raise ValueError(f"method must be 'be' or 'trap', got {method!r}")
+    ts_np = np.ascontiguousarray(np.asarray(ts, dtype=np.float64))
+    call = _Call(circuit, options)
+    S, B = call.eng.S, call.B
+    dev = call.eng.device
+    if isinstance(ic, Solution):
+        z0 = ic.z
+    elif isinstance(ic, str):
+        if ic == "dc":
+            z0 = dc(circuit, float(ts_np[0]), options=options).z
+        elif ic == "zero":
+            z0 = torch.zeros((B, S), dtype=torch.float64, device=dev)
+        else:
+            raise ValueError(f"ic must be 'dc', 'zero' or an array, got {ic!r}")
+    else:
+        z0 = torch.as_tensor(ic, dtype=torch.float64)
+    z0 = torch.as_tensor(z0, dtype=torch.float64, device=dev).detach()
+    z0 = z0.reshape(-1, S).expand(B, S).contiguous()
+    T = len(ts_np)
+    n_inst = call.n_inst
+    z_out = torch.empty((T, B, S), dtype=torch.float64, device=dev)
+    conv = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
+    iters = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
+    mode = L.VXG_MODE_BE if method == "be" else L.VXG_MODE_TRAP
+    o = options.native()
+    L.check(call.eng.lib.vxg_transient(
+        call.eng.handle, B, call.params, mode, T, ts_np.ctypes.data_as(L.PF64), z0.data_ptr(),
+        options.gmin, C.byref(o), z_out.data_ptr(), conv.data_ptr(), iters.data_ptr(),
+        call.ws.data_ptr(), stream_ptr()), "vxg_transient")
+    tt = torch.as_tensor(ts_np)
+    if circuit.batch == 1:
+        return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])
+    return Solution(tt, z_out.permute(1, 0, 2), conv.T.bool(), circuit.layout, iters.T)

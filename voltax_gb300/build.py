@@ -1,0 +1,64 @@
+"""Build ``libvxg.so`` (the CUDA kernels + C ABI) in-tree for sm_103a.
+
+Plain nvcc, one translation unit per source compiled in parallel, then one
+link; no torch, no cmake. Output: ``voltax_gb300/_lib/libvxg.so``.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "csrc"
+OUT = HERE / "_lib"
+INCLUDE = HERE.parent / "include"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["stamp.cu", "factor.cu", "solve.cu", "newton.cu", "capi.cu", "fused.cu"]
+
+
+def nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    path = Path(cuda) / "bin" / "nvcc"
+    return str(path) if path.exists() else "nvcc"
+
+
+def flags(extra=()) -> list[str]:
+    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{SRC}", *extra]
+
+
+def _compile(name: str, extra) -> Path:
+    src = SRC / name
+    obj = OUT / (src.stem + ".o")
+    deps = [src, *SRC.glob("*.cuh"), INCLUDE / "vxg.h"]
+    if obj.exists() and obj.stat().st_mtime > max(d.stat().st_mtime for d in deps):
+        return obj
+    cmd = [nvcc(), *flags(extra), "-c", str(src), "-o", str(obj)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {name}:\n{res.stdout}\n{res.stderr}")
+    return obj
+
+
+def build(verbose: bool = False, extra=()) -> Path:
+    OUT.mkdir(exist_ok=True)
+    lib = OUT / "libvxg.so"
+    sources = [s for s in SOURCES if (SRC / s).exists()]
+    with cf.ThreadPoolExecutor(max_workers=len(sources)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra), sources))
+    if not lib.exists() or lib.stat().st_mtime < max(o.stat().st_mtime for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    if verbose:
+        print(lib)
+    return lib
+
+
+if __name__ == "__main__":
+    build(verbose=True, extra=sys.argv[1:])

@@ -1,0 +1,495 @@
+// C ABI: handle management, workspace layout and the Newton / transient
+// drivers (host code). No exception crosses this boundary.
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace vxg {
+
+int launch_compose(const Topo& t, int B, int mode, double h, const double* z, const double* f,
+                   const double* q, const double* fp, const double* qp, const double* gmin,
+                   double gmin_scalar, double* rhs, cudaStream_t s);
+int launch_newton_init(int n, const int* mask, int* active, int* converged, int* iters,
+                       cudaStream_t s);
+int launch_update(const Topo& t, int B, double* z, const double* dz, int* active,
+                  int* converged, int* iters, double max_dv, double rtol, double atol,
+                  int* n_active, cudaStream_t s);
+int launch_param_vjp(const Topo& t, const GroupTable& gt, int B, const double* z, double t_now,
+                     double cf, double cq, const double* lam, double* const* grads,
+                     cudaStream_t s);
+
+static thread_local char g_err[256] = "";
+
+void set_error(cudaError_t e) {
+  std::snprintf(g_err, sizeof(g_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+size_t elem_size(int precision) { return precision == VXG_F32 ? sizeof(float) : sizeof(double); }
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Workspace regions for `B` instances.
+struct Layout {
+  size_t cf, cq, cj, f, q, fp, qp, rhs, dz, data, r64, fac, scratch, xt, active, cnt, total;
+};
+
+static Layout layout(const Topo& t, int B, int precision) {
+  Layout L;
+  const size_t es = elem_size(precision);
+  const size_t nS = (size_t)B * t.S;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o = align_up(o + bytes);
+    return at;
+  };
+  L.cf = take(sizeof(double) * (size_t)B * t.n_res_slots);
+  L.cq = take(sizeof(double) * (size_t)B * t.n_res_slots);
+  L.cj = take(sizeof(double) * (size_t)B * t.n_jac_slots);
+  L.f = take(sizeof(double) * nS);
+  L.q = take(sizeof(double) * nS);
+  L.fp = take(sizeof(double) * nS);
+  L.qp = take(sizeof(double) * nS);
+  L.rhs = take(sizeof(double) * nS);
+  L.dz = take(sizeof(double) * nS);
+  L.data = take(sizeof(double) * (size_t)B * t.nnz);
+  L.r64 = take(sizeof(double) * 2 * nS);
+  L.fac = take(es * (size_t)B * t.work);
+  L.scratch = take(es * (size_t)B * std::max<long long>(std::max(t.max_schur, t.max_bord), 1));
+  L.xt = take(es * nS);
+  L.active = take(sizeof(int) * (size_t)B * t.n_seg);
+  L.cnt = take(sizeof(int) * 4);
+  L.total = o;
+  return L;
+}
+
+template <typename P>
+static P* at(void* base, size_t off) {
+  return reinterpret_cast<P*>(static_cast<char*>(base) + off);
+}
+
+GroupTable make_table(const Topo& t, const vxg_group_params* params) {
+  GroupTable gt;
+  std::memset(&gt, 0, sizeof(gt));
+  gt.n_groups = t.n_groups;
+  long long dev = 0, res = 0, jac = 0;
+  for (int i = 0; i < t.n_groups; ++i) {
+    const vxg_group_desc& d = t.groups[i];
+    GroupDev& g = gt.g[i];
+    g.kind = d.kind;
+    g.n = d.n;
+    g.T = d.T;
+    g.K = d.K;
+    g.m = d.T + d.K;
+    g.wave = d.wave;
+    g.n_params = d.n_params;
+    g.int_offset = d.int_offset;
+    g.dev_base = dev;
+    g.res_base = res;
+    g.jac_base = jac;
+    g.nodes = t.group_nodes[i];
+    if (params) {
+      g.params = params[i].params;
+      g.row_stride = params[i].row_stride;
+      g.batch_stride = params[i].batch_stride;
+    }
+    dev += d.n;
+    res += (long long)d.n * g.m;
+    jac += (long long)d.n * g.m * g.m;
+  }
+  gt.n_dev = dev;
+  return gt;
+}
+
+template <typename X, typename Y>
+static int upload(X** dst, const Y* src, size_t n) {
+  static_assert(sizeof(X) == sizeof(Y), "element size mismatch");
+  *dst = nullptr;
+  const size_t bytes = sizeof(X) * std::max<size_t>(n, 1);
+  cudaError_t e = cudaMalloc((void**)dst, bytes);
+  if (e != cudaSuccess) {
+    set_error(e);
+    return VXG_ERR_ALLOC;
+  }
+  if (n && src) {
+    e = cudaMemcpy(*dst, src, sizeof(X) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      set_error(e);
+      return VXG_ERR_CUDA;
+    }
+  } else {
+    cudaMemset(*dst, 0, bytes);
+  }
+  return VXG_OK;
+}
+
+static void free_topo(Topo& t) {
+  void* ptrs[] = {t.indptr, t.tptr, t.tent, t.diag, t.indices, t.rows, t.res_ptr, t.res_src,
+                  t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
+                  t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
+                  t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
+                  t.d_flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < t.n_groups; ++i)
+    if (t.group_nodes[i]) cudaFree(t.group_nodes[i]);
+  if (t.h_flag) cudaFreeHost(t.h_flag);
+  delete[] t.h_lv_ptr;
+  delete[] t.h_lv_schur_len;
+  delete[] t.h_lv_bord_len;
+  delete[] t.h_lv_st_ptr;
+  delete[] t.h_lv_bt_ptr;
+  delete[] t.h_lv_kmax;
+  delete[] t.h_lv_rmax;
+}
+
+}  // namespace vxg
+
+using namespace vxg;
+
+extern "C" {
+
+const char* vxg_last_error(void) { return g_err; }
+
+int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
+  if (!d || !out || d->size <= 0 || d->n_groups < 0 || d->n_groups > VXG_MAX_GROUPS ||
+      d->n_seg <= 0 || d->n_levels < 0)
+    return VXG_ERR_INVALID;
+  *out = nullptr;
+  vxg_handle* h = new (std::nothrow) vxg_handle;
+  if (!h) return VXG_ERR_ALLOC;
+  std::memset(&h->t, 0, sizeof(Topo));
+  Topo& t = h->t;
+  t.S = d->size;
+  t.nv = d->n_nodes;
+  t.nnz = d->nnz;
+  t.n_groups = d->n_groups;
+  t.n_res_slots = d->n_res_slots;
+  t.n_jac_slots = d->n_jac_slots;
+  t.n_seg = d->n_seg;
+  t.n_sn = d->n_sn;
+  t.work = d->work;
+  t.n_levels = d->n_levels;
+  int st = VXG_OK;
+#define UP(field, src, n) \
+  if (st == VXG_OK) st = upload(&t.field, src, (size_t)(n))
+  const long long S = d->size, nnz = d->nnz;
+  UP(indptr, d->indptr, S + 1);
+  UP(indices, d->indices, nnz);
+  UP(rows, d->rows, nnz);
+  UP(tptr, d->tptr, S + 1);
+  UP(tent, d->tent, nnz);
+  UP(diag, d->diag, S);
+  UP(res_ptr, d->res_ptr, S + 1);
+  UP(res_src, d->res_src, d->res_ptr[S]);
+  UP(jac_ptr, d->jac_ptr, nnz + 1);
+  UP(jac_src, d->jac_src, d->jac_ptr[nnz]);
+  UP(seg_ptr, d->seg_ptr, d->n_seg + 1);
+  UP(seg_of, d->seg_of, S);
+  UP(sn_k, d->sn_k, d->n_sn);
+  UP(sn_r, d->sn_r, d->n_sn);
+  UP(sn_panel, d->sn_panel, d->n_sn);
+  UP(sn_piv_ptr, d->sn_piv_ptr, d->n_sn + 1);
+  UP(sn_piv, d->sn_piv, d->sn_piv_ptr[d->n_sn]);
+  UP(sn_bord_ptr, d->sn_bord_ptr, d->n_sn + 1);
+  UP(sn_bord, d->sn_bord, d->sn_bord_ptr[d->n_sn]);
+  UP(a_pos, d->a_pos, nnz);
+  const long long nl = d->n_levels;
+  const long long n_lv_sn = d->lv_ptr[nl];
+  UP(lv_sn, d->lv_sn, n_lv_sn);
+  UP(lv_schur_off, d->lv_schur_off, n_lv_sn);
+  UP(lv_bord_off, d->lv_bord_off, n_lv_sn);
+  const long long nst = d->lv_st_ptr[nl], nbt = d->lv_bt_ptr[nl];
+  UP(st_tgt, d->st_tgt, nst);
+  UP(st_ptr, d->st_ptr, nst + 1);
+  UP(st_src, d->st_src, d->st_ptr[nst]);
+  UP(bt_tgt, d->bt_tgt, nbt);
+  UP(bt_ptr, d->bt_ptr, nbt + 1);
+  UP(bt_src, d->bt_src, d->bt_ptr[nbt]);
+  UP(d_flag, (const int*)nullptr, 4);
+  for (int i = 0; i < d->n_groups && st == VXG_OK; ++i) {
+    t.groups[i] = d->groups[i];
+    st = upload(&t.group_nodes[i], d->groups[i].nodes, (size_t)d->groups[i].n * d->groups[i].T);
+  }
+#undef UP
+  if (st == VXG_OK) {
+    t.h_lv_ptr = new long long[nl + 1];
+    t.h_lv_schur_len = new long long[nl + 1];
+    t.h_lv_bord_len = new long long[nl + 1];
+    t.h_lv_st_ptr = new long long[nl + 1];
+    t.h_lv_bt_ptr = new long long[nl + 1];
+    t.h_lv_kmax = new int[nl + 1];
+    t.h_lv_rmax = new int[nl + 1];
+    t.max_schur = t.max_bord = 0;
+    t.kmax = t.rmax = 0;
+    for (long long L = 0; L <= nl; ++L) {
+      t.h_lv_ptr[L] = d->lv_ptr[L];
+      t.h_lv_st_ptr[L] = d->lv_st_ptr[L];
+      t.h_lv_bt_ptr[L] = d->lv_bt_ptr[L];
+      t.h_lv_kmax[L] = t.h_lv_rmax[L] = 0;
+      if (L < nl) {
+        t.h_lv_schur_len[L] = d->lv_schur_len[L];
+        t.h_lv_bord_len[L] = d->lv_bord_len[L];
+        t.max_schur = std::max(t.max_schur, (long long)d->lv_schur_len[L]);
+        t.max_bord = std::max(t.max_bord, (long long)d->lv_bord_len[L]);
+        for (long long p = d->lv_ptr[L]; p < d->lv_ptr[L + 1]; ++p) {
+          const int j = d->lv_sn[p];
+          t.h_lv_kmax[L] = std::max(t.h_lv_kmax[L], d->sn_k[j]);
+          t.h_lv_rmax[L] = std::max(t.h_lv_rmax[L], d->sn_r[j]);
+        }
+        t.kmax = std::max(t.kmax, t.h_lv_kmax[L]);
+        t.rmax = std::max(t.rmax, t.h_lv_rmax[L]);
+      }
+    }
+    cudaError_t e = cudaMallocHost((void**)&t.h_flag, sizeof(int) * 4);
+    if (e != cudaSuccess) {
+      set_error(e);
+      st = VXG_ERR_ALLOC;
+    }
+  }
+  if (st != VXG_OK) {
+    free_topo(t);
+    delete h;
+    return st;
+  }
+  *out = h;
+  return VXG_OK;
+}
+
+int vxg_destroy(vxg_handle* h) {
+  if (!h) return VXG_ERR_INVALID;
+  free_topo(h->t);
+  delete h;
+  return VXG_OK;
+}
+
+int vxg_workspace_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes) {
+  if (!h || !bytes || batch <= 0 || (precision != VXG_F64 && precision != VXG_F32))
+    return VXG_ERR_INVALID;
+  *bytes = layout(h->t, batch, precision).total;
+  return VXG_OK;
+}
+
+int vxg_factor_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes) {
+  if (!h || !bytes || batch <= 0 || (precision != VXG_F64 && precision != VXG_F32))
+    return VXG_ERR_INVALID;
+  *bytes = elem_size(precision) * (size_t)batch * h->t.work;
+  return VXG_OK;
+}
+
+int vxg_eval(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+             const double* z, double t_now, double cf, double cq, const double* gmin,
+             double gmin_scalar, double* f_out, double* q_out, double* data_out,
+             void* workspace, void* stream) {
+  if (!h || batch <= 0 || !params || !z || !workspace) return VXG_ERR_INVALID;
+  const Topo& t = h->t;
+  cudaStream_t s = (cudaStream_t)stream;
+  Layout L = layout(t, batch, VXG_F64);
+  GroupTable gt = make_table(t, params);
+  double* cfb = at<double>(workspace, L.cf);
+  double* cqb = at<double>(workspace, L.cq);
+  double* cjb = at<double>(workspace, L.cj);
+  int st = launch_eval(t, gt, batch, z, t_now, cf, cq, f_out != nullptr, q_out != nullptr,
+                       data_out != nullptr, cfb, cqb, cjb, s);
+  if (st) return st;
+  return launch_gather(t, batch, cfb, cqb, cjb, gmin, gmin_scalar, f_out, q_out, data_out, s);
+}
+
+int vxg_factor(const vxg_handle* h, int32_t batch, int32_t precision, const double* data,
+               void* factors, void* workspace, void* stream) {
+  if (!h || batch <= 0 || !data || !factors || !workspace) return VXG_ERR_INVALID;
+  if (precision != VXG_F64 && precision != VXG_F32) return VXG_ERR_INVALID;
+  Layout L = layout(h->t, batch, precision);
+  return launch_factor(h->t, batch, precision, data, factors,
+                       at<void>(workspace, L.scratch), (cudaStream_t)stream);
+}
+
+int vxg_solve(const vxg_handle* h, int32_t batch, int32_t precision, const void* factors,
+              const double* data, const double* b, double* x, int32_t transpose,
+              int32_t refine, void* workspace, void* stream) {
+  if (!h || batch <= 0 || !factors || !b || !x || !workspace || refine < 0)
+    return VXG_ERR_INVALID;
+  if (precision != VXG_F64 && precision != VXG_F32) return VXG_ERR_INVALID;
+  Layout L = layout(h->t, batch, precision);
+  return launch_solve(h->t, batch, precision, factors, data, b, x, transpose, refine,
+                      at<void>(workspace, L.xt), at<void>(workspace, L.scratch),
+                      at<double>(workspace, L.r64), (cudaStream_t)stream);
+}
+
+int vxg_spmv(const vxg_handle* h, int32_t batch, const double* data, const double* x,
+             double* y, int32_t transpose, void* stream) {
+  if (!h || batch <= 0 || !data || !x || !y) return VXG_ERR_INVALID;
+  return launch_spmv(h->t, batch, data, x, y, transpose, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace vxg {
+__global__ void gdata_kernel(int B, long long nnz, int S, const int* __restrict__ rows,
+                             const int* __restrict__ indices, const double* __restrict__ g,
+                             const double* __restrict__ x, double* __restrict__ gd) {
+  long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gid >= (long long)B * nnz) return;
+  const int b = (int)(gid / nnz);
+  const long long e = gid - (long long)b * nnz;
+  gd[gid] = -g[(long long)b * S + rows[e]] * x[(long long)b * S + indices[e]];
+}
+
+static int newton_core(const vxg_handle* h, int B, const vxg_group_params* params, int mode,
+                       double t_now, double t_prev, const double* z_prev, const double* gmin,
+                       double gmin_scalar, const vxg_newton_opts* o, double* z,
+                       int* converged, int* iters, void* factors_out, void* ws,
+                       const int* mask, cudaStream_t s) {
+  const Topo& t = h->t;
+  const int prec = o->precision;
+  Layout L = layout(t, B, prec);
+  GroupTable gt = make_table(t, params);
+  double* cfb = at<double>(ws, L.cf);
+  double* cqb = at<double>(ws, L.cq);
+  double* cjb = at<double>(ws, L.cj);
+  double* f = at<double>(ws, L.f);
+  double* q = at<double>(ws, L.q);
+  double* fp = at<double>(ws, L.fp);
+  double* qp = at<double>(ws, L.qp);
+  double* rhs = at<double>(ws, L.rhs);
+  double* dz = at<double>(ws, L.dz);
+  double* data = at<double>(ws, L.data);
+  void* fac = at<void>(ws, L.fac);
+  void* scratch = at<void>(ws, L.scratch);
+  void* xt = at<void>(ws, L.xt);
+  double* r64 = at<double>(ws, L.r64);
+  int* active = at<int>(ws, L.active);
+  int* cnt = t.d_flag;
+  const int ninst = B * t.n_seg;
+  int st = launch_newton_init(ninst, mask, active, converged, iters, s);
+  if (st) return st;
+  const bool dc = mode == VXG_MODE_DC;
+  const double cf = mode == VXG_MODE_TRAP ? 0.5 : 1.0;
+  const double cq = dc ? 0.0 : 1.0 / (t_now - t_prev);
+  const double hstep = t_now - t_prev;
+  if (!dc) {
+    st = launch_eval(t, gt, B, z_prev, t_prev, 1.0, 0.0, mode == VXG_MODE_TRAP, true, false,
+                     cfb, cqb, cjb, s);
+    if (st) return st;
+    st = launch_gather(t, B, cfb, cqb, cjb, nullptr, 0.0, mode == VXG_MODE_TRAP ? fp : nullptr,
+                       qp, nullptr, s);
+    if (st) return st;
+  }
+  for (int it = 0; it < o->max_steps; ++it) {
+    st = launch_eval(t, gt, B, z, t_now, cf, cq, true, !dc, true, cfb, cqb, cjb, s);
+    if (st) return st;
+    st = launch_gather(t, B, cfb, cqb, cjb, gmin, gmin_scalar, f, dc ? nullptr : q, data, s);
+    if (st) return st;
+    st = launch_compose(t, B, mode, hstep, z, f, q, fp, qp, gmin, gmin_scalar, rhs, s);
+    if (st) return st;
+    st = launch_factor(t, B, prec, data, fac, scratch, s);
+    if (st) return st;
+    st = launch_solve(t, B, prec, fac, data, rhs, dz, 0, prec == VXG_F32 ? o->refine : 0, xt,
+                      scratch, r64, s);
+    if (st) return st;
+    VXG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int), s));
+    st = launch_update(t, B, z, dz, active, converged, iters, o->max_dv, o->rtol, o->atol, cnt,
+                       s);
+    if (st) return st;
+    VXG_CUDA_TRY(cudaMemcpyAsync(t.h_flag, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    VXG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (t.h_flag[0] == 0) break;
+  }
+  if (factors_out) {  // factors of the Jacobian at the returned state (adjoint)
+    st = launch_eval(t, gt, B, z, t_now, cf, cq, false, false, true, cfb, cqb, cjb, s);
+    if (st) return st;
+    st = launch_gather(t, B, cfb, cqb, cjb, gmin, gmin_scalar, nullptr, nullptr, data, s);
+    if (st) return st;
+    st = launch_factor(t, B, prec, data, factors_out, scratch, s);
+    if (st) return st;
+  }
+  return VXG_OK;
+}
+
+}  // namespace vxg
+
+extern "C" {
+
+int vxg_spsolve_gdata(const vxg_handle* h, int32_t batch, const double* g, const double* x,
+                      double* gdata, void* stream) {
+  if (!h || batch <= 0 || !g || !x || !gdata) return VXG_ERR_INVALID;
+  const long long n = (long long)batch * h->t.nnz;
+  if (!n) return VXG_OK;
+  gdata_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      batch, h->t.nnz, h->t.S, h->t.rows, h->t.indices, g, x, gdata);
+  VXG_CUDA_TRY(cudaGetLastError());
+  return VXG_OK;
+}
+
+static bool opts_ok(const vxg_newton_opts* o) {
+  return o && o->max_steps >= 0 && (o->precision == VXG_F64 || o->precision == VXG_F32) &&
+         o->refine >= 0;
+}
+
+int vxg_newton(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+               int32_t mode, double t_now, double t_prev, const double* z_prev,
+               const double* gmin, double gmin_scalar, const vxg_newton_opts* opts, double* z,
+               int32_t* converged, int32_t* iters, void* factors, void* workspace,
+               void* stream) {
+  if (!h || batch <= 0 || !params || !z || !converged || !iters || !workspace ||
+      !opts_ok(opts) || mode < 0 || mode > 2 || (mode != VXG_MODE_DC && !z_prev))
+    return VXG_ERR_INVALID;
+  return newton_core(h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts, z,
+                     converged, iters, factors, workspace, nullptr, (cudaStream_t)stream);
+}
+
+int vxg_newton_masked(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                      int32_t mode, double t_now, double t_prev, const double* z_prev,
+                      const double* gmin, double gmin_scalar, const vxg_newton_opts* opts,
+                      double* z, int32_t* converged, int32_t* iters, const int32_t* mask,
+                      void* workspace, void* stream) {
+  if (!h || batch <= 0 || !params || !z || !converged || !iters || !workspace ||
+      !opts_ok(opts) || mode < 0 || mode > 2 || (mode != VXG_MODE_DC && !z_prev))
+    return VXG_ERR_INVALID;
+  return newton_core(h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts, z,
+                     converged, iters, nullptr, workspace, mask, (cudaStream_t)stream);
+}
+
+int vxg_transient(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                  int32_t mode, int32_t n_t, const double* ts, const double* z0,
+                  double gmin_scalar, const vxg_newton_opts* opts, double* z_out,
+                  int32_t* converged, int32_t* iters, void* workspace, void* stream) {
+  if (!h || batch <= 0 || !params || n_t <= 0 || !ts || !z0 || !z_out || !converged ||
+      !iters || !workspace || !opts_ok(opts) || (mode != VXG_MODE_BE && mode != VXG_MODE_TRAP))
+    return VXG_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nS = (size_t)batch * h->t.S;
+  const int ninst = batch * h->t.n_seg;
+  VXG_CUDA_TRY(cudaMemcpyAsync(z_out, z0, sizeof(double) * nS, cudaMemcpyDeviceToDevice, s));
+  std::vector<int> ones(ninst, 1), zeros(ninst, 0);
+  VXG_CUDA_TRY(cudaMemcpyAsync(converged, ones.data(), sizeof(int) * ninst,
+                               cudaMemcpyHostToDevice, s));
+  VXG_CUDA_TRY(cudaMemcpyAsync(iters, zeros.data(), sizeof(int) * ninst,
+                               cudaMemcpyHostToDevice, s));
+  for (int n = 1; n < n_t; ++n) {
+    double* prev = z_out + (size_t)(n - 1) * nS;
+    double* cur = z_out + (size_t)n * nS;
+    VXG_CUDA_TRY(cudaMemcpyAsync(cur, prev, sizeof(double) * nS, cudaMemcpyDeviceToDevice, s));
+    int st = newton_core(h, batch, params, mode, ts[n], ts[n - 1], prev, nullptr, gmin_scalar,
+                         opts, cur, converged + (size_t)n * ninst, iters + (size_t)n * ninst,
+                         nullptr, workspace, nullptr, s);
+    if (st) return st;
+  }
+  VXG_CUDA_TRY(cudaStreamSynchronize(s));
+  return VXG_OK;
+}
+
+int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                  const double* z, double t_now, double cf, double cq, const double* lam,
+                  double* const* grads, void* stream) {
+  if (!h || batch <= 0 || !params || !z || !lam || !grads) return VXG_ERR_INVALID;
+  GroupTable gt = make_table(h->t, params);
+  return launch_param_vjp(h->t, gt, batch, z, t_now, cf, cq, lam, grads, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,249 @@
+// Supernodal block-LDU refactorization under a fixed plan.
+//
+// Panels: every supernode j owns F11 (k x k) | F12 (k x r) | F21 (r x k),
+// row-major and unpadded. One launch per elimination level; one CTA per
+// (supernode of the level, instance). A CTA keeps F11 in shared memory and
+//   1. inverts it by Gauss-Jordan with partial pivoting inside the block
+//      (voltax/sparse.py:543-546 uses LAPACK LU + inverse: same W up to
+//      rounding), writing W over F11;
+//   2. Ub = W F12 over F12 (column tiles staged in shared memory);
+//   3. the Schur block S = F21 Ub into the level scratch (r x r);
+//   4. Lb = F21 W over F21 (row tiles staged in shared memory).
+// A second launch applies the level's Schur blocks to the ancestors' panels:
+// one thread per target slot sums its sources in ascending order
+// (deterministic, no atomics): work[t] -= sum(S[src]).
+// (voltax/sparse.py:549-572)
+
+#include "internal.cuh"
+
+namespace vxg {
+
+constexpr int kTile = 32;
+
+template <typename T>
+__global__ void fill_panels_kernel(int B, long long nnz, const long long* __restrict__ a_pos,
+                                   const double* __restrict__ data, T* __restrict__ work,
+                                   long long work_stride) {
+  long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gid >= (long long)B * nnz) return;
+  const int b = (int)(gid / nnz);
+  const long long e = gid - (long long)b * nnz;
+  work[(long long)b * work_stride + a_pos[e]] = (T)data[gid];
+}
+
+template <typename T>
+__device__ __forceinline__ T tabs(T x) {
+  return x < T(0) ? -x : x;
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT)
+    factor_level_kernel(const int* __restrict__ lv_sn, const long long* __restrict__ schur_off,
+                        const int* __restrict__ sn_k, const int* __restrict__ sn_r,
+                        const long long* __restrict__ sn_panel, T* __restrict__ work,
+                        long long work_stride, T* __restrict__ scratch,
+                        long long scratch_stride) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j = lv_sn[blockIdx.x];
+  const int b = blockIdx.y;
+  const int k = sn_k[j], r = sn_r[j];
+  T* F11 = work + (long long)b * work_stride + sn_panel[j];
+  T* F12 = F11 + (long long)k * k;
+  T* F21 = F12 + (long long)k * r;
+  T* Sout = scratch + (long long)b * scratch_stride + schur_off[blockIdx.x];
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* A = reinterpret_cast<T*>(smem_raw);  // k*k
+  T* col = A + k * k;                     // k
+  T* tA = col + k;                        // kTile*k
+  T* tB = tA + kTile * k;                 // k*kTile
+  int* perm = reinterpret_cast<int*>(tB + k * kTile);
+  __shared__ int s_piv;
+
+  for (int i = threadIdx.x; i < k * k; i += NT) A[i] = F11[i];
+  __syncthreads();
+
+  // ---- Gauss-Jordan inverse with partial pivoting (row swaps recorded)
+  for (int c = 0; c < k; ++c) {
+    if (warp == 0) {
+      T best = T(-1);
+      int bi = c;
+      for (int i = c + lane; i < k; i += 32) {
+        const T v = tabs(A[i * k + c]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        s_piv = bi;
+        perm[c] = bi;
+      }
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p != c)
+      for (int jj = threadIdx.x; jj < k; jj += NT) {
+        const T tmp = A[p * k + jj];
+        A[p * k + jj] = A[c * k + jj];
+        A[c * k + jj] = tmp;
+      }
+    __syncthreads();
+    const T d = A[c * k + c];
+    for (int i = threadIdx.x; i < k; i += NT) col[i] = (i == c) ? T(0) : A[i * k + c];
+    __syncthreads();
+    for (int jj = threadIdx.x; jj < k; jj += NT)
+      A[c * k + jj] = ((jj == c) ? T(1) : A[c * k + jj]) / d;
+    __syncthreads();
+    for (int i = warp; i < k; i += NW) {
+      if (i == c) continue;
+      const T f = col[i];
+      for (int jj = lane; jj < k; jj += 32) {
+        const T a = (jj == c) ? T(0) : A[i * k + jj];
+        A[i * k + jj] = a - f * A[c * k + jj];
+      }
+    }
+    __syncthreads();
+  }
+  for (int c = k - 1; c >= 0; --c) {
+    const int p = perm[c];
+    if (p != c)
+      for (int i = threadIdx.x; i < k; i += NT) {
+        const T tmp = A[i * k + c];
+        A[i * k + c] = A[i * k + p];
+        A[i * k + p] = tmp;
+      }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < k * k; i += NT) F11[i] = A[i];
+  if (r == 0) return;
+
+  // ---- Ub = W F12 (in place, column tiles)
+  for (int c0 = 0; c0 < r; c0 += kTile) {
+    const int tw = min(kTile, r - c0);
+    for (int i = warp; i < k; i += NW)
+      for (int jj = lane; jj < tw; jj += 32) tB[i * kTile + jj] = F12[(long long)i * r + c0 + jj];
+    __syncthreads();
+    for (int i = warp; i < k; i += NW)
+      for (int jj = lane; jj < tw; jj += 32) {
+        T acc = T(0);
+        for (int l = 0; l < k; ++l) acc += A[i * k + l] * tB[l * kTile + jj];
+        F12[(long long)i * r + c0 + jj] = acc;
+      }
+    __syncthreads();
+  }
+
+  // ---- per row tile of F21: Schur rows S = F21 Ub, then Lb = F21 W
+  for (int a0 = 0; a0 < r; a0 += kTile) {
+    const int tr = min(kTile, r - a0);
+    for (int a = warp; a < tr; a += NW)
+      for (int l = lane; l < k; l += 32) tA[a * k + l] = F21[(long long)(a0 + a) * k + l];
+    __syncthreads();
+    for (int c0 = 0; c0 < r; c0 += kTile) {
+      const int tw = min(kTile, r - c0);
+      for (int i = warp; i < k; i += NW)
+        for (int jj = lane; jj < tw; jj += 32)
+          tB[i * kTile + jj] = F12[(long long)i * r + c0 + jj];
+      __syncthreads();
+      for (int a = warp; a < tr; a += NW)
+        for (int jj = lane; jj < tw; jj += 32) {
+          T acc = T(0);
+          for (int l = 0; l < k; ++l) acc += tA[a * k + l] * tB[l * kTile + jj];
+          Sout[(long long)(a0 + a) * r + c0 + jj] = acc;
+        }
+      __syncthreads();
+    }
+    for (int a = warp; a < tr; a += NW)
+      for (int jj = lane; jj < k; jj += 32) {
+        T acc = T(0);
+        for (int l = 0; l < k; ++l) acc += tA[a * k + l] * A[l * k + jj];
+        F21[(long long)(a0 + a) * k + jj] = acc;
+      }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void schur_apply_kernel(int B, long long ntgt, const long long* __restrict__ tgt,
+                                   const long long* __restrict__ ptr,
+                                   const long long* __restrict__ src,
+                                   const T* __restrict__ scratch, long long scratch_stride,
+                                   T* __restrict__ work, long long work_stride) {
+  long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gid >= (long long)B * ntgt) return;
+  const int b = (int)(gid / ntgt);
+  const long long t = gid - (long long)b * ntgt;
+  const T* S = scratch + (long long)b * scratch_stride;
+  T acc = T(0);
+  for (long long p = ptr[t]; p < ptr[t + 1]; ++p) acc += S[src[p]];
+  work[(long long)b * work_stride + tgt[t]] -= acc;
+}
+
+size_t factor_smem_bytes(int k, size_t es) {
+  return (size_t)(k * k + k + 2 * kTile * k) * es + (size_t)k * sizeof(int) + 16;
+}
+
+template <typename T>
+static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scratch,
+                       cudaStream_t s) {
+  const long long ws = t.work, ss = t.max_schur;
+  VXG_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(T) * (size_t)B * ws, s));
+  const long long n = (long long)B * t.nnz;
+  if (n)
+    fill_panels_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, t.nnz, t.a_pos, data,
+                                                                        work, ws);
+  VXG_CUDA_TRY(cudaGetLastError());
+  int dev = 0, max_optin = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  for (int L = 0; L < t.n_levels; ++L) {
+    const long long lo = t.h_lv_ptr[L], hi = t.h_lv_ptr[L + 1];
+    if (hi == lo) continue;
+    const int kmax = t.h_lv_kmax[L];
+    const size_t smem = factor_smem_bytes(kmax, sizeof(T));
+    if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+    dim3 grid((unsigned)(hi - lo), (unsigned)B);
+    if (kmax > 48) {
+      auto kern = factor_level_kernel<T, 256>;
+      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+      kern<<<grid, 256, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
+                                   t.sn_panel, work, ws, scratch, ss);
+    } else {
+      auto kern = factor_level_kernel<T, 128>;
+      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+      kern<<<grid, 128, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
+                                   t.sn_panel, work, ws, scratch, ss);
+    }
+    VXG_CUDA_TRY(cudaGetLastError());
+    const long long tlo = t.h_lv_st_ptr[L], thi = t.h_lv_st_ptr[L + 1];
+    const long long nt = (long long)B * (thi - tlo);
+    if (nt) {
+      schur_apply_kernel<T><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(
+          B, thi - tlo, t.st_tgt + tlo, t.st_ptr + tlo, t.st_src, scratch, ss, work, ws);
+      VXG_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  return VXG_OK;
+}
+
+int launch_factor(const Topo& t, int B, int precision, const double* data, void* factors,
+                  void* scratch, cudaStream_t s) {
+  if (precision == VXG_F64)
+    return factor_impl<double>(t, B, data, (double*)factors, (double*)scratch, s);
+  if (precision == VXG_F32)
+    return factor_impl<float>(t, B, data, (float*)factors, (float*)scratch, s);
+  return VXG_ERR_INVALID;
+}
+
+}  // namespace vxg

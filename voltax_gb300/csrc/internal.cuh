@@ -1,0 +1,100 @@
+// Internal types shared by the vxg kernels and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vxg.h"
+
+namespace vxg {
+
+constexpr int kMaxM = 4;  // largest local block (EKV: 4 terminals)
+
+// One group as the kernels see it (passed by value in a GroupTable).
+struct GroupDev {
+  int kind, n, T, K, m, wave, n_params;
+  int int_offset;
+  long long dev_base;  // flattened device index of device 0
+  long long res_base;  // first residual slot (n*m slots per group)
+  long long jac_base;  // first Jacobian slot (n*m*m slots per group)
+  const int* nodes;    // device copy, n*T
+  const double* params;
+  long long row_stride, batch_stride;
+};
+
+struct GroupTable {
+  int n_groups;
+  long long n_dev;  // devices over all groups
+  GroupDev g[VXG_MAX_GROUPS];
+};
+
+// Device-resident copy of a topology + plan.
+struct Topo {
+  int S, nv;
+  long long nnz;
+  long long *indptr, *tptr, *tent, *diag;
+  int *indices, *rows;
+  int n_groups;
+  vxg_group_desc groups[VXG_MAX_GROUPS];  // host copy of the descriptors
+  int* group_nodes[VXG_MAX_GROUPS];       // device node arrays
+  long long n_res_slots, n_jac_slots, n_dev;
+  long long *res_ptr, *res_src, *jac_ptr, *jac_src;
+  int n_seg;
+  int *seg_ptr, *seg_of;
+  int n_sn;
+  int *sn_k, *sn_r, *sn_piv, *sn_bord;
+  long long *sn_panel, *sn_piv_ptr, *sn_bord_ptr, *a_pos;
+  long long work;
+  int n_levels;
+  // level tables (host copies for launch sizes, device copies for kernels)
+  long long *h_lv_ptr, *h_lv_schur_len, *h_lv_bord_len, *h_lv_st_ptr, *h_lv_bt_ptr;
+  int* h_lv_kmax;  // largest k per level
+  int* h_lv_rmax;  // largest r per level
+  int* lv_sn;
+  long long *lv_schur_off, *lv_bord_off;
+  long long *st_tgt, *st_ptr, *st_src;
+  int* bt_tgt;
+  long long *bt_ptr, *bt_src;
+  long long max_schur, max_bord;  // largest per-level scratch
+  int kmax, rmax;
+  // pinned host word for loop control
+  int* h_flag;
+  int* d_flag;
+};
+
+}  // namespace vxg
+
+struct vxg_handle {
+  vxg::Topo t;
+};
+
+#define VXG_CUDA_TRY(expr)                 \
+  do {                                     \
+    cudaError_t _e = (expr);               \
+    if (_e != cudaSuccess) {               \
+      vxg::set_error(_e);                  \
+      return VXG_ERR_CUDA;                 \
+    }                                      \
+  } while (0)
+
+namespace vxg {
+void set_error(cudaError_t e);
+GroupTable make_table(const Topo& t, const vxg_group_params* params);
+
+// ---- launchers (kernels in stamp.cu / factor.cu / solve.cu / newton.cu)
+int launch_eval(const Topo& t, const GroupTable& gt, int B, const double* z, double t_now,
+                double cf, double cq, bool want_f, bool want_q, bool want_j, double* cf_buf,
+                double* cq_buf, double* cj_buf, cudaStream_t s);
+int launch_gather(const Topo& t, int B, const double* cf_buf, const double* cq_buf,
+                  const double* cj_buf, const double* gmin, double gmin_scalar, double* f_out,
+                  double* q_out, double* data_out, cudaStream_t s);
+int launch_factor(const Topo& t, int B, int precision, const double* data, void* factors,
+                  void* scratch, cudaStream_t s);
+int launch_solve(const Topo& t, int B, int precision, const void* factors, const double* data,
+                 const double* b, double* x, int transpose, int refine, void* vec_t,
+                 void* scratch, double* r64, cudaStream_t s);
+int launch_spmv(const Topo& t, int B, const double* data, const double* x, double* y,
+                int transpose, cudaStream_t s);
+
+size_t elem_size(int precision);
+}  // namespace vxg

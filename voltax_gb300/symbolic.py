@@ -300,6 +300,7 @@ class Plan:
     levels: list = field(default_factory=list)
     sn_of: np.ndarray | None = None
     pos_in: np.ndarray | None = None
+    structure: object = None
 
 
 @dataclass(frozen=True, eq=False)
@@ -482,4 +483,4 @@ def make_plan(st: Structure, leaf: int | None = None) -> Plan:
                                  bord_off, int(rr.sum()), b_t, b_p, b_s))
 
     return Plan(S, sns, parents, borders, level, classes, stats, k, r, panel, work,
-                a_pos, levels, sn_of, pos_in)
+                a_pos, levels, sn_of, pos_in, st)
