@@ -1,0 +1,301 @@
+"""Benchmark: batched Newton solves/s on the Monte Carlo mirror-adder workload.
+
+Workload (one "step"): 4096 instances of a 4-bit ripple-carry adder of
+28-transistor mirror full adders (EKV MOSFETs, per-device Vth and log W
+mismatch), A and B stepping 0000 -> 1111 with 20 ps edges; a DC operating
+point and a 501-point backward-Euler transient over 1 ns, i.e. 4096 x 501
+Newton solves (stamp + refactor + solve until converged) per step. Inputs
+are synthetic (seeded), parameters resident in HBM before the timed region
+for ``value``; ``e2e`` goes through the public API from pinned host buffers.
+
+``value`` is the chosen form (FP32 supernodal factors + FP64 refinement);
+``plain_fp64`` is the same workload with FP64 factors, and ``match`` is the
+largest node-voltage difference between the two (relative to 1 V).
+
+``--impl reference`` times the CPU oracle port of the reference algorithm on
+the host cores (one process per core, bounded sample per step).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Newton solves/sec batched (stamp+LU+solve) vs plain FP64 GPU at 1e-9 match"
+UNIT = "solves/s"
+INSTANCES = 4096
+T_STOP, N_T = 1e-9, 501
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instances", type=int, default=INSTANCES)
+    ap.add_argument("--time-points", type=int, default=N_T)
+    ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------- oracle
+def _oracle_sample(args):
+    """CPU oracle: DC + `n_steps` BE steps of one adder instance."""
+    b, n_steps, n_t = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    import torch
+    torch.set_num_threads(1)
+    from oracle import analysis as oa
+    from voltax_gb300 import symbolic, workloads
+    c = workloads.mirror_adder_mc(INSTANCES, seed=0)
+    st = symbolic.structure(c)
+    sys_b = oa.System(c, st, st.plan, b % INSTANCES)
+    ts = np.linspace(0.0, T_STOP, n_t)[: n_steps + 1]
+    t0 = time.perf_counter()
+    _, ok, _ = oa.transient(sys_b, ts, ic="dc", method="be")
+    return (n_steps + 1), time.perf_counter() - t0, bool(ok.all())
+
+
+def cpu_baseline(n_steps=40, n_t=N_T):
+    solves, secs, ok = _oracle_sample((0, n_steps, n_t))
+    return {"value": solves / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 instance, DC + {n_steps} BE steps of the 4096-instance workload "
+                      f"({secs:.1f} s, 1 thread)", "converged": ok}
+
+
+def run_reference(a):
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_steps = 6
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(a.warmup):
+            pool.map(_oracle_sample, [(i, n_steps, a.time_points) for i in range(cores)])
+        times, solves = [], 0
+        for s in range(a.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_sample, [(s * cores + i, n_steps, a.time_points)
+                                            for i in range(cores)])
+            times.append(time.perf_counter() - t0)
+            solves += sum(r[0] for r in res)
+    total = sum(times)
+    value = solves / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"mirror_adder_mc{a.instances}",
+                       "sample": f"{cores} instances x (DC + {n_steps} BE steps) per step"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cores} processes, one instance each, DC + {n_steps} "
+                                       "BE steps per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------- GPU arm
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    # CPU baseline first (before any CUDA work), rank 0 only
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    cpu = cpu_baseline() if rank == 0 and not a.no_cpu else None
+
+    import torch
+    import voltax_gb300 as vx
+    from voltax_gb300 import _lib, workloads
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+
+    B = a.instances
+    circuit = workloads.mirror_adder_mc(B, seed=rank)
+    ts = np.linspace(0.0, T_STOP, a.time_points)
+    out_nodes = [circuit.node(n) for n in ("s0", "s1", "s2", "s3", "co")]
+
+    def to_device(c, device, pin=False):
+        out = c
+        for name in sorted(c.elements):
+            el = c.elements[name]
+            new = el.with_nodes(el.nodes)
+            for f in el.fields:
+                t = getattr(el, f)
+                setattr(new, f, t.pin_memory() if pin else t.to(device))
+            if hasattr(el, "value"):
+                new.value = el.value.map(lambda t: t.pin_memory() if pin else t.to(device))
+            if hasattr(el, "process"):
+                new.process = el.process
+            out = out.replace(name, new)
+        return out
+
+    dev_circuit = to_device(circuit, dev)
+    host_circuit = to_device(circuit, None, pin=True)
+    opts32 = vx.Options(precision="f32")
+    opts64 = vx.Options(precision="f64")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(c, opts):
+        sol = vx.transient(c, ts, ic="dc", method="be", options=opts)
+        return sol
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, k):
+        ms = []
+        for _ in range(k):
+            flush.zero_()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            barrier()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    for _ in range(a.warmup):
+        step(dev_circuit, opts32)
+    n0 = lib.vxg_launch_count()
+    with Clocks(local) as clk:
+        ms32 = timed(lambda: step(dev_circuit, opts32), a.steps)
+    launches = (lib.vxg_launch_count() - n0) // a.steps
+    solves_per_step = B * a.time_points
+    t32 = float(np.sum(ms32)) / 1e3
+    if dist is not None:
+        tt = torch.tensor([t32], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t32 = float(tt)
+    value = world * solves_per_step * a.steps / t32
+
+    # plain FP64 path on the same workload (fewer steps), and the match
+    step(dev_circuit, opts64)
+    ms64 = timed(lambda: step(dev_circuit, opts64), max(1, min(a.steps, 2)))
+    value64 = solves_per_step * len(ms64) / (float(np.sum(ms64)) / 1e3)
+    s32 = step(dev_circuit, opts32)
+    s64 = step(dev_circuit, opts64)
+    nv = circuit.n_nodes
+    match = float((s32.z[..., :nv] - s64.z[..., :nv]).abs().max())
+    conv = bool(s32.converged.all())
+    iters = float(s32.iterations[:, 1:].float().mean())
+
+    # end to end through the public API: params from pinned host memory, output
+    # node waveforms back to pinned host memory
+    h2d = sum(t.numel() * 8 for el in host_circuit.elements.values()
+              for t in ([getattr(el, f) for f in el.fields] +
+                        (el.value.params() if hasattr(el, "value") else [])))
+    out_host = torch.empty((B, a.time_points, len(out_nodes)), dtype=torch.float64,
+                           pin_memory=True)
+
+    def e2e_step():
+        s = step(host_circuit, opts32)
+        out_host.copy_(s.z[..., out_nodes], non_blocking=True)
+
+    e2e_step()
+    ms_e2e = timed(e2e_step, a.steps)
+    e2e_value = world * solves_per_step * a.steps / (float(np.sum(ms_e2e)) / 1e3)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * t32 / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 LU + f64 residual/refinement",
+        "data": "synthetic",
+        "config": {"workload": f"mirror_adder_mc{B}", "instances": B,
+                   "time_points": a.time_points, "method": "be", "t_stop_s": T_STOP,
+                   "solves_per_step": solves_per_step, "engine": "generic",
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "plain_fp64": {"value": value64, "unit": UNIT, "speedup": value / value64},
+        "match": {"max_abs_node_v_diff_vs_fp64": match, "converged": conv,
+                  "mean_newton_iters": iters},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(out_host.numel() * 8)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "roofline": None,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -235,6 +235,10 @@ int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
                   const double* z, double t, double cf, double cq, const double* lam,
                   double* const* grads, void* stream);
 
+/* Kernels this library has launched since it was loaded (a diagnostic
+ * counter; no counterpart in the reference). */
+uint64_t vxg_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

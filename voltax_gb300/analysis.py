@@ -228,7 +228,8 @@ class _DCRoot(torch.autograd.Function):
         for rows, buf in zip(call.rows, bufs):
             for r, row in enumerate(rows):
                 g = buf[r]
-                grads_out.append(g.sum(0) if row.ndim == 1 else g)
+                g = g.sum(0) if row.ndim == 1 else g
+                grads_out.append(g.to(row.device))
         return (None, None, None, *grads_out)
 
 

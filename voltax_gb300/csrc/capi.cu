@@ -2,6 +2,7 @@
 // drivers (host code). No exception crosses this boundary.
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -422,7 +423,7 @@ int vxg_spsolve_gdata(const vxg_handle* h, int32_t batch, const double* g, const
   if (!n) return VXG_OK;
   gdata_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       batch, h->t.nnz, h->t.S, h->t.rows, h->t.indices, g, x, gdata);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -493,3 +494,10 @@ int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
 }
 
 }  // extern "C"
+
+namespace vxg {
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace vxg
+
+extern "C" uint64_t vxg_launch_count(void) { return vxg::g_launches.load(); }

@@ -201,7 +201,7 @@ static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scr
   if (n)
     fill_panels_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, t.nnz, t.a_pos, data,
                                                                         work, ws);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   int dev = 0, max_optin = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -218,20 +218,21 @@ static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scr
                                         (int)smem));
       kern<<<grid, 256, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
                                    t.sn_panel, work, ws, scratch, ss);
+      VXG_LAUNCHED();
     } else {
       auto kern = factor_level_kernel<T, 128>;
       VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
       kern<<<grid, 128, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
                                    t.sn_panel, work, ws, scratch, ss);
+      VXG_LAUNCHED();
     }
-    VXG_CUDA_TRY(cudaGetLastError());
     const long long tlo = t.h_lv_st_ptr[L], thi = t.h_lv_st_ptr[L + 1];
     const long long nt = (long long)B * (thi - tlo);
     if (nt) {
       schur_apply_kernel<T><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(
           B, thi - tlo, t.st_tgt + tlo, t.st_ptr + tlo, t.st_src, scratch, ss, work, ws);
-      VXG_CUDA_TRY(cudaGetLastError());
+      VXG_LAUNCHED();
     }
   }
   return VXG_OK;

@@ -68,6 +68,17 @@ struct vxg_handle {
   vxg::Topo t;
 };
 
+namespace vxg {
+void count_launch();
+}
+
+// Count one kernel launch and surface launch errors.
+#define VXG_LAUNCHED()                     \
+  do {                                     \
+    vxg::count_launch();                   \
+    VXG_CUDA_TRY(cudaGetLastError());      \
+  } while (0)
+
 #define VXG_CUDA_TRY(expr)                 \
   do {                                     \
     cudaError_t _e = (expr);               \

@@ -303,7 +303,7 @@ int launch_param_vjp(const Topo& t, const GroupTable& gt, int B, const double* z
   for (int i = 0; i < VXG_MAX_GROUPS; ++i) gp.p[i] = i < gt.n_groups ? grads[i] : nullptr;
   param_vjp_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(gt, B, z, t.S, t_now, cf, cq,
                                                                  lam, gp);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -314,7 +314,7 @@ int launch_compose(const Topo& t, int B, int mode, double h, const double* z, co
   if (!n) return VXG_OK;
   compose_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
       B, t.S, t.nv, mode, h, z, f, q, fp, qp, gmin, gmin_scalar, t.seg_of, t.n_seg, rhs);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -322,7 +322,7 @@ int launch_newton_init(int n, const int* mask, int* active, int* converged, int*
                        cudaStream_t s) {
   if (!n) return VXG_OK;
   newton_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, mask, active, converged, iters);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -333,7 +333,7 @@ int launch_update(const Topo& t, int B, double* z, const double* dz, int* active
   if (!n) return VXG_OK;
   newton_update_kernel<256><<<n, 256, 0, s>>>(t.S, t.nv, t.n_seg, t.seg_ptr, z, dz, active,
                                               converged, iters, max_dv, rtol, atol, n_active);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 

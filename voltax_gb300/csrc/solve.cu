@@ -190,7 +190,7 @@ int launch_spmv(const Topo& t, int B, const double* data, const double* x, doubl
   else
     spmv_t_kernel<<<nblk(n, 256), 256, 0, s>>>(B, t.S, t.tptr, t.tent, t.rows, t.nnz, data, x,
                                                 y);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -208,14 +208,14 @@ static int solve_levels(const Topo& t, int B, const T* fac, T* x, T* contrib, in
                                                      t.sn_r, t.sn_panel, t.sn_piv_ptr,
                                                      t.sn_piv, fac, fs, x, t.S, contrib, cs,
                                                      transpose);
-    VXG_CUDA_TRY(cudaGetLastError());
+    VXG_LAUNCHED();
     const long long tlo = t.h_lv_bt_ptr[L], thi = t.h_lv_bt_ptr[L + 1];
     const long long nt = (long long)B * (thi - tlo);
     if (nt) {
       border_apply_kernel<T><<<nblk(nt, 256), 256, 0, s>>>(B, thi - tlo, t.bt_tgt + tlo,
                                                            t.bt_ptr + tlo, t.bt_src, contrib,
                                                            cs, x, t.S);
-      VXG_CUDA_TRY(cudaGetLastError());
+      VXG_LAUNCHED();
     }
   }
   for (int L = t.n_levels - 1; L >= 0; --L) {
@@ -226,7 +226,7 @@ static int solve_levels(const Topo& t, int B, const T* fac, T* x, T* contrib, in
     solve_bwd_kernel<T, 128><<<grid, 128, smem, s>>>(t.lv_sn + lo, t.sn_k, t.sn_r, t.sn_panel,
                                                      t.sn_piv_ptr, t.sn_piv, t.sn_bord_ptr,
                                                      t.sn_bord, fac, fs, x, t.S, transpose);
-    VXG_CUDA_TRY(cudaGetLastError());
+    VXG_LAUNCHED();
   }
   return VXG_OK;
 }
@@ -247,20 +247,23 @@ int launch_solve(const Topo& t, int B, int precision, const void* factors, const
   float* xt = (float*)vec_t;
   VXG_CUDA_TRY(cudaMemcpyAsync(bcopy, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   cast_kernel<double, float><<<nblk(n, 256), 256, 0, s>>>(n, bcopy, xt);
+  VXG_LAUNCHED();
   int st = solve_levels<float>(t, B, (const float*)factors, xt, (float*)scratch, transpose, s);
   if (st) return st;
   cast_kernel<float, double><<<nblk(n, 256), 256, 0, s>>>(n, xt, x);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   if (!data) refine = 0;
   for (int it = 0; it < refine; ++it) {
     st = launch_spmv(t, B, data, x, res, transpose, s);
     if (st) return st;
     sub_kernel<<<nblk(n, 256), 256, 0, s>>>(n, bcopy, res, res);
+    VXG_LAUNCHED();
     cast_kernel<double, float><<<nblk(n, 256), 256, 0, s>>>(n, res, xt);
+    VXG_LAUNCHED();
     st = solve_levels<float>(t, B, (const float*)factors, xt, (float*)scratch, transpose, s);
     if (st) return st;
     add_cast_kernel<<<nblk(n, 256), 256, 0, s>>>(n, xt, x);
-    VXG_CUDA_TRY(cudaGetLastError());
+    VXG_LAUNCHED();
   }
   return VXG_OK;
 }

@@ -111,7 +111,7 @@ int launch_eval(const Topo& t, const GroupTable& gt, int B, const double* z, dou
   eval_kernel<<<blocks_for(n, 128), 128, 0, s>>>(gt, B, z, t.S, t.nv, t_now, cf, cq, want_f,
                                                  want_q, want_j, t.n_res_slots, t.n_jac_slots,
                                                  cf_buf, cq_buf, cj_buf);
-  VXG_CUDA_TRY(cudaGetLastError());
+  VXG_LAUNCHED();
   return VXG_OK;
 }
 
@@ -123,14 +123,14 @@ int launch_gather(const Topo& t, int B, const double* cf_buf, const double* cq_b
     gather_jac_kernel<<<blocks_for(n, 256), 256, 0, s>>>(
         B, t.nnz, t.jac_ptr, t.jac_src, t.n_jac_slots, cj_buf, t.rows, t.indices, t.nv,
         t.seg_of, t.n_seg, gmin, gmin_scalar, data_out);
-    VXG_CUDA_TRY(cudaGetLastError());
+    VXG_LAUNCHED();
   }
   if (f_out || q_out) {
     const long long n = (long long)B * t.S;
     gather_res_kernel<<<blocks_for(n, 256), 256, 0, s>>>(B, t.S, t.res_ptr, t.res_src,
                                                           t.n_res_slots, cf_buf, cq_buf,
                                                           f_out, q_out);
-    VXG_CUDA_TRY(cudaGetLastError());
+    VXG_LAUNCHED();
   }
   return VXG_OK;
 }
