@@ -235,6 +235,27 @@ int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
                   const double* z, double t, double cf, double cq, const double* lam,
                   double* const* grads, void* stream);
 
+/* Shared memory one instance needs in the fused persistent kernel
+ * (vxg_fused_run); VXG_ERR_TOO_LARGE when the topology is not eligible
+ * (a supernode wider than 32, several segments, or more shared memory than
+ * one CTA may have). */
+int vxg_fused_smem(const vxg_handle* h, int32_t precision, size_t* bytes);
+
+/* The whole analysis of every instance in ONE persistent launch: one CTA
+ * per instance keeps the state, the stamps, the panels and the solves in
+ * shared memory. With dc_first, the DC operating point at ts[0] is solved
+ * first from the guess z0 (direct attempt of direct_steps iterations, then
+ * gmin stepping over gmins[1..gmin_steps] restarting from z0,
+ * voltax/analysis.py:236-266); otherwise z0 is the initial state. Then one
+ * Newton solve of `mode` per time point ts[1..n_t-1] (device array),
+ * warm-started from the previous state (voltax/analysis.py:434-480).
+ * z_out: n_t x B x S; converged, iters: n_t x B (row 0: the DC solve). */
+int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                  int32_t mode, int32_t n_t, const double* ts, const double* z0,
+                  int32_t dc_first, const double* gmins, int32_t gmin_steps,
+                  int32_t direct_steps, double gmin, const vxg_newton_opts* opts,
+                  double* z_out, int32_t* converged, int32_t* iters, void* stream);
+
 /* Kernels this library has launched since it was loaded (a diagnostic
  * counter; no counterpart in the reference). */
 uint64_t vxg_launch_count(void);

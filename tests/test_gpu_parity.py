@@ -105,11 +105,15 @@ def _oracle_dc(c):
     return oa.dc(oa.System(c, st, st.plan))
 
 
+ENGINES = ["fused", "generic"]
+
+
 @pytest.mark.parametrize("name", ["rc_ladder", "grid", "adder"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_dc_matches_oracle(name, precision):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_dc_matches_oracle(name, precision, engine):
     c = CIRCUITS[name]()
-    sol = vx.dc(c, options=vx.Options(precision=precision))
+    sol = vx.dc(c, options=vx.Options(precision=precision, engine=engine))
     z_ref, ok_ref, it_ref = _oracle_dc(c)
     assert bool(sol.converged) == ok_ref
     assert rel(sol.z.cpu().numpy(), z_ref) < 1e-9
@@ -117,7 +121,8 @@ def test_dc_matches_oracle(name, precision):
         assert int(sol.iterations) == it_ref
 
 
-def test_cmos_full_adder_needs_gmin_stepping():
+@pytest.mark.parametrize("engine", ENGINES)
+def test_cmos_full_adder_needs_gmin_stepping(engine):
     """voltax tests/test_analysis.py:138-149 on the GPU."""
     b = CircuitBuilder()
     b.vsource("vdd", "0", 1.2)
@@ -125,8 +130,8 @@ def test_cmos_full_adder_needs_gmin_stepping():
         b.vsource(n, "0", 0.0)
     cmos.full_adder(b, "a", "c", "0", "s", "co", "vdd")
     c = b.build()
-    plain = vx.dc(c, options=vx.Options(gmin_steps=0))
-    rescued = vx.dc(c)
+    plain = vx.dc(c, options=vx.Options(gmin_steps=0, engine=engine))
+    rescued = vx.dc(c, options=vx.Options(engine=engine))
     assert not bool(plain.converged)
     assert bool(rescued.converged)
     z_ref, ok_ref, it_ref = _oracle_dc(c)
@@ -145,11 +150,13 @@ def test_singular_circuit_fails_check():
 
 @pytest.mark.parametrize("method", ["be", "trap"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_ring_transient_matches_oracle(method, precision):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_ring_transient_matches_oracle(method, precision, engine):
     c, nodes = workloads.ring_oscillator(9)
     z0 = workloads.ring_initial_state(c, nodes)
     ts = np.linspace(0.0, 60e-12, 31)
-    sol = vx.transient(c, ts, ic=z0, method=method, options=vx.Options(precision=precision))
+    sol = vx.transient(c, ts, ic=z0, method=method,
+                       options=vx.Options(precision=precision, engine=engine))
     st = symbolic.structure(c)
     zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic=z0.numpy(), method=method)
     assert bool(sol.converged.all()) and okr.all()
@@ -167,10 +174,12 @@ def test_rc_ladder_recorded_values_on_gpu():
                                [1.0, 0.921635241, 0.766714055, -7.83647588e-05], atol=1e-8)
 
 
-def test_batched_mc_matches_per_instance_oracle():
+@pytest.mark.parametrize("engine", ENGINES)
+def test_batched_mc_matches_per_instance_oracle(engine):
     c = workloads.mirror_adder_mc(6, seed=1, bits=2)
     ts = np.linspace(0, 200e-12, 21)
-    sol = vx.transient(c, ts, ic="dc", method="be", options=vx.Options(precision="f32"))
+    sol = vx.transient(c, ts, ic="dc", method="be",
+                       options=vx.Options(precision="f32", engine=engine))
     assert sol.z.shape == (6, len(ts), c.size)
     st = symbolic.structure(c)
     for b in (0, 5):
@@ -244,3 +253,22 @@ def test_f32_refined_matches_f64_on_power_grid():
     s32 = vx.dc(c, options=vx.Options(precision="f32"))
     assert bool(s64.converged) and bool(s32.converged)
     assert rel(s32.z.cpu().numpy(), s64.z.cpu().numpy()) < 1e-9
+
+
+def test_fused_equals_generic_on_the_4bit_adder():
+    c = workloads.mirror_adder_mc(8, seed=2)
+    ts = np.linspace(0, 300e-12, 31)
+    a = vx.transient(c, ts, ic="dc", options=vx.Options(engine="fused"))
+    b = vx.transient(c, ts, ic="dc", options=vx.Options(engine="generic"))
+    assert bool(a.converged.all()) and bool(b.converged.all())
+    assert float((a.z - b.z).abs().max()) < 1e-11
+    assert torch.equal(a.iterations[:, 1:], b.iterations[:, 1:])
+
+
+def test_fused_is_bitwise_reproducible():
+    c = workloads.mirror_adder_mc(4, seed=3)
+    ts = np.linspace(0, 100e-12, 11)
+    o = vx.Options(engine="fused", precision="f32")
+    a = vx.transient(c, ts, ic="dc", options=o)
+    b = vx.transient(c, ts, ic="dc", options=o)
+    assert torch.equal(a.z, b.z)

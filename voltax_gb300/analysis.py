@@ -51,8 +51,11 @@ class Options:
     sparse_threshold: int = SPARSE_THRESHOLD
     precision: str = "f64"
     refine: int = 2
+    engine: str = "auto"
 
     def __post_init__(self):
+        if self.engine not in ("auto", "fused", "generic"):
+            raise ValueError(f"engine must be 'auto', 'fused' or 'generic', got {self.engine!r}")
         if self.solver not in ("auto", "dense", "sparse"):
             raise ValueError("solver must be 'auto', 'dense' or 'sparse', "
                              f"got {self.solver!r}")
@@ -128,6 +131,36 @@ class _Call:
         dev = self.eng.device
         self.conv = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
         self.iters = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
+        self.fused = self._use_fused()
+
+    def _use_fused(self) -> bool:
+        if self.o.engine == "generic":
+            return False
+        n = C.c_size_t()
+        ok = self.eng.lib.vxg_fused_smem(self.eng.handle, self.prec, C.byref(n)) == L.VXG_OK
+        if self.o.engine == "fused" and not ok:
+            raise L.VxgError("this topology is not eligible for the fused kernel")
+        return ok
+
+    def fused_run(self, mode, ts_np, z0, dc_first):
+        """One persistent launch: [DC at ts[0]] + one Newton solve per time point."""
+        o = self.o
+        dev = self.eng.device
+        T = len(ts_np)
+        ts_d = torch.as_tensor(ts_np, dtype=torch.float64, device=dev)
+        gmins = np.concatenate([[o.gmin], np.logspace(np.log10(o.gmin_start),
+                                                      np.log10(o.gmin), o.gmin_steps)])
+        gm_d = torch.as_tensor(gmins, dtype=torch.float64, device=dev)
+        z_out = torch.empty((T, self.B, self.eng.S), dtype=torch.float64, device=dev)
+        conv = torch.empty((T, self.B), dtype=torch.int32, device=dev)
+        iters = torch.empty((T, self.B), dtype=torch.int32, device=dev)
+        nat = o.native()
+        L.check(self.eng.lib.vxg_fused_run(
+            self.eng.handle, self.B, self.params, mode, T, ts_d.data_ptr(), z0.data_ptr(),
+            int(dc_first), gm_d.data_ptr(), o.gmin_steps, o.direct_steps, o.gmin,
+            C.byref(nat), z_out.data_ptr(), conv.data_ptr(), iters.data_ptr(), stream_ptr()),
+            "vxg_fused_run")
+        return z_out, conv, iters
 
     def newton(self, mode, z, t, t_prev=0.0, z_prev=None, gmin=None, max_steps=None,
                mask=None, factors=None):
@@ -156,6 +189,12 @@ def _gmin_stepping(call: _Call, t, guess: torch.Tensor, factors=None):
     """voltax/analysis.py:236-266 for a batch: instances that fail the
     direct attempt run the gmin stages; the others stay frozen."""
     o = call.o
+    if call.fused:
+        z_out, conv, iters = call.fused_run(L.VXG_MODE_DC, np.array([float(t)]),
+                                            guess.contiguous(), True)
+        z = z_out[0]
+        data = _refactor(call, z, t, factors) if factors is not None else None
+        return z, conv[0], iters[0], data
     z = guess.clone()
     conv, iters = call.newton(L.VXG_MODE_DC, z, t, gmin=o.gmin,
                               max_steps=o.direct_steps if o.gmin_steps else None)
@@ -271,6 +310,23 @@ def transient(circuit, ts, ic="dc", method: str = "be",
     call = _Call(circuit, options)
     S, B = call.eng.S, call.B
     dev = call.eng.device
+    mode = L.VXG_MODE_BE if method == "be" else L.VXG_MODE_TRAP
+    if call.fused and (isinstance(ic, Solution) or not isinstance(ic, str) or ic in ("dc", "zero")):
+        dc_first = isinstance(ic, str) and ic == "dc"
+        if isinstance(ic, Solution):
+            z0 = ic.z
+        elif isinstance(ic, str):
+            z0 = torch.zeros((B, S), dtype=torch.float64, device=dev)
+        else:
+            z0 = torch.as_tensor(ic, dtype=torch.float64)
+        z0 = torch.as_tensor(z0, dtype=torch.float64, device=dev).detach()
+        z0 = z0.reshape(-1, S).expand(B, S).contiguous()
+        z_out, conv, iters = call.fused_run(mode, ts_np, z0, dc_first)
+        conv[0] = 1  # the initial state counts as converged (voltax/analysis.py:479)
+        tt = torch.as_tensor(ts_np)
+        if circuit.batch == 1:
+            return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])
+        return Solution(tt, z_out.permute(1, 0, 2), conv.T.bool(), circuit.layout, iters.T)
     if isinstance(ic, Solution):
         z0 = ic.z
     elif isinstance(ic, str):
@@ -289,7 +345,6 @@ def transient(circuit, ts, ic="dc", method: str = "be",
     z_out = torch.empty((T, B, S), dtype=torch.float64, device=dev)
     conv = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
     iters = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
-    mode = L.VXG_MODE_BE if method == "be" else L.VXG_MODE_TRAP
     o = options.native()
     L.check(call.eng.lib.vxg_transient(
         call.eng.handle, B, call.params, mode, T, ts_np.ctypes.data_as(L.PF64), z0.data_ptr(),

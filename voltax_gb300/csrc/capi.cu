@@ -134,7 +134,7 @@ static void free_topo(Topo& t) {
                   t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
                   t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
                   t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
-                  t.d_flag};
+                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < t.n_groups; ++i)
@@ -213,6 +213,9 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
   UP(bt_ptr, d->bt_ptr, nbt + 1);
   UP(bt_src, d->bt_src, d->bt_ptr[nbt]);
   UP(d_flag, (const int*)nullptr, 4);
+  UP(d_lv_ptr, d->lv_ptr, nl + 1);
+  UP(d_lv_st_ptr, d->lv_st_ptr, nl + 1);
+  UP(d_lv_bt_ptr, d->lv_bt_ptr, nl + 1);
   for (int i = 0; i < d->n_groups && st == VXG_OK; ++i) {
     t.groups[i] = d->groups[i];
     st = upload(&t.group_nodes[i], d->groups[i].nodes, (size_t)d->groups[i].n * d->groups[i].T);

@@ -1,0 +1,636 @@
+// Fused persistent Newton kernel for small circuits.
+//
+// One CTA owns one circuit instance at a time (grid-stride over the batch)
+// and runs the whole analysis in shared memory: the DC operating point with
+// the gmin-stepping fallback (voltax/analysis.py:236-266), then every
+// backward-Euler or trapezoidal time step (voltax/analysis.py:434-480), each
+// a damped Newton solve (voltax/analysis.py:208-233) of
+//   device evaluation -> deterministic stamping -> supernodal refactorization
+//   -> level-scheduled solves (+ FP64 refinement) -> damped update.
+// Nothing but parameters, time points and the output states touches global
+// memory; the topology tables are read through L1.
+//
+// Supernodes are factored one per warp (k <= 32: Gauss-Jordan with partial
+// pivoting on registers and shared memory), the supernodes of one level in
+// parallel across warps; Schur and border updates of a level are applied by
+// a second pass with one thread per target slot summing its sources in a
+// fixed order, so results are bitwise reproducible.
+
+#include <algorithm>
+#include <cstring>
+
+#include "devices.cuh"
+
+namespace vxg {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct FusedArgs {
+  GroupTable gt;
+  int S, nv, nnz, n_res, n_jac, work, n_levels, max_scr;
+  const long long *res_ptr, *res_src, *jac_ptr, *jac_src, *a_pos, *indptr;
+  const int *indices, *rows;
+  const int *sn_k, *sn_r, *sn_piv, *sn_bord;
+  const long long *sn_panel, *sn_piv_ptr, *sn_bord_ptr;
+  const long long* lv_ptr;
+  const int* lv_sn;
+  const long long *lv_schur_off, *lv_bord_off;
+  const long long *lv_st_ptr, *st_tgt, *st_ptr, *st_src;
+  const long long* lv_bt_ptr;
+  const int* bt_tgt;
+  const long long *bt_ptr, *bt_src;
+  int B, mode, n_t, max_steps, refine, dc_first, gmin_steps, direct_steps;
+  double rtol, atol, max_dv, gmin;
+  const double* ts;
+  const double* gmins;
+  const double* z0;
+  double* z_out;
+  int* conv;
+  int* iters;
+};
+
+__host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Shared-memory layout of one instance.
+struct FusedLayout {
+  size_t z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, total;
+};
+
+template <typename T>
+__host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, int n_jac,
+                                                    int work, int max_scr) {
+  FusedLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o = a16(o + bytes);
+    return at;
+  };
+  const size_t d = sizeof(double);
+  L.z = take(d * S);
+  L.zp = take(d * S);
+  L.fp = take(d * S);
+  L.qp = take(d * S);
+  L.f = take(d * S);
+  L.q = take(d * S);
+  L.rhs = take(d * S);
+  L.dz = take(d * S);
+  L.res = take(d * S);
+  L.data = take(d * nnz);
+  L.cf = take(d * n_res);
+  L.cq = take(d * n_res);
+  L.cj = take(d * n_jac);
+  L.work = take(sizeof(T) * work);
+  L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
+  L.xt = take(sizeof(T) * S);
+  L.red = take(64 * sizeof(double));
+  L.total = o;
+  return L;
+}
+
+template <typename T>
+__device__ __forceinline__ T tabs_(T x) {
+  return x < T(0) ? -x : x;
+}
+
+// ------------------------------------------------------------ block helpers
+template <int NT>
+__device__ double block_max_nan(double v, int nan_flag, double* red, int* nan_out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) {
+    v = fmax(v, __shfl_xor_sync(kFull, v, off));
+    nan_flag |= __shfl_xor_sync(kFull, nan_flag, off);
+  }
+  int* redi = reinterpret_cast<int*>(red + 32);
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = v;
+    redi[warp] = nan_flag;
+  }
+  __syncthreads();
+  double m = 0.0;
+  int nf = 0;
+  for (int w = 0; w < NT / 32; ++w) {
+    m = fmax(m, red[w]);
+    nf |= redi[w];
+  }
+  *nan_out = nf;
+  return m;
+}
+
+template <int NT>
+__device__ int block_all(int ok, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ok = __all_sync(kFull, ok);
+  int* redi = reinterpret_cast<int*>(red + 32);
+  __syncthreads();
+  if (lane == 0) redi[warp] = ok;
+  __syncthreads();
+  int all = 1;
+  for (int w = 0; w < NT / 32; ++w) all &= redi[w];
+  return all;
+}
+
+// ------------------------------------------------- warp-level supernode LDU
+// Inverts F11 in place (Gauss-Jordan, partial pivoting), Ub = W F12 in place,
+// S = F21 Ub into Sout, Lb = F21 W in place. k <= 32.
+template <typename T>
+__device__ void warp_factor(T* P, int k, int r, T* Sout, int lane) {
+  T* A = P;
+  T* F12 = P + k * k;
+  T* F21 = F12 + k * r;
+  int myperm = lane;
+  for (int c = 0; c < k; ++c) {
+    T v = (lane >= c && lane < k) ? tabs_(A[lane * k + c]) : T(-1);
+    int bi = lane;
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_down_sync(kFull, v, off);
+      const int oi = __shfl_down_sync(kFull, bi, off);
+      if (ov > v || (ov == v && oi < bi)) {
+        v = ov;
+        bi = oi;
+      }
+    }
+    int p = __shfl_sync(kFull, bi, 0);
+    if (p < c || p >= k) p = c;
+    if (lane == c) myperm = p;
+    if (p != c && lane < k) {
+      const T tmp = A[p * k + lane];
+      A[p * k + lane] = A[c * k + lane];
+      A[c * k + lane] = tmp;
+    }
+    __syncwarp();
+    const T d = A[c * k + c];
+    const T colv = (lane < k && lane != c) ? A[lane * k + c] : T(0);
+    __syncwarp();
+    if (lane < k) A[c * k + lane] = ((lane == c) ? T(1) : A[c * k + lane]) / d;
+    __syncwarp();
+    const T rowc = (lane < k) ? A[c * k + lane] : T(0);
+    for (int i = 0; i < k; ++i) {
+      const T f = __shfl_sync(kFull, colv, i);
+      if (i != c && lane < k) {
+        const T a = (lane == c) ? T(0) : A[i * k + lane];
+        A[i * k + lane] = a - f * rowc;
+      }
+    }
+    __syncwarp();
+  }
+  for (int c = k - 1; c >= 0; --c) {
+    const int p = __shfl_sync(kFull, myperm, c);
+    if (p != c && lane < k) {
+      const T tmp = A[lane * k + c];
+      A[lane * k + c] = A[lane * k + p];
+      A[lane * k + p] = tmp;
+    }
+  }
+  __syncwarp();
+  if (r == 0) return;
+  // Ub = W F12, one column per lane
+  for (int c0 = 0; c0 < r; c0 += 32) {
+    const int col = c0 + lane;
+    T x[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) x[l] = (l < k && col < r) ? F12[l * r + col] : T(0);
+    __syncwarp();
+    if (col < r)
+      for (int i = 0; i < k; ++i) {
+        T acc = T(0);
+#pragma unroll
+        for (int l = 0; l < 32; ++l)
+          if (l < k) acc += A[i * k + l] * x[l];
+        F12[i * r + col] = acc;
+      }
+    __syncwarp();
+  }
+  // S = F21 Ub, one column per lane
+  for (int c0 = 0; c0 < r; c0 += 32) {
+    const int col = c0 + lane;
+    T u[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) u[l] = (l < k && col < r) ? F12[l * r + col] : T(0);
+    if (col < r)
+      for (int a = 0; a < r; ++a) {
+        T acc = T(0);
+#pragma unroll
+        for (int l = 0; l < 32; ++l)
+          if (l < k) acc += F21[a * k + l] * u[l];
+        Sout[a * r + col] = acc;
+      }
+  }
+  __syncwarp();
+  // Lb = F21 W, lane j owns column j of W
+  T w[32];
+#pragma unroll
+  for (int l = 0; l < 32; ++l) w[l] = (l < k && lane < k) ? A[l * k + lane] : T(0);
+  for (int a = 0; a < r; ++a) {
+    T acc = T(0);
+#pragma unroll
+    for (int l = 0; l < 32; ++l)
+      if (l < k) acc += F21[a * k + l] * w[l];
+    __syncwarp();
+    if (lane < k) F21[a * k + lane] = acc;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------- one instance
+template <typename T, int NT>
+struct Instance {
+  const FusedArgs& A;
+  int b;
+  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *data, *cf, *cq, *cj, *red;
+  T *work, *scr, *xt;
+
+  __device__ void eval(const double* zz, double t, double cfc, double cqc, bool wf, bool wq,
+                       bool wj) {
+    const GroupTable& gt = A.gt;
+    for (int flat = threadIdx.x; flat < gt.n_dev; flat += NT) {
+      int gi = 0;
+      while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
+      const GroupDev& g = gt.g[gi];
+      const int d = flat - (int)g.dev_base;
+      double u[kMaxM];
+      for (int i = 0; i < g.T; ++i) {
+        const int node = g.nodes[d * g.T + i];
+        u[i] = node >= 0 ? zz[node] : 0.0;
+      }
+      for (int i = 0; i < g.K; ++i) u[g.T + i] = zz[g.int_offset + d * g.K + i];
+      DevEval o;
+      eval_device(g, b, d, u, t, cfc, cqc, wf, wq, wj, o);
+      const int m = g.m;
+      const long long rb = g.res_base + (long long)d * m;
+      if (wf)
+        for (int i = 0; i < m; ++i) cf[rb + i] = o.I[i];
+      if (wq)
+        for (int i = 0; i < m; ++i) cq[rb + i] = o.Q[i];
+      if (wj) {
+        const long long jb = g.jac_base + (long long)d * m * m;
+        for (int i = 0; i < m * m; ++i) cj[jb + i] = o.J[i];
+      }
+    }
+  }
+
+  __device__ void assemble_res(double* fo, double* qo) {
+    for (int i = threadIdx.x; i < A.S; i += NT) {
+      if (fo) {
+        double acc = 0.0;
+        for (long long p = A.res_ptr[i]; p < A.res_ptr[i + 1]; ++p) acc += cf[A.res_src[p]];
+        fo[i] = acc;
+      }
+      if (qo) {
+        double acc = 0.0;
+        for (long long p = A.res_ptr[i]; p < A.res_ptr[i + 1]; ++p) acc += cq[A.res_src[p]];
+        qo[i] = acc;
+      }
+    }
+  }
+
+  // CSR values (+gmin) and the panels; residual rhs = -r
+  __device__ void assemble_system(double gmin, double h) {
+    for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
+    assemble_res(f, A.mode == VXG_MODE_DC ? nullptr : q);
+    for (int e = threadIdx.x; e < A.nnz; e += NT) {
+      double acc = 0.0;
+      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += cj[A.jac_src[p]];
+      const int r = A.rows[e];
+      if (r < A.nv && A.indices[e] == r) acc += gmin;
+      data[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < A.nnz; e += NT) work[A.a_pos[e]] = (T)data[e];
+    for (int i = threadIdx.x; i < A.S; i += NT) {
+      const double gm = i < A.nv ? gmin * z[i] : 0.0;
+      double r;
+      if (A.mode == VXG_MODE_DC)
+        r = f[i] + gm;
+      else if (A.mode == VXG_MODE_BE)
+        r = (q[i] - qp[i]) / h + f[i] + gm;
+      else
+        r = (q[i] - qp[i]) / h + 0.5 * (f[i] + fp[i]) + gm;
+      rhs[i] = -r;
+    }
+    __syncthreads();
+  }
+
+  __device__ void factor() {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int L = 0; L < A.n_levels; ++L) {
+      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
+      for (long long p = lo + warp; p < hi; p += NT / 32) {
+        const int j = A.lv_sn[p];
+        warp_factor<T>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j], scr + A.lv_schur_off[p],
+                       lane);
+      }
+      __syncthreads();
+      for (long long t = A.lv_st_ptr[L] + threadIdx.x; t < A.lv_st_ptr[L + 1]; t += NT) {
+        T acc = T(0);
+        for (long long p = A.st_ptr[t]; p < A.st_ptr[t + 1]; ++p) acc += scr[A.st_src[p]];
+        work[A.st_tgt[t]] -= acc;
+      }
+      __syncthreads();
+    }
+  }
+
+  // in-place solve of xt
+  __device__ void solve_t() {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int L = 0; L < A.n_levels; ++L) {
+      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
+      for (long long p = lo + warp; p < hi; p += NT / 32) {
+        const int j = A.lv_sn[p];
+        const int k = A.sn_k[j], r = A.sn_r[j];
+        const T* W = work + A.sn_panel[j];
+        const T* Lb = W + k * k + k * r;
+        const int* piv = A.sn_piv + A.sn_piv_ptr[j];
+        const T y = lane < k ? xt[piv[lane]] : T(0);
+        T acc = T(0);
+        T* cb = scr + A.lv_bord_off[p];
+        for (int l = 0; l < k; ++l) {
+          const T yl = __shfl_sync(kFull, y, l);
+          if (lane < k) acc += W[lane * k + l] * yl;
+        }
+        for (int a0 = 0; a0 < r; a0 += 32) {
+          const int a = a0 + lane;
+          T c = T(0);
+          for (int l = 0; l < k; ++l) {
+            const T yl = __shfl_sync(kFull, y, l);
+            if (a < r) c += Lb[a * k + l] * yl;
+          }
+          if (a < r) cb[a] = c;
+        }
+        if (lane < k) xt[piv[lane]] = acc;
+      }
+      __syncthreads();
+      for (long long t = A.lv_bt_ptr[L] + threadIdx.x; t < A.lv_bt_ptr[L + 1]; t += NT) {
+        T acc = T(0);
+        for (long long p = A.bt_ptr[t]; p < A.bt_ptr[t + 1]; ++p) acc += scr[A.bt_src[p]];
+        xt[A.bt_tgt[t]] -= acc;
+      }
+      __syncthreads();
+    }
+    for (int L = A.n_levels - 1; L >= 0; --L) {
+      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
+      for (long long p = lo + warp; p < hi; p += NT / 32) {
+        const int j = A.lv_sn[p];
+        const int k = A.sn_k[j], r = A.sn_r[j];
+        if (r == 0) continue;
+        const T* Ub = work + A.sn_panel[j] + k * k;
+        const int* piv = A.sn_piv + A.sn_piv_ptr[j];
+        const int* brd = A.sn_bord + A.sn_bord_ptr[j];
+        if (lane < k) {
+          T acc = T(0);
+          for (int a = 0; a < r; ++a) acc += Ub[lane * r + a] * xt[brd[a]];
+          xt[piv[lane]] -= acc;
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // dz = J^-1 rhs with FP64 refinement
+  __device__ void solve(int refine) {
+    for (int i = threadIdx.x; i < A.S; i += NT) xt[i] = (T)rhs[i];
+    __syncthreads();
+    solve_t();
+    for (int i = threadIdx.x; i < A.S; i += NT) dz[i] = (double)xt[i];
+    __syncthreads();
+    for (int it = 0; it < refine; ++it) {
+      for (int i = threadIdx.x; i < A.S; i += NT) {
+        double acc = 0.0;
+        for (long long e = A.indptr[i]; e < A.indptr[i + 1]; ++e) acc += data[e] * dz[A.indices[e]];
+        xt[i] = (T)(rhs[i] - acc);
+      }
+      __syncthreads();
+      solve_t();
+      for (int i = threadIdx.x; i < A.S; i += NT) dz[i] += (double)xt[i];
+      __syncthreads();
+    }
+  }
+
+  // damped update; returns converged (uniform across the block)
+  __device__ int update() {
+    double m = 0.0;
+    int nanf = 0;
+    for (int i = threadIdx.x; i < A.nv; i += NT) {
+      const double v = fabs(dz[i]);
+      if (isnan(v)) nanf = 1;
+      else m = fmax(m, v);
+    }
+    int any_nan = 0;
+    m = block_max_nan<NT>(m, nanf, red, &any_nan);
+    const double dv_max = any_nan ? nan("") : m;
+    const double qd = A.max_dv / (dv_max + 1e-300);
+    const double scale = isnan(qd) ? qd : fmin(1.0, qd);
+    int ok = 1;
+    for (int i = threadIdx.x; i < A.S; i += NT) {
+      const double d = dz[i];
+      const double zn = z[i] + scale * d;
+      if (!(fabs(d) <= A.atol + A.rtol * fabs(zn))) ok = 0;
+      if (!isfinite(zn)) ok = 0;
+      z[i] = zn;
+    }
+    ok = block_all<NT>(ok, red);
+    return ok && scale == 1.0;
+  }
+
+  __device__ int newton(int mode, double t, double t_prev, double gmin, int max_steps,
+                        int* iters_out) {
+    const bool dc = mode == VXG_MODE_DC;
+    const double cfc = mode == VXG_MODE_TRAP ? 0.5 : 1.0;
+    const double cqc = dc ? 0.0 : 1.0 / (t - t_prev);
+    const double h = t - t_prev;
+    int done = 0, it = 0;
+    while (it < max_steps && !done) {
+      eval(z, t, cfc, cqc, true, !dc, true);
+      __syncthreads();
+      assemble_system(gmin, h);
+      factor();
+      solve(sizeof(T) == sizeof(float) ? A.refine : 0);
+      done = update();
+      ++it;
+    }
+    *iters_out = it;
+    return done;
+  }
+};
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) fused_kernel(const __grid_constant__ FusedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const FusedLayout L = fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr);
+  Instance<T, NT> I{A, 0};
+  I.z = reinterpret_cast<double*>(smem + L.z);
+  I.zp = reinterpret_cast<double*>(smem + L.zp);
+  I.fp = reinterpret_cast<double*>(smem + L.fp);
+  I.qp = reinterpret_cast<double*>(smem + L.qp);
+  I.f = reinterpret_cast<double*>(smem + L.f);
+  I.q = reinterpret_cast<double*>(smem + L.q);
+  I.rhs = reinterpret_cast<double*>(smem + L.rhs);
+  I.dz = reinterpret_cast<double*>(smem + L.dz);
+  I.res = reinterpret_cast<double*>(smem + L.res);
+  I.data = reinterpret_cast<double*>(smem + L.data);
+  I.cf = reinterpret_cast<double*>(smem + L.cf);
+  I.cq = reinterpret_cast<double*>(smem + L.cq);
+  I.cj = reinterpret_cast<double*>(smem + L.cj);
+  I.work = reinterpret_cast<T*>(smem + L.work);
+  I.scr = reinterpret_cast<T*>(smem + L.scr);
+  I.xt = reinterpret_cast<T*>(smem + L.xt);
+  I.red = reinterpret_cast<double*>(smem + L.red);
+  const long long BS = (long long)A.B * A.S;
+  for (int b = blockIdx.x; b < A.B; b += gridDim.x) {
+    I.b = b;
+    for (int i = threadIdx.x; i < A.S; i += NT) I.z[i] = A.z0[(long long)b * A.S + i];
+    __syncthreads();
+    int ok = 1, it = 0;
+    if (A.dc_first) {
+      const int direct = A.gmin_steps > 0 ? A.direct_steps : A.max_steps;
+      ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmin, direct, &it);
+      if (!ok && A.gmin_steps > 0) {
+        for (int i = threadIdx.x; i < A.S; i += NT) I.z[i] = A.z0[(long long)b * A.S + i];
+        __syncthreads();
+        for (int s = 1; s <= A.gmin_steps; ++s) {
+          int its = 0;
+          ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmins[s], A.max_steps, &its);
+          it += its;
+        }
+      }
+    }
+    for (int i = threadIdx.x; i < A.S; i += NT) A.z_out[(long long)b * A.S + i] = I.z[i];
+    if (threadIdx.x == 0) {
+      A.conv[b] = ok;
+      A.iters[b] = it;
+    }
+    for (int n = 1; n < A.n_t; ++n) {
+      const double tp = A.ts[n - 1], t = A.ts[n];
+      for (int i = threadIdx.x; i < A.S; i += NT) I.zp[i] = I.z[i];
+      __syncthreads();
+      I.eval(I.zp, tp, 1.0, 0.0, A.mode == VXG_MODE_TRAP, true, false);
+      __syncthreads();
+      I.assemble_res(A.mode == VXG_MODE_TRAP ? I.fp : nullptr, I.qp);
+      __syncthreads();
+      int its = 0;
+      const int okn = I.newton(A.mode, t, tp, A.gmin, A.max_steps, &its);
+      for (int i = threadIdx.x; i < A.S; i += NT)
+        A.z_out[(long long)n * BS + (long long)b * A.S + i] = I.z[i];
+      if (threadIdx.x == 0) {
+        A.conv[(long long)n * A.B + b] = okn;
+        A.iters[(long long)n * A.B + b] = its;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+static int fused_eligible(const Topo& t, int precision, size_t* smem_out) {
+  if (t.kmax > 32 || t.n_seg != 1) return VXG_ERR_TOO_LARGE;
+  const int max_scr = (int)std::max(t.max_schur, t.max_bord);
+  const size_t smem = precision == VXG_F32
+                          ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
+                                                (int)t.n_jac_slots, (int)t.work, max_scr).total
+                          : fused_layout<double>(t.S, (int)t.nnz, (int)t.n_res_slots,
+                                                 (int)t.n_jac_slots, (int)t.work, max_scr).total;
+  int dev = 0, max_optin = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  *smem_out = smem;
+  if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+  return VXG_OK;
+}
+
+template <typename T, int NT>
+static int launch_fused(const FusedArgs& a, size_t smem, cudaStream_t s) {
+  auto kern = fused_kernel<T, NT>;
+  VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, sms = 0, per_sm = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  VXG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+  const int grid = std::max(1, std::min(a.B, sms * std::max(per_sm, 1)));
+  kern<<<grid, NT, smem, s>>>(a);
+  VXG_LAUNCHED();
+  return VXG_OK;
+}
+
+}  // namespace vxg
+
+using namespace vxg;
+
+extern "C" int vxg_fused_smem(const vxg_handle* h, int32_t precision, size_t* bytes) {
+  if (!h || !bytes || (precision != VXG_F64 && precision != VXG_F32)) return VXG_ERR_INVALID;
+  return fused_eligible(h->t, precision, bytes);
+}
+
+extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                             int32_t mode, int32_t n_t, const double* ts, const double* z0,
+                             int32_t dc_first, const double* gmins, int32_t gmin_steps,
+                             int32_t direct_steps, double gmin, const vxg_newton_opts* o,
+                             double* z_out, int32_t* converged, int32_t* iters, void* stream) {
+  if (!h || batch <= 0 || !params || n_t <= 0 || !ts || !z0 || !z_out || !converged ||
+      !iters || !o || mode < 0 || mode > 2 || (n_t > 1 && mode == VXG_MODE_DC) ||
+      (dc_first && gmin_steps > 0 && !gmins) || o->max_steps < 0 || o->refine < 0 ||
+      (o->precision != VXG_F64 && o->precision != VXG_F32))
+    return VXG_ERR_INVALID;
+  const Topo& t = h->t;
+  size_t smem = 0;
+  int st = fused_eligible(t, o->precision, &smem);
+  if (st) return st;
+  FusedArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.gt = make_table(t, params);
+  a.S = t.S;
+  a.nv = t.nv;
+  a.nnz = (int)t.nnz;
+  a.n_res = (int)t.n_res_slots;
+  a.n_jac = (int)t.n_jac_slots;
+  a.work = (int)t.work;
+  a.n_levels = t.n_levels;
+  a.max_scr = (int)std::max(t.max_schur, t.max_bord);
+  a.res_ptr = t.res_ptr;
+  a.res_src = t.res_src;
+  a.jac_ptr = t.jac_ptr;
+  a.jac_src = t.jac_src;
+  a.a_pos = t.a_pos;
+  a.indptr = t.indptr;
+  a.indices = t.indices;
+  a.rows = t.rows;
+  a.sn_k = t.sn_k;
+  a.sn_r = t.sn_r;
+  a.sn_piv = t.sn_piv;
+  a.sn_bord = t.sn_bord;
+  a.sn_panel = t.sn_panel;
+  a.sn_piv_ptr = t.sn_piv_ptr;
+  a.sn_bord_ptr = t.sn_bord_ptr;
+  a.lv_ptr = t.d_lv_ptr;
+  a.lv_sn = t.lv_sn;
+  a.lv_schur_off = t.lv_schur_off;
+  a.lv_bord_off = t.lv_bord_off;
+  a.lv_st_ptr = t.d_lv_st_ptr;
+  a.st_tgt = t.st_tgt;
+  a.st_ptr = t.st_ptr;
+  a.st_src = t.st_src;
+  a.lv_bt_ptr = t.d_lv_bt_ptr;
+  a.bt_tgt = t.bt_tgt;
+  a.bt_ptr = t.bt_ptr;
+  a.bt_src = t.bt_src;
+  a.B = batch;
+  a.mode = mode;
+  a.n_t = n_t;
+  a.max_steps = o->max_steps;
+  a.refine = o->refine;
+  a.dc_first = dc_first;
+  a.gmin_steps = gmin_steps;
+  a.direct_steps = direct_steps;
+  a.rtol = o->rtol;
+  a.atol = o->atol;
+  a.max_dv = o->max_dv;
+  a.gmin = gmin;
+  a.ts = ts;
+  a.gmins = gmins;
+  a.z0 = z0;
+  a.z_out = z_out;
+  a.conv = converged;
+  a.iters = iters;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (o->precision == VXG_F32) return launch_fused<float, 128>(a, smem, s);
+  return launch_fused<double, 128>(a, smem, s);
+}

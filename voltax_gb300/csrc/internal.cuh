@@ -52,6 +52,7 @@ struct Topo {
   int* h_lv_rmax;  // largest r per level
   int* lv_sn;
   long long *lv_schur_off, *lv_bord_off;
+  long long *d_lv_ptr, *d_lv_st_ptr, *d_lv_bt_ptr;  // device copies of the level pointers
   long long *st_tgt, *st_ptr, *st_src;
   int* bt_tgt;
   long long *bt_ptr, *bt_src;

@@ -226,12 +226,12 @@ class Engine:
             rows_per_group.append(rows)
             n = circuit.elements[name].size
             batched = any(r.ndim == 2 for r in rows)
+            dev_rows = [r.detach().to(self.device, torch.float64) for r in rows]
             if batched:
-                t = torch.stack([r.detach().expand(B, n) if r.ndim == 2 else
-                                 r.detach().expand(B, n) for r in rows])
+                t = torch.stack([r.expand(B, n) for r in dev_rows])
             else:
-                t = torch.stack([r.detach().reshape(n) for r in rows])[:, None, :]
-            t = t.to(self.device, torch.float64).contiguous()
+                t = torch.stack([r.reshape(n) for r in dev_rows])[:, None, :]
+            t = t.contiguous()
             packed.append(t)
             Bp = t.shape[1]
             arr[i] = L.GroupParams(t.data_ptr(), Bp * n, n if Bp > 1 else 0)
