@@ -1,0 +1,425 @@
+/*
+ * cvx.c -- compiled CPU restatement of the voltax Newton loop, used as the
+ * timed CPU baseline (TEST INFRASTRUCTURE: only tests/, the smoke check and
+ * bench.py's CPU legs call it; the product never does).
+ *
+ * One circuit instance, FP64 throughout, single-threaded:
+ *   device physics + local Jacobians   voltax/elements/{passive,sources,mosfet}.py,
+ *                                      voltax/signals.py:58-114 (derivatives by
+ *                                      hand; voltax uses forward-mode AD)
+ *   stamping (sequential, canonical    voltax/sparse.py:220-249, circuit.py:209-226
+ *   group/device/row/column order)
+ *   block-LDU refactorization per      voltax/sparse.py:543-572 (per supernode in
+ *   supernode, partial pivoting in     postorder rather than padded per-level
+ *   the pivot block; solves            batches, i.e. without the padding work)
+ *                                      voltax/sparse.py:575-595
+ *   damped Newton, gmin stepping,      voltax/analysis.py:208-266, 333-378,
+ *   DC, BE / trapezoidal transient     410-480
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4 };
+enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
+enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
+
+typedef struct {
+  int kind, n, T, K, wave, n_params, int_offset;
+  const int* nodes;     /* n*T, -1 = ground */
+  const double* params; /* n_params rows of n values */
+  const int* jpos;      /* n*m*m pattern positions, nnz = dropped */
+} cvx_group;
+
+typedef struct {
+  int S, nv, nnz, n_groups;
+  const cvx_group* groups;
+  const long long* indptr;
+  const int* indices;
+  const int* rows;
+  int n_sn;
+  const int* k;
+  const int* r;
+  const long long* panel;
+  const long long* piv_ptr;
+  const int* piv;
+  const long long* bord_ptr;
+  const int* bord;
+  const long long* a_pos;
+  long long work;
+  const long long* schur_ptr; /* n_sn+1 */
+  const long long* schur_tgt; /* per supernode r*r panel positions */
+} cvx_sys;
+
+typedef struct {
+  int max_steps;
+  double rtol, atol, max_dv, gmin;
+  int gmin_steps, direct_steps;
+  const double* gmins; /* gmin_steps + 1 */
+} cvx_opts;
+
+/* ------------------------------------------------------------- waveforms */
+static double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+static double py_mod(double x, double y) {
+  double r = fmod(x, y);
+  if (r != 0.0 && ((r < 0.0) != (y < 0.0))) r += y;
+  return r;
+}
+
+static double wave(const cvx_group* g, int d, double t) {
+  const double* p = g->params;
+  const int n = g->n;
+  if (g->wave == W_CONST) return p[d];
+  if (g->wave == W_STEP) {
+    double v0 = p[d], v1 = p[n + d], delay = p[2 * n + d], rise = p[3 * n + d];
+    return v0 + (v1 - v0) * clamp01((t - delay) / rise);
+  }
+  {
+    double v1 = p[d], v2 = p[n + d], delay = p[2 * n + d], rise = p[3 * n + d];
+    double fall = p[4 * n + d], width = p[5 * n + d], period = p[6 * n + d];
+    double tc = py_mod(t - delay, period);
+    double up = clamp01(tc / (rise + 1e-30));
+    double tfe = rise + width + fall;
+    double down = clamp01((tfe - tc) / (fall + 1e-30));
+    double value = v1 + (v2 - v1) * (up < down ? up : down);
+    return t < delay ? v1 : value;
+  }
+}
+
+/* ----------------------------------------------------------------- EKV */
+static void softplus2(double x, double* sp, double* sg) {
+  double e = exp(-fabs(x));
+  *sp = (x > 0.0 ? x : 0.0) + log1p(e);
+  *sg = x >= 0.0 ? 1.0 / (1.0 + e) : e / (1.0 + e);
+}
+
+/* outputs I, Q (4) and J = cf dI/dv + cq dQ/dv (4x4) of one EKV device */
+static void ekv(const cvx_group* g, int d, const double* v, double cf, double cq, int wj,
+                double* I, double* Q, double* J) {
+  const double* p = g->params;
+  const int n = g->n;
+  const double sign = p[d], i_spec = p[n + d], vth = p[2 * n + d], dvth = p[3 * n + d];
+  const double nn = p[4 * n + d], vt = p[5 * n + d], lam = p[6 * n + d];
+  const double c_ox = p[7 * n + d], cov_w = p[8 * n + d];
+  const double vd = sign * v[0], vg = sign * v[1], vs = sign * v[2], vb = sign * v[3];
+  const double two_vt = 2.0 * vt;
+  const double vp = (vg - vb - vth - dvth) / nn;
+  double spf, sgf, spr, sgr;
+  softplus2((vp - (vs - vb)) / two_vt, &spf, &sgf);
+  softplus2((vp - (vd - vb)) / two_vt, &spr, &sgr);
+  const double i_f = spf * spf, i_r = spr * spr;
+  const double dif = 2.0 * spf * sgf, dir = 2.0 * spr * sgr;
+  const double g1 = 1.0 / nn;
+  const double daf[4] = {0.0, g1 / two_vt, -1.0 / two_vt, (1.0 - g1) / two_vt};
+  const double dar[4] = {-1.0 / two_vt, g1 / two_vt, 0.0, (1.0 - g1) / two_vt};
+  const double vds = vd - vs;
+  const double root = sqrt(vds * vds + 1e-3 * 1e-3);
+  const double mfac = 1.0 + lam * (root - 1e-3);
+  const double ids = i_spec * (i_f - i_r) * mfac;
+  const double dsa = vds / root;
+  const double dmf[4] = {lam * dsa, 0.0, -lam * dsa, 0.0};
+  I[0] = sign * ids;
+  I[1] = 0.0;
+  I[2] = sign * -ids;
+  I[3] = 0.0;
+  const double xf = sqrt(0.25 + i_f), xr = sqrt(0.25 + i_r);
+  const double scale = c_ox * nn * vt;
+  const double s = xf + xr, s2 = s * s, s3 = s2 * s;
+  const double c415 = 4.0 / 15.0;
+  const double nd = 3 * xr * xr * xr + 6 * xr * xr * xf + 4 * xr * xf * xf + 2 * xf * xf * xf;
+  const double ns = 3 * xf * xf * xf + 6 * xf * xf * xr + 4 * xf * xr * xr + 2 * xr * xr * xr;
+  const double q_d = -scale * (c415 * nd / s2 - 0.5);
+  const double q_s = -scale * (c415 * ns / s2 - 0.5);
+  const double q_i = q_d + q_s;
+  const double kb = -(nn - 1.0) / nn;
+  const double q_b = kb * (c_ox * (vg - vb) + q_i);
+  const double q_g = -(q_i + q_b);
+  const double q_gs = cov_w * (vg - vs), q_gd = cov_w * (vg - vd);
+  Q[0] = sign * (q_d - q_gd);
+  Q[1] = sign * (q_g + (q_gs + q_gd));
+  Q[2] = sign * (q_s - q_gs);
+  Q[3] = sign * q_b;
+  if (!wj) return;
+  const double gd_f = ((6 * xr * xr + 8 * xr * xf + 6 * xf * xf) * s - 2 * nd) / s3;
+  const double gd_r = ((9 * xr * xr + 12 * xr * xf + 4 * xf * xf) * s - 2 * nd) / s3;
+  const double gs_f = ((9 * xf * xf + 12 * xf * xr + 4 * xr * xr) * s - 2 * ns) / s3;
+  const double gs_r = ((6 * xf * xf + 8 * xf * xr + 6 * xr * xr) * s - 2 * ns) / s3;
+  const double dxf_da = dif / (2.0 * xf), dxr_da = dir / (2.0 * xr);
+  for (int kk = 0; kk < 4; ++kk) {
+    const double dids = i_spec * ((dif * daf[kk] - dir * dar[kk]) * mfac + (i_f - i_r) * dmf[kk]);
+    const double dxf = dxf_da * daf[kk], dxr = dxr_da * dar[kk];
+    const double dqd = -scale * c415 * (gd_f * dxf + gd_r * dxr);
+    const double dqs = -scale * c415 * (gs_f * dxf + gs_r * dxr);
+    const double dqi = dqd + dqs;
+    const double dvgb = (kk == 1 ? 1.0 : 0.0) - (kk == 3 ? 1.0 : 0.0);
+    const double dqb = kb * (c_ox * dvgb + dqi);
+    const double dqg = -(dqi + dqb);
+    const double dgs = cov_w * ((kk == 1 ? 1.0 : 0.0) - (kk == 2 ? 1.0 : 0.0));
+    const double dgd = cov_w * ((kk == 1 ? 1.0 : 0.0) - (kk == 0 ? 1.0 : 0.0));
+    J[0 * 4 + kk] = cf * dids + cq * (dqd - dgd);
+    J[1 * 4 + kk] = cq * (dqg + (dgs + dgd));
+    J[2 * 4 + kk] = cf * -dids + cq * (dqs - dgs);
+    J[3 * 4 + kk] = cq * dqb;
+  }
+}
+
+/* f (cf_on), q and the CSR Jacobian (cf df + cq dq + gmin on node diagonals) */
+static void stamp(const cvx_sys* s, const double* z, double t, double cf, double cq,
+                  double gmin, double* f, double* q, double* data) {
+  const int S = s->S;
+  if (f) memset(f, 0, sizeof(double) * S);
+  if (q) memset(q, 0, sizeof(double) * S);
+  if (data) memset(data, 0, sizeof(double) * (s->nnz + 1));
+  for (int gi = 0; gi < s->n_groups; ++gi) {
+    const cvx_group* g = &s->groups[gi];
+    const int m = g->T + g->K;
+    for (int d = 0; d < g->n; ++d) {
+      double u[4], I[4] = {0, 0, 0, 0}, Q[4] = {0, 0, 0, 0}, J[16];
+      int row[4];
+      for (int i = 0; i < g->T; ++i) {
+        const int nd = g->nodes[d * g->T + i];
+        u[i] = nd >= 0 ? z[nd] : 0.0;
+        row[i] = nd;
+      }
+      for (int i = 0; i < g->K; ++i) {
+        row[g->T + i] = g->int_offset + d * g->K + i;
+        u[g->T + i] = z[row[g->T + i]];
+      }
+      memset(J, 0, sizeof(J));
+      switch (g->kind) {
+        case K_COND: {
+          const double gg = g->params[d], i = (u[0] - u[1]) * gg;
+          I[0] = i;
+          I[1] = -i;
+          J[0] = cf * gg; J[1] = -cf * gg; J[2] = -cf * gg; J[3] = cf * gg;
+          break;
+        }
+        case K_CAP: {
+          const double c = g->params[d], qq = c * (u[0] - u[1]);
+          Q[0] = qq;
+          Q[1] = -qq;
+          J[0] = cq * c; J[1] = -cq * c; J[2] = -cq * c; J[3] = cq * c;
+          break;
+        }
+        case K_VSRC:
+          I[0] = u[2];
+          I[1] = -u[2];
+          I[2] = (u[0] - u[1]) - wave(g, d, t);
+          J[2] = cf; J[5] = -cf; J[6] = cf; J[7] = -cf;
+          break;
+        case K_ISRC: {
+          const double i = wave(g, d, t);
+          I[0] = i;
+          I[1] = -i;
+          break;
+        }
+        case K_EKV:
+          ekv(g, d, u, cf, cq, data != 0, I, Q, J);
+          break;
+      }
+      for (int i = 0; i < m; ++i) {
+        if (row[i] < 0) continue;
+        if (f) f[row[i]] += I[i];
+        if (q) q[row[i]] += Q[i];
+      }
+      if (data) {
+        const int* jp = g->jpos + (long long)d * m * m;
+        for (int e = 0; e < m * m; ++e) data[jp[e]] += J[e];
+      }
+    }
+  }
+  if (data)
+    for (int e = 0; e < s->nnz; ++e)
+      if (s->rows[e] < s->nv && s->indices[e] == s->rows[e]) data[e] += gmin;
+}
+
+/* ------------------------------------------------------- factor / solve */
+static void factor(const cvx_sys* s, const double* data, double* work, int* perm, double* tmp) {
+  memset(work, 0, sizeof(double) * s->work);
+  for (int e = 0; e < s->nnz; ++e) work[s->a_pos[e]] = data[e];
+  for (int j = 0; j < s->n_sn; ++j) {
+    const int k = s->k[j], r = s->r[j];
+    double* A = work + s->panel[j];
+    double* F12 = A + (long long)k * k;
+    double* F21 = F12 + (long long)k * r;
+    for (int c = 0; c < k; ++c) { /* Gauss-Jordan, partial pivoting */
+      int p = c;
+      double best = fabs(A[c * k + c]);
+      for (int i = c + 1; i < k; ++i)
+        if (fabs(A[i * k + c]) > best) { best = fabs(A[i * k + c]); p = i; }
+      perm[c] = p;
+      if (p != c)
+        for (int jj = 0; jj < k; ++jj) { double t = A[p * k + jj]; A[p * k + jj] = A[c * k + jj]; A[c * k + jj] = t; }
+      const double dd = A[c * k + c];
+      A[c * k + c] = 1.0;
+      for (int jj = 0; jj < k; ++jj) A[c * k + jj] /= dd;
+      for (int i = 0; i < k; ++i) {
+        if (i == c) continue;
+        const double fct = A[i * k + c];
+        A[i * k + c] = 0.0;
+        for (int jj = 0; jj < k; ++jj) A[i * k + jj] -= fct * A[c * k + jj];
+      }
+    }
+    for (int c = k - 1; c >= 0; --c)
+      if (perm[c] != c)
+        for (int i = 0; i < k; ++i) { double t = A[i * k + c]; A[i * k + c] = A[i * k + perm[c]]; A[i * k + perm[c]] = t; }
+    if (!r) continue;
+    /* Ub = W F12 */
+    for (int cc = 0; cc < r; ++cc) {
+      for (int l = 0; l < k; ++l) tmp[l] = F12[(long long)l * r + cc];
+      for (int i = 0; i < k; ++i) {
+        double acc = 0.0;
+        for (int l = 0; l < k; ++l) acc += A[i * k + l] * tmp[l];
+        F12[(long long)i * r + cc] = acc;
+      }
+    }
+    /* Schur: work[target] -= F21 Ub; then Lb = F21 W */
+    const long long* tg = s->schur_tgt + s->schur_ptr[j];
+    for (int a = 0; a < r; ++a) {
+      const double* row = F21 + (long long)a * k;
+      for (int b = 0; b < r; ++b) {
+        double acc = 0.0;
+        for (int l = 0; l < k; ++l) acc += row[l] * F12[(long long)l * r + b];
+        work[tg[(long long)a * r + b]] -= acc;
+      }
+      for (int jj = 0; jj < k; ++jj) {
+        double acc = 0.0;
+        for (int l = 0; l < k; ++l) acc += row[l] * A[l * k + jj];
+        tmp[jj] = acc;
+      }
+      memcpy(F21 + (long long)a * k, tmp, sizeof(double) * k);
+    }
+  }
+}
+
+static void solve(const cvx_sys* s, const double* work, double* x, double* tmp) {
+  for (int j = 0; j < s->n_sn; ++j) {
+    const int k = s->k[j], r = s->r[j];
+    const double* W = work + s->panel[j];
+    const double* Lb = W + (long long)k * k + (long long)k * r;
+    const int* piv = s->piv + s->piv_ptr[j];
+    const int* brd = s->bord + s->bord_ptr[j];
+    for (int l = 0; l < k; ++l) tmp[l] = x[piv[l]];
+    for (int a = 0; a < r; ++a) {
+      double acc = 0.0;
+      for (int l = 0; l < k; ++l) acc += Lb[(long long)a * k + l] * tmp[l];
+      x[brd[a]] -= acc;
+    }
+    for (int i = 0; i < k; ++i) {
+      double acc = 0.0;
+      for (int l = 0; l < k; ++l) acc += W[i * k + l] * tmp[l];
+      x[piv[i]] = acc;
+    }
+  }
+  for (int j = s->n_sn - 1; j >= 0; --j) {
+    const int k = s->k[j], r = s->r[j];
+    const double* Ub = work + s->panel[j] + (long long)k * k;
+    const int* piv = s->piv + s->piv_ptr[j];
+    const int* brd = s->bord + s->bord_ptr[j];
+    for (int i = 0; i < k; ++i) {
+      double acc = 0.0;
+      for (int a = 0; a < r; ++a) acc += Ub[(long long)i * r + a] * x[brd[a]];
+      x[piv[i]] -= acc;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- Newton */
+typedef struct {
+  double *f, *q, *fp, *qp, *data, *work, *dz, *tmp;
+  int* perm;
+} ws_t;
+
+static int newton(const cvx_sys* s, const cvx_opts* o, ws_t* w, int mode, double t, double tp,
+                  double gmin, int max_steps, double* z, int* iters) {
+  const int S = s->S;
+  const double cf = mode == M_TRAP ? 0.5 : 1.0;
+  const double cq = mode == M_DC ? 0.0 : 1.0 / (t - tp);
+  const double h = t - tp;
+  int done = 0, it = 0;
+  while (it < max_steps && !done) {
+    stamp(s, z, t, cf, cq, gmin, w->f, mode == M_DC ? 0 : w->q, w->data);
+    for (int i = 0; i < S; ++i) {
+      const double gm = i < s->nv ? gmin * z[i] : 0.0;
+      double r;
+      if (mode == M_DC) r = w->f[i] + gm;
+      else if (mode == M_BE) r = (w->q[i] - w->qp[i]) / h + w->f[i] + gm;
+      else r = (w->q[i] - w->qp[i]) / h + 0.5 * (w->f[i] + w->fp[i]) + gm;
+      w->dz[i] = -r;
+    }
+    factor(s, w->data, w->work, w->perm, w->tmp);
+    solve(s, w->work, w->dz, w->tmp);
+    double m = 0.0;
+    int nan_seen = 0;
+    for (int i = 0; i < s->nv; ++i) {
+      const double v = fabs(w->dz[i]);
+      if (isnan(v)) nan_seen = 1;
+      else if (v > m) m = v;
+    }
+    const double dv = nan_seen ? NAN : m;
+    const double qd = o->max_dv / (dv + 1e-300);
+    const double scale = isnan(qd) ? qd : (qd < 1.0 ? qd : 1.0);
+    int ok = 1;
+    for (int i = 0; i < S; ++i) {
+      const double zn = z[i] + scale * w->dz[i];
+      if (!(fabs(w->dz[i]) <= o->atol + o->rtol * fabs(zn))) ok = 0;
+      if (!isfinite(zn)) ok = 0;
+      z[i] = zn;
+    }
+    done = ok && scale == 1.0;
+    ++it;
+  }
+  *iters = it;
+  return done;
+}
+
+int cvx_run(const cvx_sys* s, const cvx_opts* o, int mode, int n_t, const double* ts,
+            const double* z0, int dc_first, double* z_out, int* conv, int* iters) {
+  const int S = s->S;
+  int maxk = 1;
+  for (int j = 0; j < s->n_sn; ++j) {
+    if (s->k[j] > maxk) maxk = s->k[j];
+    if (s->r[j] > maxk) maxk = s->r[j];
+  }
+  ws_t w;
+  w.f = calloc(S, sizeof(double));
+  w.q = calloc(S, sizeof(double));
+  w.fp = calloc(S, sizeof(double));
+  w.qp = calloc(S, sizeof(double));
+  w.dz = calloc(S, sizeof(double));
+  w.data = calloc(s->nnz + 1, sizeof(double));
+  w.work = calloc(s->work > 0 ? s->work : 1, sizeof(double));
+  w.tmp = calloc(maxk + S, sizeof(double));
+  w.perm = calloc(maxk, sizeof(int));
+  double* z = calloc(S, sizeof(double));
+  if (!w.f || !w.q || !w.fp || !w.qp || !w.dz || !w.data || !w.work || !w.tmp || !w.perm || !z)
+    return 1;
+  memcpy(z, z0, sizeof(double) * S);
+  int ok = 1, it = 0;
+  if (dc_first) {
+    ok = newton(s, o, &w, M_DC, ts[0], 0.0, o->gmin,
+                o->gmin_steps > 0 ? o->direct_steps : o->max_steps, z, &it);
+    if (!ok && o->gmin_steps > 0) {
+      memcpy(z, z0, sizeof(double) * S);
+      for (int k = 1; k <= o->gmin_steps; ++k) {
+        int its = 0;
+        ok = newton(s, o, &w, M_DC, ts[0], 0.0, o->gmins[k], o->max_steps, z, &its);
+        it += its;
+      }
+    }
+  }
+  memcpy(z_out, z, sizeof(double) * S);
+  conv[0] = ok;
+  iters[0] = it;
+  for (int n = 1; n < n_t; ++n) {
+    stamp(s, z, ts[n - 1], 1.0, 0.0, 0.0, mode == M_TRAP ? w.fp : 0, w.qp, 0);
+    int its = 0;
+    conv[n] = newton(s, o, &w, mode, ts[n], ts[n - 1], o->gmin, o->max_steps, z, &its);
+    iters[n] = its;
+    memcpy(z_out + (long long)n * S, z, sizeof(double) * S);
+  }
+  free(w.f); free(w.q); free(w.fp); free(w.qp); free(w.dz); free(w.data); free(w.work);
+  free(w.tmp); free(w.perm); free(z);
+  return 0;
+}

@@ -215,3 +215,22 @@ def test_power_grid_dc_matches_superlu():
     r0 = ost.dc_residual(c, np.zeros(c.size), 0.0, 1e-12)
     ref = spla.splu(st.to_scipy(A).tocsc()).solve(-r0)
     np.testing.assert_allclose(z, ref, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap")])
+def test_compiled_baseline_matches_oracle(name, method):
+    """oracle/cvx.c (the timed CPU baseline) equals the torch restatement."""
+    from oracle import cbase
+    c = _cases()[name]()
+    st = symbolic.structure(c)
+    ts = np.linspace(0.0, 40e-12, 9)
+    z0 = None
+    if name == "ring":
+        z0 = workloads.ring_initial_state(c, [f"n{k}" for k in range(9)]).numpy()
+    zc, okc, itc = cbase.CSystem(c, st, st.plan).run(ts, z0=z0, method=method,
+                                                      dc_first=z0 is None)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc" if z0 is None else z0,
+                                method=method)
+    assert okc.all() and okr.all()
+    assert np.array_equal(itc[1:], itr[1:])
+    np.testing.assert_allclose(zc, zr, rtol=1e-10, atol=1e-12)

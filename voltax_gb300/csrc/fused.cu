@@ -286,9 +286,9 @@ struct Instance {
   }
 
   // CSR values (+gmin) and the panels; residual rhs = -r
-  __device__ void assemble_system(double gmin, double h) {
+  __device__ void assemble_system(int mode, double gmin, double h) {
     for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
-    assemble_res(f, A.mode == VXG_MODE_DC ? nullptr : q);
+    assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
     for (int e = threadIdx.x; e < A.nnz; e += NT) {
       double acc = 0.0;
       for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += cj[A.jac_src[p]];
@@ -301,9 +301,9 @@ struct Instance {
     for (int i = threadIdx.x; i < A.S; i += NT) {
       const double gm = i < A.nv ? gmin * z[i] : 0.0;
       double r;
-      if (A.mode == VXG_MODE_DC)
+      if (mode == VXG_MODE_DC)
         r = f[i] + gm;
-      else if (A.mode == VXG_MODE_BE)
+      else if (mode == VXG_MODE_BE)
         r = (q[i] - qp[i]) / h + f[i] + gm;
       else
         r = (q[i] - qp[i]) / h + 0.5 * (f[i] + fp[i]) + gm;
@@ -443,7 +443,7 @@ struct Instance {
     while (it < max_steps && !done) {
       eval(z, t, cfc, cqc, true, !dc, true);
       __syncthreads();
-      assemble_system(gmin, h);
+      assemble_system(mode, gmin, h);
       factor();
       solve(sizeof(T) == sizeof(float) ? A.refine : 0);
       done = update();
