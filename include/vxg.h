@@ -256,6 +256,20 @@ int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
                   int32_t direct_steps, double gmin, const vxg_newton_opts* opts,
                   double* z_out, int32_t* converged, int32_t* iters, void* stream);
 
+/* vxg_factor for callers that cannot allocate device memory when they
+ * refactor (allocation-free plugin or custom-call hooks, real-time loops,
+ * hosts whose allocator is owned by another runtime). No counterpart in
+ * the reference. The per-level Schur scratch that vxg_factor takes from the
+ * caller's workspace lives instead in an 8 MiB array inside this library;
+ * the call allocates nothing, and data and factors are still the caller's.
+ * Returns VXG_ERR_TOO_LARGE when batch * (largest level Schur scratch) *
+ * element size exceeds 8 MiB. Every GPU that loads the library holds the
+ * 8 MiB until exit. All calls share the array: calls that overlap on a GPU
+ * race, so serialise them. The first call on a device looks up the array's
+ * address; make it before any stream capture. */
+int vxg_factor_static(const vxg_handle* h, int32_t batch, int32_t precision,
+                      const double* data, void* factors, void* stream);
+
 /* Kernels this library has launched since it was loaded (a diagnostic
  * counter; no counterpart in the reference). */
 uint64_t vxg_launch_count(void);

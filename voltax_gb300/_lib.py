@@ -79,6 +79,7 @@ SIGNATURES = {
     "vxg_fused_smem": ([P, I32, C.POINTER(C.c_size_t)], I32),
     "vxg_fused_run": ([P, I32, C.POINTER(GroupParams), I32, I32, P, P, I32, P, I32, I32, F64,
                        C.POINTER(NewtonOpts), P, P, P, P], I32),
+    "vxg_factor_static": ([P, I32, I32, P, P, P], I32),
     "vxg_launch_count": ([], C.c_uint64),
     "vxg_param_vjp": ([P, I32, C.POINTER(GroupParams), P, F64, F64, F64, P,
                        C.POINTER(P), P], I32),

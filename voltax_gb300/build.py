@@ -17,7 +17,8 @@ SRC = HERE / "csrc"
 OUT = HERE / "_lib"
 INCLUDE = HERE.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["stamp.cu", "factor.cu", "solve.cu", "newton.cu", "capi.cu", "fused.cu"]
+SOURCES = ["stamp.cu", "factor.cu", "solve.cu", "newton.cu", "capi.cu", "fused.cu",
+           "factor_static.cu"]
 
 
 def nvcc() -> str:

@@ -30,6 +30,8 @@ void set_error(cudaError_t e) {
   std::snprintf(g_err, sizeof(g_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
+char* last_error_buffer() { return g_err; }
+
 size_t elem_size(int precision) { return precision == VXG_F32 ? sizeof(float) : sizeof(double); }
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }

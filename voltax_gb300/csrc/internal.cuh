@@ -71,6 +71,7 @@ struct vxg_handle {
 
 namespace vxg {
 void count_launch();
+char* last_error_buffer();  // this thread's vxg_last_error text (256 bytes)
 }
 
 // Count one kernel launch and surface launch errors.
