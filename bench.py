@@ -40,17 +40,70 @@ INSTANCES = 4096
 T_STOP, N_T = 1e-9, 501
 
 
+class Workload:
+    """One benchmark configuration: how to build it and what one solve is."""
+
+    def __init__(self, name, analysis, method, t_stop, n_t, outputs, default_instances):
+        self.name, self.analysis, self.method = name, analysis, method
+        self.t_stop, self.n_t, self.outputs = t_stop, n_t, outputs
+        self.default_instances = default_instances
+
+    def circuit(self, instances, seed=0):
+        from voltax_gb300 import workloads as wl
+        if self.name == "adder_mc":
+            return wl.mirror_adder_mc(instances, seed=seed)
+        if self.name == "ring101":
+            return wl.ring_oscillator(101)[0]
+        if self.name == "grid100":
+            return wl.power_grid(100, seed=seed)
+        raise ValueError(self.name)
+
+    def ic(self, circuit):
+        """Initial condition: "dc" or a state vector."""
+        if self.name == "ring101":
+            from voltax_gb300 import workloads as wl
+            return wl.ring_initial_state(circuit, [f"n{k}" for k in range(101)])
+        return "dc"
+
+    def times(self, n_t=None):
+        n = self.n_t if n_t is None else n_t
+        return np.linspace(0.0, self.t_stop, n) if self.analysis == "transient" else \
+            np.zeros(1)
+
+    def label(self, instances, n_t):
+        if self.name == "adder_mc":
+            return f"mirror_adder_mc{instances}"
+        if self.name == "ring101":
+            return f"ring_oscillator101_trap{n_t}"
+        return "power_grid100_dc"
+
+
+WORKLOADS = {
+    "adder_mc": Workload("adder_mc", "transient", "be", T_STOP, N_T,
+                         ["s0", "s1", "s2", "s3", "co"], INSTANCES),
+    "ring101": Workload("ring101", "transient", "trap", 2e-9, 2001, ["n0", "n50", "n100"], 1),
+    "grid100": Workload("grid100", "dc", None, 0.0, 1, None, 1),
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--instances", type=int, default=INSTANCES)
-    ap.add_argument("--time-points", type=int, default=N_T)
+    ap.add_argument("--workload", default="adder_mc", choices=sorted(WORKLOADS))
+    ap.add_argument("--instances", type=int, default=None)
+    ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    return ap.parse_args()
+    a = ap.parse_args()
+    w = WORKLOADS[a.workload]
+    if a.instances is None:
+        a.instances = w.default_instances
+    if a.time_points is None:
+        a.time_points = w.n_t
+    return a
 
 
 # ----------------------------------------------------------------- clocks
@@ -102,29 +155,38 @@ class Clocks:
 
 
 # ----------------------------------------------------------------- CPU legs
-def _cpu_systems(instances, count, seed=0):
+def _cpu_systems(w, instances, count, seed=0):
     from oracle import cbase
-    from voltax_gb300 import symbolic, workloads
-    c = workloads.mirror_adder_mc(instances, seed=seed)
+    from voltax_gb300 import symbolic
+    c = w.circuit(instances, seed=seed)
     st = symbolic.structure(c)
-    return [cbase.CSystem(c, st, st.plan, b % instances) for b in range(count)]
+    ic = w.ic(c)
+    z0 = None if isinstance(ic, str) else ic.numpy()
+    return [cbase.CSystem(c, st, st.plan, b % c.batch) for b in range(count)], z0
 
 
-def cpu_baseline(n_t=N_T, instances=INSTANCES, min_seconds=10.0):
+def _cpu_run(w, sysm, z0, ts):
+    if w.analysis == "dc":
+        return sysm.run(ts[:1], dc_first=True)
+    return sysm.run(ts, z0=z0, method=w.method, dc_first=z0 is None)
+
+
+def cpu_baseline(w, n_t, instances, min_seconds=10.0):
     """The compiled CPU restatement (oracle/cvx.c), one thread, whole
-    instances (DC + n_t - 1 BE steps) until `min_seconds` have passed."""
-    systems = _cpu_systems(instances, 64)
-    ts = np.linspace(0.0, T_STOP, n_t)
-    systems[0].run(ts[:3])
+    instances until `min_seconds` have passed."""
+    systems, z0 = _cpu_systems(w, instances, min(instances, 64))
+    ts = w.times(n_t)
+    _cpu_run(w, systems[0], z0, ts[:3])
     solves, t0, i = 0, time.perf_counter(), 0
-    while time.perf_counter() - t0 < min_seconds and i < len(systems):
-        _, ok, _ = systems[i].run(ts)
-        solves += n_t
+    while time.perf_counter() - t0 < min_seconds and i < 10000:
+        _cpu_run(w, systems[i % len(systems)], z0, ts)
+        solves += len(ts)
         i += 1
     secs = time.perf_counter() - t0
+    what = "DC solve" if w.analysis == "dc" else f"DC + {len(ts) - 1} {w.method.upper()} steps"
     return {"value": solves / secs, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{i} whole instances (DC + {n_t - 1} BE steps each) on 1 thread, "
-                      f"{secs:.1f} s; compiled C restatement oracle/cvx.c"}
+            "sample": f"{i} whole instances ({what} each) on 1 thread, {secs:.1f} s; "
+                      "compiled C restatement oracle/cvx.c"}
 
 
 def run_reference(a):
@@ -132,15 +194,18 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    w = WORKLOADS[a.workload]
     cores = os.cpu_count() or 1
-    per_thread = 4
-    ts = np.linspace(0.0, T_STOP, a.time_points)
-    systems = _cpu_systems(a.instances, cores * per_thread)
+    per_thread = 4 if w.analysis == "transient" and w.name == "adder_mc" else 1
+    if w.name == "grid100":
+        per_thread = 8
+    ts = w.times(a.time_points)
+    systems, z0 = _cpu_systems(w, a.instances, cores * per_thread)
 
     def work(i):  # ctypes releases the GIL inside cvx_run
         for j in range(per_thread):
-            systems[i * per_thread + j].run(ts)
-        return per_thread * a.time_points
+            _cpu_run(w, systems[i * per_thread + j], z0, ts)
+        return per_thread * len(ts)
 
     with ThreadPoolExecutor(cores) as ex:
         for _ in range(a.warmup):
@@ -152,13 +217,13 @@ def run_reference(a):
             times.append(time.perf_counter() - t0)
     total = sum(times)
     value = solves / total
-    sample = (f"{cores} threads x {per_thread} whole instances (DC + {a.time_points - 1} BE "
-              "steps) per step; compiled C restatement oracle/cvx.c")
+    sample = (f"{cores} threads x {per_thread} whole instances ({len(ts)} solves each) per "
+              "step; compiled C restatement oracle/cvx.c")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"mirror_adder_mc{a.instances}", "sample": sample},
+            "config": {"workload": w.label(a.instances, len(ts)), "sample": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -175,7 +240,8 @@ def main():
     # CPU baseline first (before any CUDA work), rank 0 only
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    cpu = cpu_baseline() if rank == 0 and not a.no_cpu else None
+    w = WORKLOADS[a.workload]
+    cpu = cpu_baseline(w, a.time_points, a.instances) if rank == 0 and not a.no_cpu else None
 
     import torch
     import voltax_gb300 as vx
@@ -190,10 +256,12 @@ def main():
     dev = torch.device("cuda", local)
     lib = _lib.load()
 
-    B = a.instances
-    circuit = workloads.mirror_adder_mc(B, seed=rank)
-    ts = np.linspace(0.0, T_STOP, a.time_points)
-    out_nodes = [circuit.node(n) for n in ("s0", "s1", "s2", "s3", "co")]
+    circuit = w.circuit(a.instances, seed=rank)
+    B = circuit.batch
+    ts = w.times(a.time_points)
+    ic = w.ic(circuit)
+    out_nodes = ([circuit.node(n) for n in w.outputs] if w.outputs
+                 else list(range(circuit.n_nodes)))
 
     def to_device(c, device, pin=False):
         out = c
@@ -225,8 +293,9 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def step(c, opts):
-        sol = vx.transient(c, ts, ic="dc", method="be", options=opts)
-        return sol
+        if w.analysis == "dc":
+            return vx.dc(c, options=opts)
+        return vx.transient(c, ts, ic=ic, method=w.method, options=opts)
 
     def barrier():
         if dist is not None:
@@ -252,7 +321,7 @@ def main():
     with Clocks(local) as clk:
         ms32 = timed(lambda: step(dev_circuit, opts32), a.steps)
     launches = (lib.vxg_launch_count() - n0) // a.steps
-    solves_per_step = B * a.time_points
+    solves_per_step = B * len(ts)
     t32 = float(np.sum(ms32)) / 1e3
     if dist is not None:
         tt = torch.tensor([t32], device=dev)
@@ -269,8 +338,10 @@ def main():
     nv = circuit.n_nodes
     match = float((s32.z[..., :nv] - s64.z[..., :nv]).abs().max())
     conv = bool(s32.converged.all())
-    iters = float(s32.iterations[:, 1:].float().mean())
-    total_iters = int(s32.iterations.sum())  # Newton iterations of one step, all instances
+    it = s32.iterations.reshape(-1, len(ts)).float() if w.analysis == "transient" else \
+        s32.iterations.reshape(-1, 1).float()
+    iters = float(it[:, 1:].mean()) if w.analysis == "transient" else float(it.mean())
+    total_iters = int(it.sum())  # Newton iterations of one step, all instances
 
     # roofline of the dominant kernel. Algorithmic bytes per Newton iteration
     # and instance: 8 nnz (stamp write) + 4 (nnz + 2 factor_entries) (panel
@@ -283,7 +354,7 @@ def main():
     step_s = t32 / a.steps
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_per_iter * total_iters / step_s / 1e9
-    roofline = {"bound": "hbm", "kernel": "fused_kernel<float,128>" if engine_used == "fused"
+    roofline = {"bound": "hbm", "kernel": "fused_kernel<float>" if engine_used == "fused"
                 else "factor/solve level kernels", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                 "peak_source": "measured" if peaks else "fallback",
@@ -297,7 +368,7 @@ def main():
     h2d = sum(t.numel() * 8 for el in host_circuit.elements.values()
               for t in ([getattr(el, f) for f in el.fields] +
                         (el.value.params() if hasattr(el, "value") else [])))
-    out_host = torch.empty((B, a.time_points, len(out_nodes)), dtype=torch.float64,
+    out_host = torch.empty(tuple(s32.z[..., out_nodes].shape), dtype=torch.float64,
                            pin_memory=True)
 
     def e2e_step():
@@ -315,8 +386,8 @@ def main():
         "warmup": a.warmup, "ms_per_step": 1e3 * t32 / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 LU + f64 residual/refinement",
         "data": "synthetic",
-        "config": {"workload": f"mirror_adder_mc{B}", "instances": B,
-                   "time_points": a.time_points, "method": "be", "t_stop_s": T_STOP,
+        "config": {"workload": w.label(B, len(ts)), "instances": B,
+                   "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},

@@ -272,3 +272,48 @@ def test_fused_is_bitwise_reproducible():
     a = vx.transient(c, ts, ic="dc", options=o)
     b = vx.transient(c, ts, ic="dc", options=o)
     assert torch.equal(a.z, b.z)
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_rc_ladder_transient_gradient_matches_recorded_values(engine):
+    """voltax tests/test_analysis.py:41-49: d sum(v_out) / d log r through the
+    transient (implicit adjoint over every step)."""
+    c = rc_ladder()
+    el = c.elements["Resistor"]
+    e2 = el.with_nodes(el.nodes)
+    e2.log_r = el.log_r.clone().requires_grad_(True)
+    c2 = c.replace("Resistor", e2)
+    ts = np.linspace(0, 1e-5, 101)
+    sol = vx.transient(c2, ts, ic="zero", options=vx.Options(engine=engine))
+    sol.v("out").sum().backward()
+    names = c.devices("Resistor")  # R1, R2, Rload in group order
+    assert names == ["R1", "R2", "Rload"]
+    np.testing.assert_allclose(e2.log_r.grad.numpy(),
+                               -np.array([13.35247162, 13.96802873, -11.62111701]), rtol=1e-6)
+
+
+@pytest.mark.parametrize("method", ["be", "trap"])
+@pytest.mark.parametrize("engine", ENGINES)
+def test_ekv_transient_gradient_matches_finite_differences(method, engine):
+    c = workloads.mirror_adder(1)
+    ts = np.linspace(0, 120e-12, 13)
+    name = "EKVMOSFET_n"
+    el = c.elements[name]
+    o = vx.Options(engine=engine)
+
+    def loss(dvth):
+        e2 = el.with_nodes(el.nodes)
+        e2.dvth = dvth
+        sol = vx.transient(c.replace(name, e2), ts, ic="dc", method=method, options=o)
+        return (sol.v("s0") ** 2).sum() + sol.v("co").sum()
+
+    dv = el.dvth.clone().requires_grad_(True)
+    loss(dv).backward()
+    g = dv.grad.numpy()
+    k = int(np.argmax(np.abs(g)))
+    eps = 1e-5
+    up, dn = el.dvth.clone(), el.dvth.clone()
+    up[k] += eps
+    dn[k] -= eps
+    fd = (float(loss(up)) - float(loss(dn))) / (2 * eps)
+    assert np.isclose(g[k], fd, rtol=1e-5, atol=1e-9)

@@ -50,7 +50,7 @@ class Options:
     solver: str = "auto"
     sparse_threshold: int = SPARSE_THRESHOLD
     precision: str = "f64"
-    refine: int = 2
+    refine: int = 1
     engine: str = "auto"
 
     def __post_init__(self):
@@ -301,6 +301,102 @@ def dc(circuit, t: float = 0.0, guess=None, options: Options = Options()) -> Sol
     return Solution(torch.as_tensor(t, dtype=torch.float64), z, conv, circuit.layout, iters)
 
 
+def _attach_adjoint(call, ts_np, mode, dc_first, options, z_out):
+    rows = _flat_rows(call)
+    if not any(r.requires_grad for r in rows):
+        return z_out
+    return _TransientAdjoint.apply(call, ts_np, mode, dc_first, options.gmin, z_out, *rows)
+
+
+def _param_vjp(call: _Call, z, t, cf, cq, lam):
+    """Per group ``(P, B, n)`` of ``-lam^T d(cf f(z, t) + cq q(z))/d rows``."""
+    eng = call.eng
+    bufs = [torch.zeros((len(rows), call.B, call.c.elements[name].size), dtype=torch.float64,
+                        device=eng.device)
+            for name, rows in zip(eng.tables.group_names, call.rows)]
+    ptrs = (C.c_void_p * max(len(bufs), 1))(*[b.data_ptr() for b in bufs])
+    L.check(eng.lib.vxg_param_vjp(eng.handle, call.B, call.params, z.contiguous().data_ptr(),
+                                  float(t), float(cf), float(cq), lam.contiguous().data_ptr(),
+                                  ptrs, stream_ptr()), "vxg_param_vjp")
+    return bufs
+
+
+class _TransientAdjoint(torch.autograd.Function):
+    """Reverse sweep of the implicit-function adjoint over the time steps
+    (voltax differentiates its ``lax.scan`` of ``_root`` solves,
+    voltax/analysis.py:269-288, 470-477). With R_n the step residual:
+    ``J_n^T lam_n = g_n - (dR_{n+1}/dz_n)^T lam_{n+1}`` from the last step
+    back (to the DC point when ``ic="dc"``), and
+    ``dL/dp = -sum_n lam_n^T dR_n/dp``."""
+
+    @staticmethod
+    def forward(ctx, call, ts, mode, dc_first, gmin, z_out, *rows):
+        ctx.call, ctx.ts, ctx.mode, ctx.dc_first, ctx.gmin = call, ts, mode, dc_first, gmin
+        ctx.save_for_backward(z_out)
+        return z_out.clone()
+
+    @staticmethod
+    def backward(ctx, gz):
+        (z,) = ctx.saved_tensors
+        call, ts, trap = ctx.call, ctx.ts, ctx.mode == L.VXG_MODE_TRAP
+        eng, B = call.eng, call.B
+        f64 = L.VXG_F64
+        ws = eng.workspace(B, f64)
+        fac = eng.factor_buffer(B, f64)
+        data = torch.empty((B, eng.nnz), dtype=torch.float64, device=eng.device)
+        tmp = torch.empty((B, eng.S), dtype=torch.float64, device=eng.device)
+        gz = gz.contiguous()
+        acc = None
+        lam_next = None
+
+        def stamp(zn, t, cf, cq, gm):
+            L.check(eng.lib.vxg_eval(eng.handle, B, call.params, zn.data_ptr(), float(t),
+                                     float(cf), float(cq), None, float(gm), None, None,
+                                     data.data_ptr(), ws.data_ptr(), stream_ptr()), "vxg_eval")
+
+        for n in range(len(ts) - 1, -1, -1):
+            if n == 0 and not ctx.dc_first:
+                break
+            zn = z[n].contiguous()
+            rhs = gz[n].clone()
+            if lam_next is not None:  # - (dR_{n+1}/dz_n)^T lam_{n+1}
+                h1 = ts[n + 1] - ts[n]
+                stamp(zn, ts[n], 0.5 if trap else 0.0, -1.0 / h1, 0.0)
+                L.check(eng.lib.vxg_spmv(eng.handle, B, data.data_ptr(), lam_next.data_ptr(),
+                                         tmp.data_ptr(), 1, stream_ptr()), "vxg_spmv")
+                rhs -= tmp
+            if n == 0:
+                cf, cq = 1.0, 0.0
+            else:
+                h = ts[n] - ts[n - 1]
+                cf, cq = (0.5 if trap else 1.0), 1.0 / h
+            stamp(zn, ts[n], cf, cq, ctx.gmin)
+            L.check(eng.lib.vxg_factor(eng.handle, B, f64, data.data_ptr(), fac.data_ptr(),
+                                       ws.data_ptr(), stream_ptr()), "vxg_factor")
+            lam = torch.empty_like(rhs)
+            L.check(eng.lib.vxg_solve(eng.handle, B, f64, fac.data_ptr(), None, rhs.data_ptr(),
+                                      lam.data_ptr(), 1, 0, ws.data_ptr(), stream_ptr()),
+                    "vxg_solve")
+            parts = [_param_vjp(call, zn, ts[n], cf, cq, lam)]
+            if n > 0:
+                parts.append(_param_vjp(call, z[n - 1], ts[n - 1], 0.5 if trap else 0.0,
+                                        -cq, lam))
+            for bufs in parts:
+                acc = bufs if acc is None else [a + b for a, b in zip(acc, bufs)]
+            lam_next = lam
+        grads = []
+        for rows, buf in zip(call.rows, acc if acc is not None else
+                             [None] * len(call.rows)):
+            for r, row in enumerate(rows):
+                if buf is None:
+                    grads.append(None)
+                    continue
+                g = buf[r]
+                g = g.sum(0) if row.ndim == 1 else g
+                grads.append(g.to(row.device))
+        return (None, None, None, None, None, None, *grads)
+
+
 def transient(circuit, ts, ic="dc", method: str = "be",
               options: Options = Options()) -> Solution:
     """Transient analysis on the time grid `ts` (voltax/analysis.py:434-480)."""
@@ -323,6 +419,7 @@ def transient(circuit, ts, ic="dc", method: str = "be",
         z0 = z0.reshape(-1, S).expand(B, S).contiguous()
         z_out, conv, iters = call.fused_run(mode, ts_np, z0, dc_first)
         conv[0] = 1  # the initial state counts as converged (voltax/analysis.py:479)
+        z_out = _attach_adjoint(call, ts_np, mode, dc_first, options, z_out)
         tt = torch.as_tensor(ts_np)
         if circuit.batch == 1:
             return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])
@@ -350,6 +447,7 @@ def transient(circuit, ts, ic="dc", method: str = "be",
         call.eng.handle, B, call.params, mode, T, ts_np.ctypes.data_as(L.PF64), z0.data_ptr(),
         options.gmin, C.byref(o), z_out.data_ptr(), conv.data_ptr(), iters.data_ptr(),
         call.ws.data_ptr(), stream_ptr()), "vxg_transient")
+    z_out = _attach_adjoint(call, ts_np, mode, isinstance(ic, str) and ic == "dc", options, z_out)
     tt = torch.as_tensor(ts_np)
     if circuit.batch == 1:
         return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])

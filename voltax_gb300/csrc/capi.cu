@@ -136,7 +136,7 @@ static void free_topo(Topo& t) {
                   t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
                   t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
                   t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
-                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr};
+                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < t.n_groups; ++i)
@@ -252,6 +252,9 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
         t.rmax = std::max(t.rmax, t.h_lv_rmax[L]);
       }
     }
+    st = upload(&t.d_lv_kmax, t.h_lv_kmax, (size_t)nl);
+  }
+  if (st == VXG_OK) {
     cudaError_t e = cudaMallocHost((void**)&t.h_flag, sizeof(int) * 4);
     if (e != cudaSuccess) {
       set_error(e);

@@ -268,3 +268,239 @@ __device__ inline void eval_device(const GroupDev& g, int b, int d, const double
 }
 
 }  // namespace vxg
+
+namespace vxg {
+
+// --------------------------------------------------------------------------
+// Structure-of-arrays evaluation. Slot (i, d) of a group's residual block is
+// res[i * n + d]; slot (i, j, d) of its Jacobian block is jac[(i * m + j) * n
+// + d]. Consecutive devices therefore write consecutive addresses. Values
+// (currents, charges) are FP64; Jacobian entries are computed and stored in
+// JT (double for the plain form, float for the FP32-factor form, whose
+// Jacobian only feeds the FP32 factorization and the refinement matrix).
+// --------------------------------------------------------------------------
+template <typename JT>
+__device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const double* u,
+                                        double cf, double cq, bool wf, bool wq, bool wj,
+                                        double* fo, double* qo, JT* jo) {
+  const int n = g.n;
+  const EkvIn p = ekv_params(g, b, d);
+  const double vd = p.sign * u[0], vg = p.sign * u[1], vs = p.sign * u[2], vb = p.sign * u[3];
+  const double two_vt = 2.0 * p.vt;
+  const double vp = (vg - vb - p.vth - p.dvth) / p.n;
+  const double af = (vp - (vs - vb)) / two_vt;
+  const double ar = (vp - (vd - vb)) / two_vt;
+  double spf, sgf, spr, sgr;
+  softplus_and_sigmoid(af, &spf, &sgf);
+  softplus_and_sigmoid(ar, &spr, &sgr);
+  const double i_f = spf * spf, i_r = spr * spr;
+  const bool need_i = wf || (wj && cf != 0.0);
+  const bool need_q = wq || (wj && cq != 0.0);
+  const double vds = vd - vs;
+  const double root = sqrt(vds * vds + 1e-3 * 1e-3);
+  const double mfac = 1.0 + p.lam * (root - 1e-3);
+  if (wf) {
+    const double ids = p.i_spec * (i_f - i_r) * mfac;
+    fo[0 * n + d] = p.sign * ids;
+    fo[1 * n + d] = p.sign * 0.0;
+    fo[2 * n + d] = p.sign * -ids;
+    fo[3 * n + d] = p.sign * 0.0;
+  }
+  double xf = 0.0, xr = 0.0, s = 1.0, nd = 0.0, ns = 0.0, scale = 0.0, kb = 0.0;
+  if (need_q) {
+    xf = sqrt(0.25 + i_f);
+    xr = sqrt(0.25 + i_r);
+    scale = p.c_ox * p.n * p.vt;
+    s = xf + xr;
+    nd = 3 * xr * xr * xr + 6 * xr * xr * xf + 4 * xr * xf * xf + 2 * xf * xf * xf;
+    ns = 3 * xf * xf * xf + 6 * xf * xf * xr + 4 * xf * xr * xr + 2 * xr * xr * xr;
+    kb = -(p.n - 1.0) / p.n;
+  }
+  if (wq) {
+    const double s2 = s * s;
+    const double c415 = 4.0 / 15.0;
+    const double q_d = -scale * (c415 * nd / s2 - 0.5);
+    const double q_s = -scale * (c415 * ns / s2 - 0.5);
+    const double q_i = q_d + q_s;
+    const double q_b = kb * (p.c_ox * (vg - vb) + q_i);
+    const double q_g = -(q_i + q_b);
+    const double q_gs = p.cov_w * (vg - vs), q_gd = p.cov_w * (vg - vd);
+    qo[0 * n + d] = p.sign * (q_d + -q_gd);
+    qo[1 * n + d] = p.sign * (q_g + (q_gs + q_gd));
+    qo[2 * n + d] = p.sign * (q_s + -q_gs);
+    qo[3 * n + d] = p.sign * (q_b + 0.0);
+  }
+  if (!wj) return;
+  // derivatives in JT
+  const JT tv = (JT)two_vt;
+  const JT g1 = JT(1) / (JT)p.n;
+  const JT af_g = g1 / tv, af_s = JT(-1) / tv, af_b = (JT(1) - g1) / tv;
+  const JT dif = JT(2) * (JT)spf * (JT)sgf, dir = JT(2) * (JT)spr * (JT)sgr;
+  const JT cfj = (JT)cf, cqj = (JT)cq;
+  JT ji[4] = {JT(0), JT(0), JT(0), JT(0)};
+  if (need_i && cf != 0.0) {
+    const JT isp = (JT)p.i_spec, mf = (JT)mfac, dI = (JT)(i_f - i_r);
+    const JT dsa = (JT)(vds / root), lam = (JT)p.lam;
+    // d ids / d (vd, vg, vs, vb)
+    ji[0] = isp * ((-dir * af_s) * mf + dI * lam * dsa);
+    ji[1] = isp * ((dif - dir) * af_g * mf);
+    ji[2] = isp * ((dif * af_s) * mf - dI * lam * dsa);
+    ji[3] = isp * ((dif - dir) * af_b * mf);
+  }
+  JT dq0[4] = {JT(0), JT(0), JT(0), JT(0)}, dq1[4] = {JT(0), JT(0), JT(0), JT(0)};
+  JT dq2[4] = {JT(0), JT(0), JT(0), JT(0)}, dq3[4] = {JT(0), JT(0), JT(0), JT(0)};
+  if (need_q && cq != 0.0) {
+    const JT fx = (JT)xf, rx = (JT)xr, ss = (JT)s, s3 = ss * ss * ss;
+    const JT ndj = (JT)nd, nsj = (JT)ns, sc = (JT)scale, kbj = (JT)kb, cox = (JT)p.c_ox;
+    const JT cw = (JT)p.cov_w;
+    const JT gd_f = ((JT(6) * rx * rx + JT(8) * rx * fx + JT(6) * fx * fx) * ss - JT(2) * ndj) / s3;
+    const JT gd_r = ((JT(9) * rx * rx + JT(12) * rx * fx + JT(4) * fx * fx) * ss - JT(2) * ndj) / s3;
+    const JT gs_f = ((JT(9) * fx * fx + JT(12) * fx * rx + JT(4) * rx * rx) * ss - JT(2) * nsj) / s3;
+    const JT gs_r = ((JT(6) * fx * fx + JT(8) * fx * rx + JT(6) * rx * rx) * ss - JT(2) * nsj) / s3;
+    const JT dxf_da = dif / (JT(2) * fx), dxr_da = dir / (JT(2) * rx);
+    const JT c415 = JT(4) / JT(15);
+    // daf, dar per terminal (vd, vg, vs, vb)
+    const JT dafk[4] = {JT(0), af_g, af_s, af_b};
+    const JT dark[4] = {af_s, af_g, JT(0), af_b};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const JT dxf = dxf_da * dafk[k], dxr = dxr_da * dark[k];
+      const JT dqd = -sc * c415 * (gd_f * dxf + gd_r * dxr);
+      const JT dqs = -sc * c415 * (gs_f * dxf + gs_r * dxr);
+      const JT dqi = dqd + dqs;
+      const JT dvgb = (k == 1 ? JT(1) : JT(0)) - (k == 3 ? JT(1) : JT(0));
+      const JT dqb = kbj * (cox * dvgb + dqi);
+      const JT dqg = -(dqi + dqb);
+      const JT dgs = cw * ((k == 1 ? JT(1) : JT(0)) - (k == 2 ? JT(1) : JT(0)));
+      const JT dgd = cw * ((k == 1 ? JT(1) : JT(0)) - (k == 0 ? JT(1) : JT(0)));
+      dq0[k] = dqd - dgd;
+      dq1[k] = dqg + (dgs + dgd);
+      dq2[k] = dqs - dgs;
+      dq3[k] = dqb;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    JT r0 = cf != 0.0 ? cfj * ji[j] : JT(0);
+    JT r2 = cf != 0.0 ? cfj * -ji[j] : JT(0);
+    JT r1 = JT(0), r3 = JT(0);
+    if (cq != 0.0) {
+      r0 = r0 + cqj * dq0[j];
+      r1 = r1 + cqj * dq1[j];
+      r2 = r2 + cqj * dq2[j];
+      r3 = r3 + cqj * dq3[j];
+    }
+    jo[(0 * 4 + j) * n + d] = r0;
+    jo[(1 * 4 + j) * n + d] = r1;
+    jo[(2 * 4 + j) * n + d] = r2;
+    jo[(3 * 4 + j) * n + d] = r3;
+  }
+}
+
+// Evaluate device d of group g (instance b) reading state zz; write its slots.
+// fo/qo/jo point at the group's first slot in each contribution array.
+template <typename JT>
+__device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const double* zz,
+                                         double t, double cf, double cq, bool wf, bool wq,
+                                         bool wj, double* fo, double* qo, JT* jo) {
+  const int n = g.n;
+  double u[kMaxM];
+#pragma unroll
+  for (int i = 0; i < kMaxM; ++i) {
+    if (i < g.T) {
+      const int node = g.nodes[d * g.T + i];
+      u[i] = node >= 0 ? zz[node] : 0.0;
+    } else if (i < g.m) {
+      u[i] = zz[g.int_offset + d * g.K + (i - g.T)];
+    } else {
+      u[i] = 0.0;
+    }
+  }
+  switch (g.kind) {
+    case VXG_KIND_CONDUCTANCE: {
+      const double gg = prm(g, 0, b, d);
+      const double i = (u[0] - u[1]) * gg;
+      if (wf) {
+        fo[d] = i;
+        fo[n + d] = -i;
+      }
+      if (wq) {
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+      }
+      if (wj) {
+        const JT a = cf != 0.0 ? (JT)(cf * gg) : JT(0);
+        jo[d] = a;
+        jo[n + d] = -a;
+        jo[2 * n + d] = -a;
+        jo[3 * n + d] = a;
+      }
+      break;
+    }
+    case VXG_KIND_CAPACITOR: {
+      const double c = prm(g, 0, b, d);
+      const double q = c * (u[0] - u[1]);
+      if (wf) {
+        fo[d] = 0.0;
+        fo[n + d] = 0.0;
+      }
+      if (wq) {
+        qo[d] = q;
+        qo[n + d] = -q;
+      }
+      if (wj) {
+        const JT a = cq != 0.0 ? (JT)(cq * c) : JT(0);
+        jo[d] = a;
+        jo[n + d] = -a;
+        jo[2 * n + d] = -a;
+        jo[3 * n + d] = a;
+      }
+      break;
+    }
+    case VXG_KIND_VSOURCE: {
+      if (wf) {
+        fo[d] = u[2];
+        fo[n + d] = -u[2];
+        fo[2 * n + d] = (u[0] - u[1]) - wave_value(g, b, d, t);
+      }
+      if (wq) {
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+        qo[2 * n + d] = 0.0;
+      }
+      if (wj) {  // rows (p, n, eq), cols (vp, vn, i)
+        const JT a = (JT)cf;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) jo[e * n + d] = JT(0);
+        if (cf != 0.0) {
+          jo[2 * n + d] = a;
+          jo[5 * n + d] = -a;
+          jo[6 * n + d] = a;
+          jo[7 * n + d] = -a;
+        }
+      }
+      break;
+    }
+    case VXG_KIND_ISOURCE: {
+      if (wf) {
+        const double i = wave_value(g, b, d, t);
+        fo[d] = i;
+        fo[n + d] = -i;
+      }
+      if (wq) {
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+      }
+      if (wj) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) jo[e * n + d] = JT(0);
+      }
+      break;
+    }
+    case VXG_KIND_EKV:
+      ekv_soa<JT>(g, b, d, u, cf, cq, wf, wq, wj, fo, qo, jo);
+      break;
+  }
+}
+
+}  // namespace vxg

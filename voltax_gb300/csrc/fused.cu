@@ -33,6 +33,7 @@ struct FusedArgs {
   const int *sn_k, *sn_r, *sn_piv, *sn_bord;
   const long long *sn_panel, *sn_piv_ptr, *sn_bord_ptr;
   const long long* lv_ptr;
+  const int* lv_kmax;  // largest supernode of each level
   const int* lv_sn;
   const long long *lv_schur_off, *lv_bord_off;
   const long long *lv_st_ptr, *st_tgt, *st_ptr, *st_src;
@@ -53,12 +54,13 @@ __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15;
 
 // Shared-memory layout of one instance.
 struct FusedLayout {
-  size_t z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, total;
+  size_t z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, sbuf, total;
 };
 
 template <typename T>
 __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, int n_jac,
                                                     int work, int max_scr) {
+  // T is the panel type; the Jacobian contributions use the same type
   FusedLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -79,11 +81,12 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.data = take(d * nnz);
   L.cf = take(d * n_res);
   L.cq = take(d * n_res);
-  L.cj = take(d * n_jac);
+  L.cj = take(sizeof(T) * n_jac);
   L.work = take(sizeof(T) * work);
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
   L.xt = take(sizeof(T) * S);
   L.red = take(64 * sizeof(double));
+  L.sbuf = take(sizeof(T) * 2 * 32 * 8 + sizeof(int) * 32 * 8);  // per-warp col/row/perm
   L.total = o;
   return L;
 }
@@ -131,105 +134,199 @@ __device__ int block_all(int ok, double* red) {
   return all;
 }
 
-// ------------------------------------------------- warp-level supernode LDU
-// Inverts F11 in place (Gauss-Jordan, partial pivoting), Ub = W F12 in place,
-// S = F21 Ub into Sout, Lb = F21 W in place. k <= 32.
-template <typename T>
-__device__ void warp_factor(T* P, int k, int r, T* Sout, int lane) {
+// ------------------------------------------------------- supernode LDU
+// One supernode's block LDU by a group of threads: one warp (CTA = false,
+// the supernodes of a wide level in parallel) or the whole CTA (CTA = true,
+// the single supernodes of the top levels). k <= 32.
+//   W  = F11^-1 by Gauss-Jordan with partial pivoting (row swaps recorded,
+//        undone as column swaps), two group barriers per pivot step;
+//   Ub = W F12 in place (one column per warp, shuffles across the column);
+//   S  = F21 Ub into Sout;  Lb = F21 W in place (one row per warp).
+template <bool CTA, int NT>
+__device__ __forceinline__ void group_sync() {
+  if (CTA)
+    __syncthreads();
+  else
+    __syncwarp();
+}
+
+template <typename T, bool CTA, int NT>
+__device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* perm) {
+  constexpr int GW = CTA ? NT / 32 : 1;  // warps in the group
+  const int lane = threadIdx.x & 31;
+  const int gw = CTA ? (threadIdx.x >> 5) : 0;  // warp index inside the group
   T* A = P;
   T* F12 = P + k * k;
   T* F21 = F12 + k * r;
-  int myperm = lane;
   for (int c = 0; c < k; ++c) {
-    T v = (lane >= c && lane < k) ? tabs_(A[lane * k + c]) : T(-1);
-    int bi = lane;
-    for (int off = 16; off > 0; off >>= 1) {
-      const T ov = __shfl_down_sync(kFull, v, off);
-      const int oi = __shfl_down_sync(kFull, bi, off);
-      if (ov > v || (ov == v && oi < bi)) {
-        v = ov;
-        bi = oi;
+    if (gw == 0) {
+      T v = (lane >= c && lane < k) ? tabs_(A[lane * k + c]) : T(-1);
+      int bi = lane;
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ov = __shfl_down_sync(kFull, v, off);
+        const int oi = __shfl_down_sync(kFull, bi, off);
+        if (ov > v || (ov == v && oi < bi)) {
+          v = ov;
+          bi = oi;
+        }
+      }
+      int p = __shfl_sync(kFull, bi, 0);
+      if (p < c || p >= k) p = c;
+      if (lane == 0) perm[c] = p;
+      if (p != c && lane < k) {
+        const T tmp = A[p * k + lane];
+        A[p * k + lane] = A[c * k + lane];
+        A[c * k + lane] = tmp;
+      }
+      __syncwarp();
+      if (lane < k) {
+        rowb[lane] = A[c * k + lane];
+        colb[lane] = (lane == c) ? T(0) : A[lane * k + c];
       }
     }
-    int p = __shfl_sync(kFull, bi, 0);
-    if (p < c || p >= k) p = c;
-    if (lane == c) myperm = p;
-    if (p != c && lane < k) {
-      const T tmp = A[p * k + lane];
-      A[p * k + lane] = A[c * k + lane];
-      A[c * k + lane] = tmp;
-    }
-    __syncwarp();
-    const T d = A[c * k + c];
-    const T colv = (lane < k && lane != c) ? A[lane * k + c] : T(0);
-    __syncwarp();
-    if (lane < k) A[c * k + lane] = ((lane == c) ? T(1) : A[c * k + lane]) / d;
-    __syncwarp();
-    const T rowc = (lane < k) ? A[c * k + lane] : T(0);
-    for (int i = 0; i < k; ++i) {
-      const T f = __shfl_sync(kFull, colv, i);
-      if (i != c && lane < k) {
-        const T a = (lane == c) ? T(0) : A[i * k + lane];
-        A[i * k + lane] = a - f * rowc;
+    group_sync<CTA, NT>();
+    const T d = rowb[c];
+    const T rc = lane < k ? ((lane == c) ? T(1) : rowb[lane]) / d : T(0);
+    if (lane < k)
+      for (int i = gw; i < k; i += GW) {
+        if (i == c) {
+          A[c * k + lane] = rc;
+        } else {
+          const T a = (lane == c) ? T(0) : A[i * k + lane];
+          A[i * k + lane] = a - colb[i] * rc;
+        }
+      }
+    group_sync<CTA, NT>();
+  }
+  // undo the row swaps as column swaps; one thread per row
+  for (int i = CTA ? threadIdx.x : lane; i < k; i += CTA ? NT : 32)
+    for (int c = k - 1; c >= 0; --c) {
+      const int p = perm[c];
+      if (p != c) {
+        const T tmp = A[i * k + c];
+        A[i * k + c] = A[i * k + p];
+        A[i * k + p] = tmp;
       }
     }
-    __syncwarp();
-  }
-  for (int c = k - 1; c >= 0; --c) {
-    const int p = __shfl_sync(kFull, myperm, c);
-    if (p != c && lane < k) {
-      const T tmp = A[lane * k + c];
-      A[lane * k + c] = A[lane * k + p];
-      A[lane * k + p] = tmp;
-    }
-  }
-  __syncwarp();
+  group_sync<CTA, NT>();
   if (r == 0) return;
-  // Ub = W F12, one column per lane
-  for (int c0 = 0; c0 < r; c0 += 32) {
-    const int col = c0 + lane;
-    T x[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) x[l] = (l < k && col < r) ? F12[l * r + col] : T(0);
-    __syncwarp();
-    if (col < r)
-      for (int i = 0; i < k; ++i) {
-        T acc = T(0);
-#pragma unroll
-        for (int l = 0; l < 32; ++l)
-          if (l < k) acc += A[i * k + l] * x[l];
-        F12[i * r + col] = acc;
-      }
-    __syncwarp();
-  }
-  // S = F21 Ub, one column per lane
-  for (int c0 = 0; c0 < r; c0 += 32) {
-    const int col = c0 + lane;
-    T u[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) u[l] = (l < k && col < r) ? F12[l * r + col] : T(0);
-    if (col < r)
-      for (int a = 0; a < r; ++a) {
-        T acc = T(0);
-#pragma unroll
-        for (int l = 0; l < 32; ++l)
-          if (l < k) acc += F21[a * k + l] * u[l];
-        Sout[a * r + col] = acc;
-      }
-  }
-  __syncwarp();
-  // Lb = F21 W, lane j owns column j of W
-  T w[32];
-#pragma unroll
-  for (int l = 0; l < 32; ++l) w[l] = (l < k && lane < k) ? A[l * k + lane] : T(0);
-  for (int a = 0; a < r; ++a) {
+  // Ub = W F12: warp-strided columns, lane l holds F12[l][col]
+  for (int col = gw; col < r; col += GW) {
+    const T v = lane < k ? F12[lane * r + col] : T(0);
     T acc = T(0);
-#pragma unroll
-    for (int l = 0; l < 32; ++l)
-      if (l < k) acc += F21[a * k + l] * w[l];
+    for (int l = 0; l < k; ++l) {
+      const T x = __shfl_sync(kFull, v, l);
+      if (lane < k) acc += A[lane * k + l] * x;
+    }
+    if (lane < k) F12[lane * r + col] = acc;
+  }
+  group_sync<CTA, NT>();
+  // S = F21 Ub
+  for (int a = gw; a < r; a += GW)
+    for (int b = lane; b < r; b += 32) {
+      T acc = T(0);
+      for (int l = 0; l < k; ++l) acc += F21[a * k + l] * F12[l * r + b];
+      Sout[a * r + b] = acc;
+    }
+  group_sync<CTA, NT>();
+  // Lb = F21 W, one row per warp
+  for (int a = gw; a < r; a += GW) {
+    T acc = T(0);
+    if (lane < k)
+      for (int l = 0; l < k; ++l) acc += F21[a * k + l] * A[l * k + lane];
     __syncwarp();
     if (lane < k) F21[a * k + lane] = acc;
     __syncwarp();
+  }
+  group_sync<CTA, NT>();
+}
+
+// ---------------------------------------------- tiny supernodes (k <= 4)
+// One thread per supernode: closed loops over k <= 4 with the same
+// Gauss-Jordan / Ub / S / Lb steps as sn_factor.
+constexpr int kTiny = 4;
+
+template <typename T>
+__device__ void tiny_factor(T* P, int k, int r, T* Sout) {
+  T* A = P;
+  T* F12 = P + k * k;
+  T* F21 = F12 + k * r;
+  int perm[kTiny];
+#pragma unroll
+  for (int c = 0; c < kTiny; ++c) {
+    if (c >= k) break;
+    int p = c;
+    T best = tabs_(A[c * k + c]);
+    for (int i = c + 1; i < k; ++i) {
+      const T v = tabs_(A[i * k + c]);
+      if (v > best) {
+        best = v;
+        p = i;
+      }
+    }
+    perm[c] = p;
+    if (p != c)
+      for (int j = 0; j < k; ++j) {
+        const T t = A[p * k + j];
+        A[p * k + j] = A[c * k + j];
+        A[c * k + j] = t;
+      }
+    const T d = A[c * k + c];
+    A[c * k + c] = T(1);
+    for (int j = 0; j < k; ++j) A[c * k + j] = A[c * k + j] / d;
+    for (int i = 0; i < k; ++i) {
+      if (i == c) continue;
+      const T f = A[i * k + c];
+      A[i * k + c] = T(0);
+      for (int j = 0; j < k; ++j) A[i * k + j] -= f * A[c * k + j];
+    }
+  }
+#pragma unroll
+  for (int c = kTiny - 1; c >= 0; --c) {
+    if (c >= k) continue;
+    const int p = perm[c];
+    if (p != c)
+      for (int i = 0; i < k; ++i) {
+        const T t = A[i * k + c];
+        A[i * k + c] = A[i * k + p];
+        A[i * k + p] = t;
+      }
+  }
+  if (r == 0) return;
+  for (int col = 0; col < r; ++col) {  // Ub = W F12
+    T x[kTiny];
+#pragma unroll
+    for (int l = 0; l < kTiny; ++l) x[l] = l < k ? F12[l * r + col] : T(0);
+#pragma unroll
+    for (int i = 0; i < kTiny; ++i) {
+      if (i >= k) break;
+      T acc = T(0);
+#pragma unroll
+      for (int l = 0; l < kTiny; ++l)
+        if (l < k) acc += A[i * k + l] * x[l];
+      F12[i * r + col] = acc;
+    }
+  }
+  for (int a = 0; a < r; ++a) {  // S = F21 Ub, then Lb = F21 W (row a)
+    T f[kTiny];
+#pragma unroll
+    for (int l = 0; l < kTiny; ++l) f[l] = l < k ? F21[a * k + l] : T(0);
+    for (int b = 0; b < r; ++b) {
+      T acc = T(0);
+#pragma unroll
+      for (int l = 0; l < kTiny; ++l)
+        if (l < k) acc += f[l] * F12[l * r + b];
+      Sout[a * r + b] = acc;
+    }
+#pragma unroll
+    for (int j = 0; j < kTiny; ++j) {
+      if (j >= k) break;
+      T acc = T(0);
+#pragma unroll
+      for (int l = 0; l < kTiny; ++l)
+        if (l < k) acc += f[l] * A[l * k + j];
+      F21[a * k + j] = acc;
+    }
   }
 }
 
@@ -238,9 +335,11 @@ template <typename T, int NT>
 struct Instance {
   const FusedArgs& A;
   int b;
-  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *data, *cf, *cq, *cj, *red;
-  T *work, *scr, *xt;
+  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *data, *cf, *cq, *red;
+  T *cj, *work, *scr, *xt, *sbuf;
+  int* ibuf;
 
+  // devices -> contribution slots (structure of arrays per group)
   __device__ void eval(const double* zz, double t, double cfc, double cqc, bool wf, bool wq,
                        bool wj) {
     const GroupTable& gt = A.gt;
@@ -248,54 +347,42 @@ struct Instance {
       int gi = 0;
       while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
       const GroupDev& g = gt.g[gi];
-      const int d = flat - (int)g.dev_base;
-      double u[kMaxM];
-      for (int i = 0; i < g.T; ++i) {
-        const int node = g.nodes[d * g.T + i];
-        u[i] = node >= 0 ? zz[node] : 0.0;
-      }
-      for (int i = 0; i < g.K; ++i) u[g.T + i] = zz[g.int_offset + d * g.K + i];
-      DevEval o;
-      eval_device(g, b, d, u, t, cfc, cqc, wf, wq, wj, o);
-      const int m = g.m;
-      const long long rb = g.res_base + (long long)d * m;
-      if (wf)
-        for (int i = 0; i < m; ++i) cf[rb + i] = o.I[i];
-      if (wq)
-        for (int i = 0; i < m; ++i) cq[rb + i] = o.Q[i];
-      if (wj) {
-        const long long jb = g.jac_base + (long long)d * m * m;
-        for (int i = 0; i < m * m; ++i) cj[jb + i] = o.J[i];
-      }
+      eval_soa<T>(g, b, flat - (int)g.dev_base, zz, t, cfc, cqc, wf, wq, wj, cf + g.res_base,
+                  cq + g.res_base, cj + g.jac_base);
     }
   }
 
   __device__ void assemble_res(double* fo, double* qo) {
     for (int i = threadIdx.x; i < A.S; i += NT) {
+      const long long p0 = A.res_ptr[i], p1 = A.res_ptr[i + 1];
       if (fo) {
         double acc = 0.0;
-        for (long long p = A.res_ptr[i]; p < A.res_ptr[i + 1]; ++p) acc += cf[A.res_src[p]];
+        for (long long p = p0; p < p1; ++p) acc += cf[A.res_src[p]];
         fo[i] = acc;
       }
       if (qo) {
         double acc = 0.0;
-        for (long long p = A.res_ptr[i]; p < A.res_ptr[i + 1]; ++p) acc += cq[A.res_src[p]];
+        for (long long p = p0; p < p1; ++p) acc += cq[A.res_src[p]];
         qo[i] = acc;
       }
     }
   }
 
-  // CSR values (+gmin) and the panels; residual rhs = -r
-  __device__ void assemble_system(int mode, double gmin, double h) {
+  // CSR values (+gmin), panels and rhs = -r. On the first iteration of a
+  // time step the state is still z_prev, so q(z_prev) (and, for BE, nothing
+  // else) is taken from this evaluation instead of a separate one.
+  __device__ void assemble_system(int mode, double gmin, double h, bool first) {
     for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
     assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
     for (int e = threadIdx.x; e < A.nnz; e += NT) {
       double acc = 0.0;
-      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += cj[A.jac_src[p]];
+      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += (double)cj[A.jac_src[p]];
       const int r = A.rows[e];
       if (r < A.nv && A.indices[e] == r) acc += gmin;
       data[e] = acc;
     }
+    if (first && mode != VXG_MODE_DC)
+      for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
     __syncthreads();
     for (int e = threadIdx.x; e < A.nnz; e += NT) work[A.a_pos[e]] = (T)data[e];
     for (int i = threadIdx.x; i < A.S; i += NT) {
@@ -313,13 +400,30 @@ struct Instance {
   }
 
   __device__ void factor() {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = NT / 32;
+    const int warp = threadIdx.x >> 5;
+    T* colb = sbuf + warp * 64;
+    T* rowb = colb + 32;
+    int* perm = ibuf + warp * 32;
     for (int L = 0; L < A.n_levels; ++L) {
       const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
-      for (long long p = lo + warp; p < hi; p += NT / 32) {
-        const int j = A.lv_sn[p];
-        warp_factor<T>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j], scr + A.lv_schur_off[p],
-                       lane);
+      if (A.lv_kmax[L] <= kTiny) {  // tiny supernodes: one thread each
+        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = A.lv_sn[p];
+          tiny_factor<T>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j], scr + A.lv_schur_off[p]);
+        }
+      } else if (hi - lo >= NW) {  // wide level: one warp per supernode
+        for (long long p = lo + warp; p < hi; p += NW) {
+          const int j = A.lv_sn[p];
+          sn_factor<T, false, NT>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j],
+                                  scr + A.lv_schur_off[p], colb, rowb, perm);
+        }
+      } else {  // narrow level: the whole CTA on each supernode
+        for (long long p = lo; p < hi; ++p) {
+          const int j = A.lv_sn[p];
+          sn_factor<T, true, NT>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j],
+                                 scr + A.lv_schur_off[p], sbuf, sbuf + 32, ibuf);
+        }
       }
       __syncthreads();
       for (long long t = A.lv_st_ptr[L] + threadIdx.x; t < A.lv_st_ptr[L + 1]; t += NT) {
@@ -336,6 +440,35 @@ struct Instance {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int L = 0; L < A.n_levels; ++L) {
       const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
+      if (A.lv_kmax[L] <= kTiny) {
+        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = A.lv_sn[p];
+          const int k = A.sn_k[j], r = A.sn_r[j];
+          const T* W = work + A.sn_panel[j];
+          const T* Lb = W + k * k + k * r;
+          const int* piv = A.sn_piv + A.sn_piv_ptr[j];
+          T* cb = scr + A.lv_bord_off[p];
+          T y[kTiny];
+#pragma unroll
+          for (int l = 0; l < kTiny; ++l) y[l] = l < k ? xt[piv[l]] : T(0);
+          for (int a = 0; a < r; ++a) {
+            T c = T(0);
+#pragma unroll
+            for (int l = 0; l < kTiny; ++l)
+              if (l < k) c += Lb[a * k + l] * y[l];
+            cb[a] = c;
+          }
+#pragma unroll
+          for (int i = 0; i < kTiny; ++i) {
+            if (i >= k) break;
+            T acc = T(0);
+#pragma unroll
+            for (int l = 0; l < kTiny; ++l)
+              if (l < k) acc += W[i * k + l] * y[l];
+            xt[piv[i]] = acc;
+          }
+        }
+      } else
       for (long long p = lo + warp; p < hi; p += NT / 32) {
         const int j = A.lv_sn[p];
         const int k = A.sn_k[j], r = A.sn_r[j];
@@ -370,10 +503,28 @@ struct Instance {
     }
     for (int L = A.n_levels - 1; L >= 0; --L) {
       const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
+      bool any = false;
+      if (A.lv_kmax[L] <= kTiny) {
+        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = A.lv_sn[p];
+          const int k = A.sn_k[j], r = A.sn_r[j];
+          const T* Ub = work + A.sn_panel[j] + k * k;
+          const int* piv = A.sn_piv + A.sn_piv_ptr[j];
+          const int* brd = A.sn_bord + A.sn_bord_ptr[j];
+          for (int i = 0; i < k; ++i) {
+            T acc = T(0);
+            for (int a = 0; a < r; ++a) acc += Ub[i * r + a] * xt[brd[a]];
+            xt[piv[i]] -= acc;
+          }
+        }
+        __syncthreads();
+        continue;
+      }
       for (long long p = lo + warp; p < hi; p += NT / 32) {
         const int j = A.lv_sn[p];
         const int k = A.sn_k[j], r = A.sn_r[j];
         if (r == 0) continue;
+        any = true;
         const T* Ub = work + A.sn_panel[j] + k * k;
         const int* piv = A.sn_piv + A.sn_piv_ptr[j];
         const int* brd = A.sn_bord + A.sn_bord_ptr[j];
@@ -383,6 +534,7 @@ struct Instance {
           xt[piv[lane]] -= acc;
         }
       }
+      (void)any;
       __syncthreads();
     }
   }
@@ -443,7 +595,7 @@ struct Instance {
     while (it < max_steps && !done) {
       eval(z, t, cfc, cqc, true, !dc, true);
       __syncthreads();
-      assemble_system(mode, gmin, h);
+      assemble_system(mode, gmin, h, it == 0);
       factor();
       solve(sizeof(T) == sizeof(float) ? A.refine : 0);
       done = update();
@@ -455,7 +607,7 @@ struct Instance {
 };
 
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) fused_kernel(const __grid_constant__ FusedArgs A) {
+__global__ void __launch_bounds__(NT, 4) fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L = fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr);
   Instance<T, NT> I{A, 0};
@@ -471,11 +623,13 @@ __global__ void __launch_bounds__(NT) fused_kernel(const __grid_constant__ Fused
   I.data = reinterpret_cast<double*>(smem + L.data);
   I.cf = reinterpret_cast<double*>(smem + L.cf);
   I.cq = reinterpret_cast<double*>(smem + L.cq);
-  I.cj = reinterpret_cast<double*>(smem + L.cj);
+  I.cj = reinterpret_cast<T*>(smem + L.cj);
   I.work = reinterpret_cast<T*>(smem + L.work);
   I.scr = reinterpret_cast<T*>(smem + L.scr);
   I.xt = reinterpret_cast<T*>(smem + L.xt);
   I.red = reinterpret_cast<double*>(smem + L.red);
+  I.sbuf = reinterpret_cast<T*>(smem + L.sbuf);
+  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * 2 * 32 * 8);
   const long long BS = (long long)A.B * A.S;
   for (int b = blockIdx.x; b < A.B; b += gridDim.x) {
     I.b = b;
@@ -502,12 +656,12 @@ __global__ void __launch_bounds__(NT) fused_kernel(const __grid_constant__ Fused
     }
     for (int n = 1; n < A.n_t; ++n) {
       const double tp = A.ts[n - 1], t = A.ts[n];
-      for (int i = threadIdx.x; i < A.S; i += NT) I.zp[i] = I.z[i];
-      __syncthreads();
-      I.eval(I.zp, tp, 1.0, 0.0, A.mode == VXG_MODE_TRAP, true, false);
-      __syncthreads();
-      I.assemble_res(A.mode == VXG_MODE_TRAP ? I.fp : nullptr, I.qp);
-      __syncthreads();
+      if (A.mode == VXG_MODE_TRAP) {  // f(z_prev, t_prev); q(z_prev) comes from iteration 0
+        I.eval(I.z, tp, 1.0, 0.0, true, false, false);
+        __syncthreads();
+        I.assemble_res(I.fp, nullptr);
+        __syncthreads();
+      }
       int its = 0;
       const int okn = I.newton(A.mode, t, tp, A.gmin, A.max_steps, &its);
       for (int i = threadIdx.x; i < A.S; i += NT)
@@ -601,6 +755,7 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   a.sn_piv_ptr = t.sn_piv_ptr;
   a.sn_bord_ptr = t.sn_bord_ptr;
   a.lv_ptr = t.d_lv_ptr;
+  a.lv_kmax = t.d_lv_kmax;
   a.lv_sn = t.lv_sn;
   a.lv_schur_off = t.lv_schur_off;
   a.lv_bord_off = t.lv_bord_off;

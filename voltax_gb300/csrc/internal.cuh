@@ -53,6 +53,7 @@ struct Topo {
   int* lv_sn;
   long long *lv_schur_off, *lv_bord_off;
   long long *d_lv_ptr, *d_lv_st_ptr, *d_lv_bt_ptr;  // device copies of the level pointers
+  int* d_lv_kmax;                                   // device copy of h_lv_kmax
   long long *st_tgt, *st_ptr, *st_src;
   int* bt_tgt;
   long long *bt_ptr, *bt_src;

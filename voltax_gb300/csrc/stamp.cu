@@ -3,11 +3,13 @@
 // Phase 1 (eval_kernel): one thread per (instance, device) gathers the
 // device's local unknowns, evaluates its physics (devices.cuh) and writes
 // its residual contributions and its local Jacobian block to contribution
-// slots (group-major, device-major, row-major within a block).
+// slots, laid out structure-of-arrays per group (slot (i, j) of device d at
+// (i*m + j)*n + d) so that neighbouring threads store to neighbouring words.
 //
 // Phase 2 (gather_kernel): one thread per (instance, CSR entry) or
-// (instance, row) sums its contribution slots in ascending slot order --
-// the canonical order (group, device, local row, local column) -- then adds
+// (instance, row) sums its contribution slots in the canonical order
+// (group, device, local row, local column; the host sorts each source list
+// by that key) -- then adds
 // gmin on node diagonals. The same inputs therefore always give the same
 // bits, and they equal the oracle's ordered np.add.at assembly bit for bit.
 // No atomics anywhere.
@@ -29,28 +31,10 @@ __global__ void eval_kernel(GroupTable gt, int B, const double* __restrict__ z, 
   while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
   const GroupDev& g = gt.g[gi];
   const int d = (int)(flat - g.dev_base);
-  const double* zb = z + (long long)b * S;
-  double u[kMaxM];
-  for (int i = 0; i < g.T; ++i) {
-    const int node = g.nodes[d * g.T + i];
-    u[i] = node >= 0 ? zb[node] : 0.0;
-  }
-  for (int i = 0; i < g.K; ++i) u[g.T + i] = zb[g.int_offset + d * g.K + i];
-  DevEval o;
-  eval_device(g, b, d, u, t, cf, cq, want_f, want_q, want_j, o);
-  const int m = g.m;
-  if (want_f) {
-    double* dst = cf_buf + (long long)b * n_res_slots + g.res_base + (long long)d * m;
-    for (int i = 0; i < m; ++i) dst[i] = o.I[i];
-  }
-  if (want_q) {
-    double* dst = cq_buf + (long long)b * n_res_slots + g.res_base + (long long)d * m;
-    for (int i = 0; i < m; ++i) dst[i] = o.Q[i];
-  }
-  if (want_j) {
-    double* dst = cj_buf + (long long)b * n_jac_slots + g.jac_base + (long long)d * m * m;
-    for (int i = 0; i < m * m; ++i) dst[i] = o.J[i];
-  }
+  eval_soa<double>(g, b, d, z + (long long)b * S, t, cf, cq, want_f, want_q, want_j,
+                   cf_buf + (long long)b * n_res_slots + g.res_base,
+                   cq_buf + (long long)b * n_res_slots + g.res_base,
+                   cj_buf + (long long)b * n_jac_slots + g.jac_base);
 }
 
 // data[e] = sum of Jacobian slots of entry e (+ gmin on node diagonals)

@@ -61,7 +61,7 @@ class Tables:
         offsets = ({g: (n, k, off) for g, n, k, off in circuit.layout.groups}
                    if circuit is not None else {})
         self.group_names, self.group_descs, self._nodes = [], [], []
-        res_tgt, jac_tgt = [], []
+        res_tgt, jac_tgt, res_id, jac_id = [], [], [], []
         res_base = jac_base = 0
         devices = list(zip(st.devices, st.stamps)) if circuit is not None else []
         for (name, allv, T, local), (_, pos, _) in devices:
@@ -76,18 +76,23 @@ class Tables:
             n_params = len(el.gpu_params())
             self.group_names.append(name)
             self.group_descs.append((el.kind, n, T, K, wave, n_params, off))
+            # canonical (AoS) order: device-major, then local row (and column);
+            # storage (SoA): slot (i, d) at i*n + d, slot (i, j, d) at (i*m + j)*n + d
             tg = allv.copy()  # terminal nodes then internals: the row of each slot
             tg[tg < 0] = -1
             res_tgt.append(tg.ravel())
+            dd, ii = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
+            res_id.append((res_base + ii * n + dd).ravel())
             pj = pos.reshape(n, m * m).astype(np.int64)
             jac_tgt.append(np.where(pj >= nnz, -1, pj).ravel())
+            dd, ee = np.meshgrid(np.arange(n), np.arange(m * m), indexing="ij")
+            jac_id.append((jac_base + ee * n + dd).ravel())
             res_base += n * m
             jac_base += n * m * m
         self.n_res_slots, self.n_jac_slots = res_base, jac_base
-        self.res_ptr, self.res_src = self._pull(np.concatenate(res_tgt) if res_tgt else
-                                                np.zeros(0, np.int64), S)
-        self.jac_ptr, self.jac_src = self._pull(np.concatenate(jac_tgt) if jac_tgt else
-                                                np.zeros(0, np.int64), nnz)
+        cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0, np.int64)  # noqa: E731
+        self.res_ptr, self.res_src = self._pull(cat(res_tgt), cat(res_id), S)
+        self.jac_ptr, self.jac_src = self._pull(cat(jac_tgt), cat(jac_id), nnz)
 
         # ---- segments
         if seg_ptr is None:
@@ -127,11 +132,13 @@ class Tables:
         self.work = int(plan.work)
 
     @staticmethod
-    def _pull(targets: np.ndarray, n_out: int):
-        """Slots grouped by target (ascending slot order); CSR over 0..n_out-1."""
+    def _pull(targets: np.ndarray, slot_ids: np.ndarray, n_out: int):
+        """Slots grouped by target; within a target in canonical order (the
+        position in `targets`), stored as their storage ids. CSR over
+        0..n_out-1."""
         keep = np.flatnonzero(targets >= 0)
         order = np.argsort(targets[keep], kind="stable")
-        src = keep[order].astype(np.int64)
+        src = slot_ids[keep[order]].astype(np.int64)
         counts = np.bincount(targets[keep], minlength=n_out)
         ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
         return ptr, np.ascontiguousarray(src)
