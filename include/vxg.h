@@ -53,7 +53,8 @@ enum {
   VXG_KIND_CAPACITOR = 1,   /* Capacitor                 [c]                    */
   VXG_KIND_VSOURCE = 2,     /* VoltageSource             [waveform rows]        */
   VXG_KIND_ISOURCE = 3,     /* CurrentSource             [waveform rows]        */
-  VXG_KIND_EKV = 4          /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w] */
+  VXG_KIND_EKV = 4          /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w,
+                                     1/n, 1/(2 vt), c_ox n vt, -(n-1)/n] */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 

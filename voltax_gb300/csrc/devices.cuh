@@ -284,82 +284,88 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
                                         double cf, double cq, bool wf, bool wq, bool wj,
                                         double* fo, double* qo, JT* jo) {
   const int n = g.n;
-  const EkvIn p = ekv_params(g, b, d);
-  const double vd = p.sign * u[0], vg = p.sign * u[1], vs = p.sign * u[2], vb = p.sign * u[3];
-  const double two_vt = 2.0 * p.vt;
-  const double vp = (vg - vb - p.vth - p.dvth) / p.n;
-  const double af = (vp - (vs - vb)) / two_vt;
-  const double ar = (vp - (vd - vb)) / two_vt;
-  double spf, sgf, spr, sgr;
-  softplus_and_sigmoid(af, &spf, &sgf);
-  softplus_and_sigmoid(ar, &spr, &sgr);
+  const bool neg = prm(g, 0, b, d) < 0.0;  // PMOS: evaluate in the mirrored n-frame
+  const double i_spec = prm(g, 1, b, d), vth = prm(g, 2, b, d), dvth = prm(g, 3, b, d);
+  const double nn = prm(g, 4, b, d), lam = prm(g, 6, b, d), c_ox = prm(g, 7, b, d);
+  const double cov_w = prm(g, 8, b, d), inv_n = prm(g, 9, b, d), inv_2vt = prm(g, 10, b, d);
+  const double scale = prm(g, 11, b, d), kb = prm(g, 12, b, d);
+  const double vd = neg ? -u[0] : u[0], vg = neg ? -u[1] : u[1];
+  const double vs = neg ? -u[2] : u[2], vb = neg ? -u[3] : u[3];
+  const double vp = (vg - vb - vth - dvth) * inv_n;
+  const double af = (vp - (vs - vb)) * inv_2vt;
+  const double ar = (vp - (vd - vb)) * inv_2vt;
+  // softplus(x) = max(x, 0) + log1p(exp(-|x|)), exp kept for the sigmoid
+  const double ef = exp(-fabs(af)), er = exp(-fabs(ar));
+  const double spf = fmax(af, 0.0) + log1p(ef), spr = fmax(ar, 0.0) + log1p(er);
   const double i_f = spf * spf, i_r = spr * spr;
   const bool need_i = wf || (wj && cf != 0.0);
   const bool need_q = wq || (wj && cq != 0.0);
   const double vds = vd - vs;
-  const double root = sqrt(vds * vds + 1e-3 * 1e-3);
-  const double mfac = 1.0 + p.lam * (root - 1e-3);
-  if (wf) {
-    const double ids = p.i_spec * (i_f - i_r) * mfac;
-    fo[0 * n + d] = p.sign * ids;
-    fo[1 * n + d] = p.sign * 0.0;
-    fo[2 * n + d] = p.sign * -ids;
-    fo[3 * n + d] = p.sign * 0.0;
+  double root = 0.0, mfac = 0.0;
+  if (need_i) {
+    root = sqrt(vds * vds + 1e-3 * 1e-3);
+    mfac = 1.0 + lam * (root - 1e-3);
   }
-  double xf = 0.0, xr = 0.0, s = 1.0, nd = 0.0, ns = 0.0, scale = 0.0, kb = 0.0;
+  if (wf) {
+    const double ids = i_spec * (i_f - i_r) * mfac;
+    fo[0 * n + d] = neg ? -ids : ids;
+    fo[1 * n + d] = 0.0;
+    fo[2 * n + d] = neg ? ids : -ids;
+    fo[3 * n + d] = 0.0;
+  }
+  double xf = 0.0, xr = 0.0, s = 1.0, nd = 0.0, ns = 0.0;
   if (need_q) {
     xf = sqrt(0.25 + i_f);
     xr = sqrt(0.25 + i_r);
-    scale = p.c_ox * p.n * p.vt;
     s = xf + xr;
-    nd = 3 * xr * xr * xr + 6 * xr * xr * xf + 4 * xr * xf * xf + 2 * xf * xf * xf;
-    ns = 3 * xf * xf * xf + 6 * xf * xf * xr + 4 * xf * xr * xr + 2 * xr * xr * xr;
-    kb = -(p.n - 1.0) / p.n;
+    const double xf2 = xf * xf, xr2 = xr * xr;
+    nd = xr2 * (3 * xr + 6 * xf) + xf2 * (4 * xr + 2 * xf);
+    ns = xf2 * (3 * xf + 6 * xr) + xr2 * (4 * xf + 2 * xr);
   }
   if (wq) {
-    const double s2 = s * s;
-    const double c415 = 4.0 / 15.0;
-    const double q_d = -scale * (c415 * nd / s2 - 0.5);
-    const double q_s = -scale * (c415 * ns / s2 - 0.5);
+    const double w415 = (4.0 / 15.0) / (s * s);
+    const double q_d = -scale * (w415 * nd - 0.5);
+    const double q_s = -scale * (w415 * ns - 0.5);
     const double q_i = q_d + q_s;
-    const double q_b = kb * (p.c_ox * (vg - vb) + q_i);
+    const double q_b = kb * (c_ox * (vg - vb) + q_i);
     const double q_g = -(q_i + q_b);
-    const double q_gs = p.cov_w * (vg - vs), q_gd = p.cov_w * (vg - vd);
-    qo[0 * n + d] = p.sign * (q_d + -q_gd);
-    qo[1 * n + d] = p.sign * (q_g + (q_gs + q_gd));
-    qo[2 * n + d] = p.sign * (q_s + -q_gs);
-    qo[3 * n + d] = p.sign * (q_b + 0.0);
+    const double q_gs = cov_w * (vg - vs), q_gd = cov_w * (vg - vd);
+    const double o0 = q_d - q_gd, o1 = q_g + (q_gs + q_gd), o2 = q_s - q_gs;
+    qo[0 * n + d] = neg ? -o0 : o0;
+    qo[1 * n + d] = neg ? -o1 : o1;
+    qo[2 * n + d] = neg ? -o2 : o2;
+    qo[3 * n + d] = neg ? -q_b : q_b;
   }
   if (!wj) return;
   // derivatives in JT
-  const JT tv = (JT)two_vt;
-  const JT g1 = JT(1) / (JT)p.n;
-  const JT af_g = g1 / tv, af_s = JT(-1) / tv, af_b = (JT(1) - g1) / tv;
-  const JT dif = JT(2) * (JT)spf * (JT)sgf, dir = JT(2) * (JT)spr * (JT)sgr;
+  const JT tv2 = (JT)inv_2vt;
+  const JT g1 = (JT)inv_n;
+  const JT af_g = g1 * tv2, af_s = -tv2, af_b = (JT(1) - g1) * tv2;
+  const JT sgf = af >= 0.0 ? JT(1) / (JT(1) + (JT)ef) : (JT)ef / (JT(1) + (JT)ef);
+  const JT sgr = ar >= 0.0 ? JT(1) / (JT(1) + (JT)er) : (JT)er / (JT(1) + (JT)er);
+  const JT dif = JT(2) * (JT)spf * sgf, dir = JT(2) * (JT)spr * sgr;
   const JT cfj = (JT)cf, cqj = (JT)cq;
   JT ji[4] = {JT(0), JT(0), JT(0), JT(0)};
   if (need_i && cf != 0.0) {
-    const JT isp = (JT)p.i_spec, mf = (JT)mfac, dI = (JT)(i_f - i_r);
-    const JT dsa = (JT)(vds / root), lam = (JT)p.lam;
-    // d ids / d (vd, vg, vs, vb)
-    ji[0] = isp * ((-dir * af_s) * mf + dI * lam * dsa);
+    const JT isp = (JT)i_spec, mf = (JT)mfac, dI = (JT)(i_f - i_r);
+    const JT dsa = (JT)vds / (JT)root, lmj = (JT)lam;
+    ji[0] = isp * ((-dir * af_s) * mf + dI * lmj * dsa);
     ji[1] = isp * ((dif - dir) * af_g * mf);
-    ji[2] = isp * ((dif * af_s) * mf - dI * lam * dsa);
+    ji[2] = isp * ((dif * af_s) * mf - dI * lmj * dsa);
     ji[3] = isp * ((dif - dir) * af_b * mf);
   }
   JT dq0[4] = {JT(0), JT(0), JT(0), JT(0)}, dq1[4] = {JT(0), JT(0), JT(0), JT(0)};
   JT dq2[4] = {JT(0), JT(0), JT(0), JT(0)}, dq3[4] = {JT(0), JT(0), JT(0), JT(0)};
   if (need_q && cq != 0.0) {
     const JT fx = (JT)xf, rx = (JT)xr, ss = (JT)s, s3 = ss * ss * ss;
-    const JT ndj = (JT)nd, nsj = (JT)ns, sc = (JT)scale, kbj = (JT)kb, cox = (JT)p.c_ox;
-    const JT cw = (JT)p.cov_w;
+    const JT ndj = (JT)nd, nsj = (JT)ns, sc = (JT)scale, kbj = (JT)kb, cox = (JT)c_ox;
+    const JT cw = (JT)cov_w;
     const JT gd_f = ((JT(6) * rx * rx + JT(8) * rx * fx + JT(6) * fx * fx) * ss - JT(2) * ndj) / s3;
     const JT gd_r = ((JT(9) * rx * rx + JT(12) * rx * fx + JT(4) * fx * fx) * ss - JT(2) * ndj) / s3;
     const JT gs_f = ((JT(9) * fx * fx + JT(12) * fx * rx + JT(4) * rx * rx) * ss - JT(2) * nsj) / s3;
     const JT gs_r = ((JT(6) * fx * fx + JT(8) * fx * rx + JT(6) * rx * rx) * ss - JT(2) * nsj) / s3;
     const JT dxf_da = dif / (JT(2) * fx), dxr_da = dir / (JT(2) * rx);
     const JT c415 = JT(4) / JT(15);
-    // daf, dar per terminal (vd, vg, vs, vb)
     const JT dafk[4] = {JT(0), af_g, af_s, af_b};
     const JT dark[4] = {af_s, af_g, JT(0), af_b};
 #pragma unroll

@@ -78,7 +78,7 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.rhs = take(d * S);
   L.dz = take(d * S);
   L.res = take(d * S);
-  L.data = take(d * nnz);
+  L.data = take(sizeof(T) * nnz);
   L.cf = take(d * n_res);
   L.cq = take(d * n_res);
   L.cj = take(sizeof(T) * n_jac);
@@ -335,8 +335,8 @@ template <typename T, int NT>
 struct Instance {
   const FusedArgs& A;
   int b;
-  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *data, *cf, *cq, *red;
-  T *cj, *work, *scr, *xt, *sbuf;
+  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *cf, *cq, *red;
+  T *data, *cj, *work, *scr, *xt, *sbuf;
   int* ibuf;
 
   // devices -> contribution slots (structure of arrays per group)
@@ -374,17 +374,20 @@ struct Instance {
   __device__ void assemble_system(int mode, double gmin, double h, bool first) {
     for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
     assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
+    // Jacobian values in the panel type: FP64 in the plain form; FP32 in the
+    // chosen form, where they feed the FP32 factorization and the FP64
+    // refinement residual rhs - J dz (accumulated in FP64)
     for (int e = threadIdx.x; e < A.nnz; e += NT) {
-      double acc = 0.0;
-      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += (double)cj[A.jac_src[p]];
+      T acc = T(0);
+      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += cj[A.jac_src[p]];
       const int r = A.rows[e];
-      if (r < A.nv && A.indices[e] == r) acc += gmin;
+      if (r < A.nv && A.indices[e] == r) acc += (T)gmin;
       data[e] = acc;
     }
     if (first && mode != VXG_MODE_DC)
       for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
     __syncthreads();
-    for (int e = threadIdx.x; e < A.nnz; e += NT) work[A.a_pos[e]] = (T)data[e];
+    for (int e = threadIdx.x; e < A.nnz; e += NT) work[A.a_pos[e]] = data[e];
     for (int i = threadIdx.x; i < A.S; i += NT) {
       const double gm = i < A.nv ? gmin * z[i] : 0.0;
       double r;
@@ -549,7 +552,8 @@ struct Instance {
     for (int it = 0; it < refine; ++it) {
       for (int i = threadIdx.x; i < A.S; i += NT) {
         double acc = 0.0;
-        for (long long e = A.indptr[i]; e < A.indptr[i + 1]; ++e) acc += data[e] * dz[A.indices[e]];
+        for (long long e = A.indptr[i]; e < A.indptr[i + 1]; ++e)
+          acc += (double)data[e] * dz[A.indices[e]];
         xt[i] = (T)(rhs[i] - acc);
       }
       __syncthreads();
@@ -607,7 +611,7 @@ struct Instance {
 };
 
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, 4) fused_kernel(const __grid_constant__ FusedArgs A) {
+__global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L = fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr);
   Instance<T, NT> I{A, 0};
@@ -620,7 +624,7 @@ __global__ void __launch_bounds__(NT, 4) fused_kernel(const __grid_constant__ Fu
   I.rhs = reinterpret_cast<double*>(smem + L.rhs);
   I.dz = reinterpret_cast<double*>(smem + L.dz);
   I.res = reinterpret_cast<double*>(smem + L.res);
-  I.data = reinterpret_cast<double*>(smem + L.data);
+  I.data = reinterpret_cast<T*>(smem + L.data);
   I.cf = reinterpret_cast<double*>(smem + L.cf);
   I.cq = reinterpret_cast<double*>(smem + L.cq);
   I.cj = reinterpret_cast<T*>(smem + L.cj);
@@ -786,6 +790,12 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   a.conv = converged;
   a.iters = iters;
   cudaStream_t s = (cudaStream_t)stream;
-  if (o->precision == VXG_F32) return launch_fused<float, 128>(a, smem, s);
-  return launch_fused<double, 128>(a, smem, s);
+  int dev = 0, sms = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // few instances: wider CTAs shorten each instance's critical path
+  const bool wide = batch < 2 * sms;
+  if (o->precision == VXG_F32)
+    return wide ? launch_fused<float, 256>(a, smem, s) : launch_fused<float, 128>(a, smem, s);
+  return wide ? launch_fused<double, 256>(a, smem, s) : launch_fused<double, 128>(a, smem, s);
 }

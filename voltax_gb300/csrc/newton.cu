@@ -251,7 +251,7 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
   }
 }
 
-constexpr int kMaxParams = 9;
+constexpr int kMaxParams = 13;
 
 struct GradPtrs {
   double* p[VXG_MAX_GROUPS];

@@ -30,7 +30,7 @@ _F64 = torch.float64
 VT_300K = 0.025852
 """Thermal voltage kT/q at 300 K (voltax/elements/semiconductor.py:13)."""
 
-# kernel codes of the device table (must match csrc/vxg_types.h)
+# kernel codes of the device table (must match include/vxg.h)
 KIND_CONDUCTANCE = 0
 KIND_CAPACITOR = 1
 KIND_VSOURCE = 2
@@ -403,7 +403,8 @@ class EKVMOSFET(Element):
     """EKV 2.6-style MOSFET (mosfet.py:155-205); terminals ``(d, g, s, b)``.
 
     Kernel parameter rows (all per device): sign, i_spec = 2 n kp (W/L) vt^2,
-    vth, dvth, n, vt, lam, c_ox = cox W L, cov W.
+    vth, dvth, n, vt, lam, c_ox = cox W L, cov W, then the derived 1/n,
+    1/(2 vt), c_ox n vt and -(n - 1)/n.
     """
 
     terminals = ("d", "g", "s", "b")
@@ -447,8 +448,13 @@ class EKVMOSFET(Element):
         def full(x):
             return _t(x).expand(shape)
 
+        c_ox = p.cox * w * l
+        # rows 9-12 are derived from rows 4, 5 and 7 so the kernel multiplies
+        # instead of dividing; gradients flow through rows 0-8
         return [full(self.sign), i_spec, full(p.vth), self.dvth.expand(shape),
-                full(p.n), full(p.vt), full(p.lam), p.cox * w * l, p.cov * w]
+                full(p.n), full(p.vt), full(p.lam), c_ox, p.cov * w,
+                full(1.0 / p.n), full(1.0 / (2.0 * p.vt)), c_ox * p.n * p.vt,
+                full(-(p.n - 1.0) / p.n)]
 
 
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
