@@ -136,7 +136,8 @@ static void free_topo(Topo& t) {
                   t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
                   t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
                   t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
-                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax};
+                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax,
+                  t.d_blob};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < t.n_groups; ++i)
@@ -149,6 +150,75 @@ static void free_topo(Topo& t) {
   delete[] t.h_lv_bt_ptr;
   delete[] t.h_lv_kmax;
   delete[] t.h_lv_rmax;
+}
+
+// Build the 16-bit table blob of the fused kernel; false if a value does not fit.
+static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& out, Blob& b) {
+  bool ok = true;
+  auto push = [&](int sec, const auto* src, long long n, bool nodes = false) {
+    b.off[sec] = (int)out.size();
+    for (long long i = 0; i < n; ++i) {
+      const long long v = (long long)src[i];
+      if (nodes && v < 0) {
+        out.push_back(0xFFFF);
+      } else if (v < 0 || v >= 0xFFFF) {
+        ok = false;
+        out.push_back(0);
+      } else {
+        out.push_back((unsigned short)v);
+      }
+    }
+  };
+  const long long S = d->size, nnz = d->nnz, nl = d->n_levels, nsn = d->n_sn;
+  push(B_RES_PTR, d->res_ptr, S + 1);
+  push(B_RES_SRC, d->res_src, d->res_ptr[S]);
+  push(B_JAC_PTR, d->jac_ptr, nnz + 1);
+  push(B_JAC_SRC, d->jac_src, d->jac_ptr[nnz]);
+  push(B_ROWS, d->rows, nnz);
+  push(B_INDICES, d->indices, nnz);
+  push(B_INDPTR, d->indptr, S + 1);
+  push(B_APOS, d->a_pos, nnz);
+  push(B_SN_K, d->sn_k, nsn);
+  push(B_SN_R, d->sn_r, nsn);
+  push(B_SN_PANEL, d->sn_panel, nsn);
+  push(B_SN_PIV_PTR, d->sn_piv_ptr, nsn + 1);
+  push(B_SN_PIV, d->sn_piv, d->sn_piv_ptr[nsn]);
+  push(B_SN_BORD_PTR, d->sn_bord_ptr, nsn + 1);
+  push(B_SN_BORD, d->sn_bord, d->sn_bord_ptr[nsn]);
+  push(B_LV_PTR, d->lv_ptr, nl + 1);
+  std::vector<int> kmax(nl, 0);
+  for (long long L = 0; L < nl; ++L)
+    for (long long q = d->lv_ptr[L]; q < d->lv_ptr[L + 1]; ++q)
+      kmax[L] = std::max(kmax[L], d->sn_k[d->lv_sn[q]]);
+  push(B_LV_KMAX, kmax.data(), nl);
+  push(B_LV_SN, d->lv_sn, d->lv_ptr[nl]);
+  push(B_LV_SCHUR_OFF, d->lv_schur_off, d->lv_ptr[nl]);
+  push(B_LV_BORD_OFF, d->lv_bord_off, d->lv_ptr[nl]);
+  const long long nst = d->lv_st_ptr[nl], nbt = d->lv_bt_ptr[nl];
+  push(B_LV_ST_PTR, d->lv_st_ptr, nl + 1);
+  push(B_ST_TGT, d->st_tgt, nst);
+  push(B_ST_PTR, d->st_ptr, nst + 1);
+  push(B_ST_SRC, d->st_src, d->st_ptr[nst]);
+  push(B_LV_BT_PTR, d->lv_bt_ptr, nl + 1);
+  push(B_BT_TGT, d->bt_tgt, nbt);
+  push(B_BT_PTR, d->bt_ptr, nbt + 1);
+  push(B_BT_SRC, d->bt_src, d->bt_ptr[nbt]);
+  b.off[B_NODES] = (int)out.size();
+  for (int g = 0; g < d->n_groups; ++g) {
+    b.node_off[g] = (int)out.size() - b.off[B_NODES];
+    const long long cnt = (long long)d->groups[g].n * d->groups[g].T;
+    const int32_t* nd = d->groups[g].nodes;
+    for (long long i = 0; i < cnt; ++i) {
+      const long long v = nd[i];
+      if (v < 0) out.push_back(0xFFFF);
+      else if (v >= 0xFFFF) { ok = false; out.push_back(0); }
+      else out.push_back((unsigned short)v);
+    }
+  }
+  b.off[B_COUNT] = (int)out.size();
+  while (out.size() % 8) out.push_back(0);  // 16-byte granules for the copy
+  b.len = (int)out.size();
+  return ok;
 }
 
 }  // namespace vxg
@@ -253,6 +323,10 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
       }
     }
     st = upload(&t.d_lv_kmax, t.h_lv_kmax, (size_t)nl);
+  }
+  if (st == VXG_OK) {
+    std::vector<unsigned short> blob;
+    if (build_blob(d, blob, t.blob)) st = upload(&t.d_blob, blob.data(), blob.size());
   }
   if (st == VXG_OK) {
     cudaError_t e = cudaMallocHost((void**)&t.h_flag, sizeof(int) * 4);

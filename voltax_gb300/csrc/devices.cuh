@@ -405,23 +405,12 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
 
 // Evaluate device d of group g (instance b) reading state zz; write its slots.
 // fo/qo/jo point at the group's first slot in each contribution array.
+// u: the device's local unknowns (terminal voltages, then internals).
 template <typename JT>
-__device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const double* zz,
+__device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const double* u,
                                          double t, double cf, double cq, bool wf, bool wq,
                                          bool wj, double* fo, double* qo, JT* jo) {
   const int n = g.n;
-  double u[kMaxM];
-#pragma unroll
-  for (int i = 0; i < kMaxM; ++i) {
-    if (i < g.T) {
-      const int node = g.nodes[d * g.T + i];
-      u[i] = node >= 0 ? zz[node] : 0.0;
-    } else if (i < g.m) {
-      u[i] = zz[g.int_offset + d * g.K + (i - g.T)];
-    } else {
-      u[i] = 0.0;
-    }
-  }
   switch (g.kind) {
     case VXG_KIND_CONDUCTANCE: {
       const double gg = prm(g, 0, b, d);
@@ -509,4 +498,22 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
   }
 }
 
+}  // namespace vxg
+
+namespace vxg {
+// Local unknowns of device d from the state, node table in global memory.
+__device__ __forceinline__ void gather_u(const GroupDev& g, int d, const double* zz,
+                                         double* u) {
+#pragma unroll
+  for (int i = 0; i < kMaxM; ++i) {
+    if (i < g.T) {
+      const int node = g.nodes[d * g.T + i];
+      u[i] = node >= 0 ? zz[node] : 0.0;
+    } else if (i < g.m) {
+      u[i] = zz[g.int_offset + d * g.K + (i - g.T)];
+    } else {
+      u[i] = 0.0;
+    }
+  }
+}
 }  // namespace vxg

@@ -40,6 +40,8 @@ struct FusedArgs {
   const long long* lv_bt_ptr;
   const int* bt_tgt;
   const long long *bt_ptr, *bt_src;
+  const unsigned short* blob;  // 16-bit tables (global), staged into shared memory
+  Blob bo;
   int B, mode, n_t, max_steps, refine, dc_first, gmin_steps, direct_steps;
   double rtol, atol, max_dv, gmin;
   const double* ts;
@@ -54,15 +56,17 @@ __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15;
 
 // Shared-memory layout of one instance.
 struct FusedLayout {
-  size_t z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, sbuf, total;
+  size_t blob, z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, sbuf, total;
 };
 
 template <typename T>
 __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, int n_jac,
-                                                    int work, int max_scr) {
+                                                    int work, int max_scr, int blob_len) {
   // T is the panel type; the Jacobian contributions use the same type
   FusedLayout L;
   size_t o = 0;
+  L.blob = o;
+  o = a16(o + sizeof(unsigned short) * (size_t)blob_len);
   auto take = [&](size_t bytes) {
     size_t at = o;
     o = a16(o + bytes);
@@ -331,6 +335,8 @@ __device__ void tiny_factor(T* P, int k, int r, T* Sout) {
 }
 
 // ------------------------------------------------------------- one instance
+typedef unsigned short u16;
+
 template <typename T, int NT>
 struct Instance {
   const FusedArgs& A;
@@ -338,56 +344,82 @@ struct Instance {
   double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *cf, *cq, *red;
   T *data, *cj, *work, *scr, *xt, *sbuf;
   int* ibuf;
+  const u16* tb;  // shared-memory tables
+
+  __device__ __forceinline__ const u16* sec(int k) const { return tb + A.bo.off[k]; }
 
   // devices -> contribution slots (structure of arrays per group)
   __device__ void eval(const double* zz, double t, double cfc, double cqc, bool wf, bool wq,
                        bool wj) {
     const GroupTable& gt = A.gt;
+    const u16* nodes = sec(B_NODES);
     for (int flat = threadIdx.x; flat < gt.n_dev; flat += NT) {
       int gi = 0;
       while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
       const GroupDev& g = gt.g[gi];
-      eval_soa<T>(g, b, flat - (int)g.dev_base, zz, t, cfc, cqc, wf, wq, wj, cf + g.res_base,
-                  cq + g.res_base, cj + g.jac_base);
+      const int d = flat - (int)g.dev_base;
+      const u16* nd = nodes + A.bo.node_off[gi] + d * g.T;
+      double u[kMaxM];
+#pragma unroll
+      for (int i = 0; i < kMaxM; ++i) {
+        if (i < g.T) {
+          const u16 node = nd[i];
+          u[i] = node != 0xFFFF ? zz[node] : 0.0;
+        } else if (i < g.m) {
+          u[i] = zz[g.int_offset + d * g.K + (i - g.T)];
+        } else {
+          u[i] = 0.0;
+        }
+      }
+      eval_soa<T>(g, b, d, u, t, cfc, cqc, wf, wq, wj, cf + g.res_base, cq + g.res_base,
+                  cj + g.jac_base);
     }
   }
 
   __device__ void assemble_res(double* fo, double* qo) {
+    const u16* ptr = sec(B_RES_PTR);
+    const u16* src = sec(B_RES_SRC);
     for (int i = threadIdx.x; i < A.S; i += NT) {
-      const long long p0 = A.res_ptr[i], p1 = A.res_ptr[i + 1];
+      const int p0 = ptr[i], p1 = ptr[i + 1];
       if (fo) {
         double acc = 0.0;
-        for (long long p = p0; p < p1; ++p) acc += cf[A.res_src[p]];
+        for (int p = p0; p < p1; ++p) acc += cf[src[p]];
         fo[i] = acc;
       }
       if (qo) {
         double acc = 0.0;
-        for (long long p = p0; p < p1; ++p) acc += cq[A.res_src[p]];
+        for (int p = p0; p < p1; ++p) acc += cq[src[p]];
         qo[i] = acc;
       }
     }
   }
 
   // CSR values (+gmin), panels and rhs = -r. On the first iteration of a
-  // time step the state is still z_prev, so q(z_prev) (and, for BE, nothing
-  // else) is taken from this evaluation instead of a separate one.
+  // time step the state is still z_prev, so q(z_prev) is taken from this
+  // evaluation instead of a separate one.
   __device__ void assemble_system(int mode, double gmin, double h, bool first) {
     for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
     assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
     // Jacobian values in the panel type: FP64 in the plain form; FP32 in the
     // chosen form, where they feed the FP32 factorization and the FP64
     // refinement residual rhs - J dz (accumulated in FP64)
+    const u16* jptr = sec(B_JAC_PTR);
+    const u16* jsrc = sec(B_JAC_SRC);
+    const u16* rows = sec(B_ROWS);
+    const u16* cols = sec(B_INDICES);
     for (int e = threadIdx.x; e < A.nnz; e += NT) {
       T acc = T(0);
-      for (long long p = A.jac_ptr[e]; p < A.jac_ptr[e + 1]; ++p) acc += cj[A.jac_src[p]];
-      const int r = A.rows[e];
-      if (r < A.nv && A.indices[e] == r) acc += (T)gmin;
+      const int p1 = jptr[e + 1];
+      for (int p = jptr[e]; p < p1; ++p) acc += cj[jsrc[p]];
+      const int r = rows[e];
+      if (r < A.nv && cols[e] == r) acc += (T)gmin;
       data[e] = acc;
     }
     if (first && mode != VXG_MODE_DC)
       for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
     __syncthreads();
-    for (int e = threadIdx.x; e < A.nnz; e += NT) work[A.a_pos[e]] = data[e];
+    const u16* apos = sec(B_APOS);
+    for (int e = threadIdx.x; e < A.nnz; e += NT) work[apos[e]] = data[e];
     for (int i = threadIdx.x; i < A.S; i += NT) {
       const double gm = i < A.nv ? gmin * z[i] : 0.0;
       double r;
@@ -408,31 +440,36 @@ struct Instance {
     T* colb = sbuf + warp * 64;
     T* rowb = colb + 32;
     int* perm = ibuf + warp * 32;
+    const u16 *lv_ptr = sec(B_LV_PTR), *lv_kmax = sec(B_LV_KMAX), *lv_sn = sec(B_LV_SN);
+    const u16 *sch_off = sec(B_LV_SCHUR_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
+    const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR), *st_tgt = sec(B_ST_TGT);
+    const u16 *st_ptr = sec(B_ST_PTR), *st_src = sec(B_ST_SRC);
     for (int L = 0; L < A.n_levels; ++L) {
-      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
-      if (A.lv_kmax[L] <= kTiny) {  // tiny supernodes: one thread each
-        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
-          const int j = A.lv_sn[p];
-          tiny_factor<T>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j], scr + A.lv_schur_off[p]);
+      const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
+      if (lv_kmax[L] <= kTiny) {  // tiny supernodes: one thread each
+        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = lv_sn[p];
+          tiny_factor<T>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p]);
         }
       } else if (hi - lo >= NW) {  // wide level: one warp per supernode
-        for (long long p = lo + warp; p < hi; p += NW) {
-          const int j = A.lv_sn[p];
-          sn_factor<T, false, NT>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j],
-                                  scr + A.lv_schur_off[p], colb, rowb, perm);
+        for (int p = lo + warp; p < hi; p += NW) {
+          const int j = lv_sn[p];
+          sn_factor<T, false, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], colb,
+                                  rowb, perm);
         }
       } else {  // narrow level: the whole CTA on each supernode
-        for (long long p = lo; p < hi; ++p) {
-          const int j = A.lv_sn[p];
-          sn_factor<T, true, NT>(work + A.sn_panel[j], A.sn_k[j], A.sn_r[j],
-                                 scr + A.lv_schur_off[p], sbuf, sbuf + 32, ibuf);
+        for (int p = lo; p < hi; ++p) {
+          const int j = lv_sn[p];
+          sn_factor<T, true, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], sbuf,
+                                 sbuf + 32, ibuf);
         }
       }
       __syncthreads();
-      for (long long t = A.lv_st_ptr[L] + threadIdx.x; t < A.lv_st_ptr[L + 1]; t += NT) {
+      for (int t = st_lv[L] + threadIdx.x; t < st_lv[L + 1]; t += NT) {
         T acc = T(0);
-        for (long long p = A.st_ptr[t]; p < A.st_ptr[t + 1]; ++p) acc += scr[A.st_src[p]];
-        work[A.st_tgt[t]] -= acc;
+        const int p1 = st_ptr[t + 1];
+        for (int p = st_ptr[t]; p < p1; ++p) acc += scr[st_src[p]];
+        work[st_tgt[t]] -= acc;
       }
       __syncthreads();
     }
@@ -441,16 +478,22 @@ struct Instance {
   // in-place solve of xt
   __device__ void solve_t() {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u16 *lv_ptr = sec(B_LV_PTR), *lv_kmax = sec(B_LV_KMAX), *lv_sn = sec(B_LV_SN);
+    const u16 *bord_off = sec(B_LV_BORD_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
+    const u16 *sn_panel = sec(B_SN_PANEL), *piv_ptr = sec(B_SN_PIV_PTR), *pivs = sec(B_SN_PIV);
+    const u16 *bord_ptr = sec(B_SN_BORD_PTR), *bords = sec(B_SN_BORD);
+    const u16 *bt_lv = sec(B_LV_BT_PTR), *bt_tgt = sec(B_BT_TGT), *bt_ptr = sec(B_BT_PTR);
+    const u16* bt_src = sec(B_BT_SRC);
     for (int L = 0; L < A.n_levels; ++L) {
-      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
-      if (A.lv_kmax[L] <= kTiny) {
-        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
-          const int j = A.lv_sn[p];
-          const int k = A.sn_k[j], r = A.sn_r[j];
-          const T* W = work + A.sn_panel[j];
+      const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
+      if (lv_kmax[L] <= kTiny) {
+        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          const T* W = work + sn_panel[j];
           const T* Lb = W + k * k + k * r;
-          const int* piv = A.sn_piv + A.sn_piv_ptr[j];
-          T* cb = scr + A.lv_bord_off[p];
+          const u16* piv = pivs + piv_ptr[j];
+          T* cb = scr + bord_off[p];
           T y[kTiny];
 #pragma unroll
           for (int l = 0; l < kTiny; ++l) y[l] = l < k ? xt[piv[l]] : T(0);
@@ -471,73 +514,71 @@ struct Instance {
             xt[piv[i]] = acc;
           }
         }
-      } else
-      for (long long p = lo + warp; p < hi; p += NT / 32) {
-        const int j = A.lv_sn[p];
-        const int k = A.sn_k[j], r = A.sn_r[j];
-        const T* W = work + A.sn_panel[j];
-        const T* Lb = W + k * k + k * r;
-        const int* piv = A.sn_piv + A.sn_piv_ptr[j];
-        const T y = lane < k ? xt[piv[lane]] : T(0);
-        T acc = T(0);
-        T* cb = scr + A.lv_bord_off[p];
-        for (int l = 0; l < k; ++l) {
-          const T yl = __shfl_sync(kFull, y, l);
-          if (lane < k) acc += W[lane * k + l] * yl;
-        }
-        for (int a0 = 0; a0 < r; a0 += 32) {
-          const int a = a0 + lane;
-          T c = T(0);
+      } else {
+        for (int p = lo + warp; p < hi; p += NT / 32) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          const T* W = work + sn_panel[j];
+          const T* Lb = W + k * k + k * r;
+          const u16* piv = pivs + piv_ptr[j];
+          const T y = lane < k ? xt[piv[lane]] : T(0);
+          T acc = T(0);
+          T* cb = scr + bord_off[p];
           for (int l = 0; l < k; ++l) {
             const T yl = __shfl_sync(kFull, y, l);
-            if (a < r) c += Lb[a * k + l] * yl;
+            if (lane < k) acc += W[lane * k + l] * yl;
           }
-          if (a < r) cb[a] = c;
+          for (int a0 = 0; a0 < r; a0 += 32) {
+            const int a = a0 + lane;
+            T c = T(0);
+            for (int l = 0; l < k; ++l) {
+              const T yl = __shfl_sync(kFull, y, l);
+              if (a < r) c += Lb[a * k + l] * yl;
+            }
+            if (a < r) cb[a] = c;
+          }
+          if (lane < k) xt[piv[lane]] = acc;
         }
-        if (lane < k) xt[piv[lane]] = acc;
       }
       __syncthreads();
-      for (long long t = A.lv_bt_ptr[L] + threadIdx.x; t < A.lv_bt_ptr[L + 1]; t += NT) {
+      for (int t = bt_lv[L] + threadIdx.x; t < bt_lv[L + 1]; t += NT) {
         T acc = T(0);
-        for (long long p = A.bt_ptr[t]; p < A.bt_ptr[t + 1]; ++p) acc += scr[A.bt_src[p]];
-        xt[A.bt_tgt[t]] -= acc;
+        const int p1 = bt_ptr[t + 1];
+        for (int p = bt_ptr[t]; p < p1; ++p) acc += scr[bt_src[p]];
+        xt[bt_tgt[t]] -= acc;
       }
       __syncthreads();
     }
     for (int L = A.n_levels - 1; L >= 0; --L) {
-      const long long lo = A.lv_ptr[L], hi = A.lv_ptr[L + 1];
-      bool any = false;
-      if (A.lv_kmax[L] <= kTiny) {
-        for (long long p = lo + threadIdx.x; p < hi; p += NT) {
-          const int j = A.lv_sn[p];
-          const int k = A.sn_k[j], r = A.sn_r[j];
-          const T* Ub = work + A.sn_panel[j] + k * k;
-          const int* piv = A.sn_piv + A.sn_piv_ptr[j];
-          const int* brd = A.sn_bord + A.sn_bord_ptr[j];
+      const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
+      if (lv_kmax[L] <= kTiny) {
+        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          const T* Ub = work + sn_panel[j] + k * k;
+          const u16* piv = pivs + piv_ptr[j];
+          const u16* brd = bords + bord_ptr[j];
           for (int i = 0; i < k; ++i) {
             T acc = T(0);
             for (int a = 0; a < r; ++a) acc += Ub[i * r + a] * xt[brd[a]];
             xt[piv[i]] -= acc;
           }
         }
-        __syncthreads();
-        continue;
-      }
-      for (long long p = lo + warp; p < hi; p += NT / 32) {
-        const int j = A.lv_sn[p];
-        const int k = A.sn_k[j], r = A.sn_r[j];
-        if (r == 0) continue;
-        any = true;
-        const T* Ub = work + A.sn_panel[j] + k * k;
-        const int* piv = A.sn_piv + A.sn_piv_ptr[j];
-        const int* brd = A.sn_bord + A.sn_bord_ptr[j];
-        if (lane < k) {
-          T acc = T(0);
-          for (int a = 0; a < r; ++a) acc += Ub[lane * r + a] * xt[brd[a]];
-          xt[piv[lane]] -= acc;
+      } else {
+        for (int p = lo + warp; p < hi; p += NT / 32) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          if (r == 0) continue;
+          const T* Ub = work + sn_panel[j] + k * k;
+          const u16* piv = pivs + piv_ptr[j];
+          const u16* brd = bords + bord_ptr[j];
+          if (lane < k) {
+            T acc = T(0);
+            for (int a = 0; a < r; ++a) acc += Ub[lane * r + a] * xt[brd[a]];
+            xt[piv[lane]] -= acc;
+          }
         }
       }
-      (void)any;
       __syncthreads();
     }
   }
@@ -549,11 +590,13 @@ struct Instance {
     solve_t();
     for (int i = threadIdx.x; i < A.S; i += NT) dz[i] = (double)xt[i];
     __syncthreads();
+    const u16* indptr = sec(B_INDPTR);
+    const u16* cols = sec(B_INDICES);
     for (int it = 0; it < refine; ++it) {
       for (int i = threadIdx.x; i < A.S; i += NT) {
         double acc = 0.0;
-        for (long long e = A.indptr[i]; e < A.indptr[i + 1]; ++e)
-          acc += (double)data[e] * dz[A.indices[e]];
+        const int e1 = indptr[i + 1];
+        for (int e = indptr[i]; e < e1; ++e) acc += (double)data[e] * dz[cols[e]];
         xt[i] = (T)(rhs[i] - acc);
       }
       __syncthreads();
@@ -613,8 +656,15 @@ struct Instance {
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const FusedLayout L = fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr);
+  const FusedLayout L =
+      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.bo.len);
+  {  // stage the 16-bit tables once per CTA
+    const uint4* src = reinterpret_cast<const uint4*>(A.blob);
+    uint4* dst = reinterpret_cast<uint4*>(smem + L.blob);
+    for (int i = threadIdx.x; i < A.bo.len / 8; i += NT) dst[i] = src[i];
+  }
   Instance<T, NT> I{A, 0};
+  I.tb = reinterpret_cast<const unsigned short*>(smem + L.blob);
   I.z = reinterpret_cast<double*>(smem + L.z);
   I.zp = reinterpret_cast<double*>(smem + L.zp);
   I.fp = reinterpret_cast<double*>(smem + L.fp);
@@ -680,13 +730,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_consta
 }
 
 static int fused_eligible(const Topo& t, int precision, size_t* smem_out) {
-  if (t.kmax > 32 || t.n_seg != 1) return VXG_ERR_TOO_LARGE;
+  if (t.kmax > 32 || t.n_seg != 1 || !t.d_blob) return VXG_ERR_TOO_LARGE;
   const int max_scr = (int)std::max(t.max_schur, t.max_bord);
   const size_t smem = precision == VXG_F32
                           ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
-                                                (int)t.n_jac_slots, (int)t.work, max_scr).total
+                                                (int)t.n_jac_slots, (int)t.work, max_scr,
+                                                t.blob.len).total
                           : fused_layout<double>(t.S, (int)t.nnz, (int)t.n_res_slots,
-                                                 (int)t.n_jac_slots, (int)t.work, max_scr).total;
+                                                 (int)t.n_jac_slots, (int)t.work, max_scr,
+                                                 t.blob.len).total;
   int dev = 0, max_optin = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -699,9 +751,20 @@ template <typename T, int NT>
 static int launch_fused(const FusedArgs& a, size_t smem, cudaStream_t s) {
   auto kern = fused_kernel<T, NT>;
   VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, per_sm = 0, smem_sm = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  // Carve out only the shared memory the resident CTAs need; the rest of the
+  // SM's unified L1/shared storage stays L1, where the topology tables (stamp
+  // gathers, plan and level tables) that every CTA walks every iteration live.
+  cudaFuncAttributes fa;
+  VXG_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+  const int by_regs = std::max(1, 65536 / std::max(1, fa.numRegs * NT));
+  const int resident = std::max(1, std::min(by_regs, (a.B + sms - 1) / sms));
+  const size_t need = (smem + 1024) * (size_t)resident;
+  const int pct = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / smem_sm);
+  VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
   VXG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
   const int grid = std::max(1, std::min(a.B, sms * std::max(per_sm, 1)));
   kern<<<grid, NT, smem, s>>>(a);
@@ -771,6 +834,8 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   a.bt_tgt = t.bt_tgt;
   a.bt_ptr = t.bt_ptr;
   a.bt_src = t.bt_src;
+  a.blob = t.d_blob;
+  a.bo = t.blob;
   a.B = batch;
   a.mode = mode;
   a.n_t = n_t;

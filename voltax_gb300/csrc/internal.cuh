@@ -28,6 +28,22 @@ struct GroupTable {
   GroupDev g[VXG_MAX_GROUPS];
 };
 
+// 16-bit copy of every table the fused kernel walks each Newton iteration,
+// staged into shared memory once per CTA. Section k starts at off[k]
+// (elements); node tables hold 0xFFFF for ground.
+enum BlobSection {
+  B_RES_PTR, B_RES_SRC, B_JAC_PTR, B_JAC_SRC, B_ROWS, B_INDICES, B_INDPTR, B_APOS,
+  B_SN_K, B_SN_R, B_SN_PANEL, B_SN_PIV_PTR, B_SN_PIV, B_SN_BORD_PTR, B_SN_BORD,
+  B_LV_PTR, B_LV_KMAX, B_LV_SN, B_LV_SCHUR_OFF, B_LV_BORD_OFF,
+  B_LV_ST_PTR, B_ST_TGT, B_ST_PTR, B_ST_SRC, B_LV_BT_PTR, B_BT_TGT, B_BT_PTR, B_BT_SRC,
+  B_NODES, B_COUNT
+};
+struct Blob {
+  int off[B_COUNT + 1];
+  int node_off[VXG_MAX_GROUPS];
+  int len;  // elements, a multiple of 8
+};
+
 // Device-resident copy of a topology + plan.
 struct Topo {
   int S, nv;
@@ -62,6 +78,9 @@ struct Topo {
   // pinned host word for loop control
   int* h_flag;
   int* d_flag;
+  // 16-bit tables of the fused kernel (null when some index does not fit)
+  unsigned short* d_blob;
+  Blob blob;
 };
 
 }  // namespace vxg

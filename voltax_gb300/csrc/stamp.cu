@@ -31,7 +31,9 @@ __global__ void eval_kernel(GroupTable gt, int B, const double* __restrict__ z, 
   while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
   const GroupDev& g = gt.g[gi];
   const int d = (int)(flat - g.dev_base);
-  eval_soa<double>(g, b, d, z + (long long)b * S, t, cf, cq, want_f, want_q, want_j,
+  double u[kMaxM];
+  gather_u(g, d, z + (long long)b * S, u);
+  eval_soa<double>(g, b, d, u, t, cf, cq, want_f, want_q, want_j,
                    cf_buf + (long long)b * n_res_slots + g.res_base,
                    cq_buf + (long long)b * n_res_slots + g.res_base,
                    cj_buf + (long long)b * n_jac_slots + g.jac_base);
