@@ -152,6 +152,8 @@ static void free_topo(Topo& t) {
   delete[] t.h_lv_rmax;
 }
 
+constexpr long long kLongSum = 32;
+
 // Build the 16-bit table blob of the fused kernel; false if a value does not fit.
 static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& out, Blob& b) {
   bool ok = true;
@@ -215,6 +217,18 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
       else out.push_back((unsigned short)v);
     }
   }
+  // rows / entries with more than kLongSum contributions: summed by a warp
+  std::vector<long long> lr, lj;
+  for (long long i = 0; i < S; ++i)
+    if (d->res_ptr[i + 1] - d->res_ptr[i] > kLongSum) lr.push_back(i);
+  for (long long e = 0; e < nnz; ++e)
+    if (d->jac_ptr[e + 1] - d->jac_ptr[e] > kLongSum) lj.push_back(e);
+  std::vector<long long> lrow;
+  for (long long i = 0; i < S; ++i)
+    if (d->indptr[i + 1] - d->indptr[i] > kLongSum) lrow.push_back(i);
+  push(B_LONG_RES, lr.data(), (long long)lr.size());
+  push(B_LONG_JAC, lj.data(), (long long)lj.size());
+  push(B_LONG_ROW, lrow.data(), (long long)lrow.size());
   b.off[B_COUNT] = (int)out.size();
   while (out.size() % 8) out.push_back(0);  // 16-byte granules for the copy
   b.len = (int)out.size();

@@ -376,11 +376,26 @@ struct Instance {
     }
   }
 
+  // Sum of vals[src[p]] over p in [p0, p1): one thread in order for short
+  // lists; lists longer than 32 are summed by a whole warp -- lane l adds
+  // p0 + l, p0 + l + 32, ... in order, then a fixed butterfly combines the
+  // lanes -- so a node with hundreds of contributions (a supply rail) is not
+  // one long serial chain. Both orders are fixed: bitwise reproducible.
+  template <typename V>
+  __device__ __forceinline__ V warp_list_sum(const V* vals, const u16* src, int p0, int p1) {
+    const int lane = threadIdx.x & 31;
+    V acc = V(0);
+    for (int p = p0 + lane; p < p1; p += 32) acc += vals[src[p]];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
+    return acc;
+  }
+
   __device__ void assemble_res(double* fo, double* qo) {
     const u16* ptr = sec(B_RES_PTR);
     const u16* src = sec(B_RES_SRC);
     for (int i = threadIdx.x; i < A.S; i += NT) {
       const int p0 = ptr[i], p1 = ptr[i + 1];
+      if (p1 - p0 > 32) continue;  // long rows: below
       if (fo) {
         double acc = 0.0;
         for (int p = p0; p < p1; ++p) acc += cf[src[p]];
@@ -390,6 +405,21 @@ struct Instance {
         double acc = 0.0;
         for (int p = p0; p < p1; ++p) acc += cq[src[p]];
         qo[i] = acc;
+      }
+    }
+    const u16* longs = sec(B_LONG_RES);
+    const int n_long = A.bo.off[B_LONG_RES + 1] - A.bo.off[B_LONG_RES];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int li = warp; li < n_long; li += NT / 32) {
+      const int i = longs[li];
+      const int p0 = ptr[i], p1 = ptr[i + 1];
+      if (fo) {
+        const double v = warp_list_sum<double>(cf, src, p0, p1);
+        if (lane == 0) fo[i] = v;
+      }
+      if (qo) {
+        const double v = warp_list_sum<double>(cq, src, p0, p1);
+        if (lane == 0) qo[i] = v;
       }
     }
   }
@@ -408,12 +438,25 @@ struct Instance {
     const u16* rows = sec(B_ROWS);
     const u16* cols = sec(B_INDICES);
     for (int e = threadIdx.x; e < A.nnz; e += NT) {
+      const int p0 = jptr[e], p1 = jptr[e + 1];
+      if (p1 - p0 > 32) continue;  // long entries: below
       T acc = T(0);
-      const int p1 = jptr[e + 1];
-      for (int p = jptr[e]; p < p1; ++p) acc += cj[jsrc[p]];
+      for (int p = p0; p < p1; ++p) acc += cj[jsrc[p]];
       const int r = rows[e];
       if (r < A.nv && cols[e] == r) acc += (T)gmin;
       data[e] = acc;
+    }
+    {
+      const u16* longs = sec(B_LONG_JAC);
+      const int n_long = A.bo.off[B_LONG_JAC + 1] - A.bo.off[B_LONG_JAC];
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int li = warp; li < n_long; li += NT / 32) {
+        const int e = longs[li];
+        T acc = warp_list_sum<T>(cj, jsrc, jptr[e], jptr[e + 1]);
+        const int r = rows[e];
+        if (r < A.nv && cols[e] == r) acc += (T)gmin;
+        if (lane == 0) data[e] = acc;
+      }
     }
     if (first && mode != VXG_MODE_DC)
       for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
@@ -592,12 +635,24 @@ struct Instance {
     __syncthreads();
     const u16* indptr = sec(B_INDPTR);
     const u16* cols = sec(B_INDICES);
+    const u16* longs = sec(B_LONG_ROW);
+    const int n_long = A.bo.off[B_LONG_ROW + 1] - A.bo.off[B_LONG_ROW];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int it = 0; it < refine; ++it) {
       for (int i = threadIdx.x; i < A.S; i += NT) {
+        const int e0 = indptr[i], e1 = indptr[i + 1];
+        if (e1 - e0 > 32) continue;  // long rows: a warp each, below
         double acc = 0.0;
-        const int e1 = indptr[i + 1];
-        for (int e = indptr[i]; e < e1; ++e) acc += (double)data[e] * dz[cols[e]];
+        for (int e = e0; e < e1; ++e) acc += (double)data[e] * dz[cols[e]];
         xt[i] = (T)(rhs[i] - acc);
+      }
+      for (int li = warp; li < n_long; li += NT / 32) {
+        const int i = longs[li];
+        double acc = 0.0;
+        for (int e = indptr[i] + lane; e < indptr[i + 1]; e += 32)
+          acc += (double)data[e] * dz[cols[e]];
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
+        if (lane == 0) xt[i] = (T)(rhs[i] - acc);
       }
       __syncthreads();
       solve_t();

@@ -110,3 +110,77 @@ def mirror_adder_mc(instances: int = 4096, seed: int = 0, bits: int = 4,
         new.log_l = el.log_l.expand(instances, n).clone()
         c = c.replace(name, new)
     return c
+
+
+# ----------------------------------------------------------------- OTA chain
+OTA_GROUPS = 21
+"""OTAs of the chain share their parameter shifts by position modulo this."""
+
+
+def ota_chain(stages: int = 66, vbias: float = 0.6, vin: float = 0.6):
+    """A chain of 5-transistor OTAs, each wired as a unity-gain follower of the
+    previous output (the 5T OTA of voltax/benchmarks/benchmark_ota.py:51-68,
+    with EKV devices): per stage the nodes d1 (mirror), out and tail, plus
+    the shared vdd, bias and input -> 3 * stages + 3 nodes (66 stages: 201).
+
+    Parameters enter through `ota_params`; the nominal circuit has VDD 1.2 V.
+    """
+    b = CircuitBuilder()
+    b.vsource("vdd", "0", VDD, name="Vdd")
+    b.vsource("bias", "0", vbias, name="Vbias")
+    b.vsource("in", "0", vin, name="Vin")
+    prev = "in"
+    for k in range(stages):
+        d1, out, tail = f"d1_{k}", f"out{k}", f"tail{k}"
+        b.nmos(d1, prev, tail, "0", w=2e-6, name=f"M1_{k}")
+        b.nmos(out, out, tail, "0", w=2e-6, name=f"M2_{k}")
+        b.pmos(d1, d1, "vdd", "vdd", w=4e-6, name=f"M3_{k}")
+        b.pmos(out, d1, "vdd", "vdd", w=4e-6, name=f"M4_{k}")
+        b.nmos(tail, "bias", "0", "0", w=2e-6, name=f"M5_{k}")
+        prev = out
+    return b.build()
+
+
+def ota_params(n: int, seed: int = 0) -> np.ndarray:
+    """``(n, 64)`` parameter vectors: VDD ~ U(0.9, 1.3) V, then per position
+    group g < 21: the input-pair Vth shift ~ N(0, 30 mV), the mirror log-W
+    shift ~ N(0, 0.05) and the tail Vth shift ~ N(0, 30 mV)."""
+    rng = np.random.default_rng(seed)
+    p = np.empty((n, 1 + 3 * OTA_GROUPS))
+    p[:, 0] = rng.uniform(0.9, 1.3, n)
+    shifts = rng.normal(0.0, 1.0, (n, OTA_GROUPS, 3)) * np.array([0.03, 0.05, 0.03])
+    p[:, 1:] = shifts.reshape(n, -1)
+    return p
+
+
+def apply_ota_params(circuit, params: np.ndarray):
+    """Batched copy of `ota_chain` with the parameter vectors applied."""
+    params = torch.as_tensor(params, dtype=torch.float64)
+    B = params.shape[0]
+    c = circuit
+    vdd = c.elements["VoltageSource"]
+    idx = c.layout.device("Vdd")[1]
+    val = vdd.value.value.expand(B, vdd.size).clone()
+    val[:, idx] = params[:, 0]
+    c = c.replace("VoltageSource", vdd.with_dc(val))
+    shifts = params[:, 1:].reshape(B, OTA_GROUPS, 3)
+    for gname in ("EKVMOSFET_n", "EKVMOSFET_p"):
+        el = c.elements[gname]
+        names = c.devices(gname)
+        dv = torch.zeros(B, el.size, dtype=torch.float64)
+        lw = el.log_w.expand(B, el.size).clone()
+        for i, name in enumerate(names):
+            role, k = name.split("_")
+            grp = int(k) % OTA_GROUPS
+            if role in ("M1", "M2"):
+                dv[:, i] = shifts[:, grp, 0]
+            elif role == "M5":
+                dv[:, i] = shifts[:, grp, 2]
+            else:  # M3, M4: the mirror
+                lw[:, i] = lw[:, i] + shifts[:, grp, 1]
+        new = el.with_nodes(el.nodes)
+        new.dvth = dv
+        new.log_w = lw
+        new.log_l = el.log_l.expand(B, el.size).clone()
+        c = c.replace(gname, new)
+    return c
