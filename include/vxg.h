@@ -271,6 +271,53 @@ int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
 int vxg_factor_static(const vxg_handle* h, int32_t batch, int32_t precision,
                       const double* data, void* factors, void* stream);
 
+/* ---- Learned Newton warm start ------------------------------------------
+ * No counterpart in the reference: voltax's DC Newton starts from the
+ * caller's guess or zeros (voltax/analysis.py:410-431). These are the
+ * kernels of an MLP that predicts a DC operating point from an instance's
+ * parameter vector; the analysis then runs the ordinary Newton from the
+ * prediction, and from the default guess where that fails. Layers are
+ * y = act(x W^T + b): W is [out, in] BF16, b FP32, activations BF16, every
+ * product accumulated in FP32. All buffers are the caller's; every kernel
+ * reduces in a fixed order (bitwise reproducible). */
+enum { VXG_ACT_NONE = 0, VXG_ACT_GELU = 1 /* exact erf form */ };
+
+/* x_bf16[m, k] = bf16((x[rows[m] * ldx + k] - mean[k]) * inv_std[k]) for
+ * m < M, k < K (rows NULL: identity). */
+int vxg_mlp_normalize(int64_t M, int32_t K, const double* x, int64_t ldx, const int64_t* rows,
+                      const float* mean, const float* inv_std, void* x_bf16, void* stream);
+
+/* Forward layer: v = x[M, K] W[N, K]^T + bias. Optional outputs: pre[M, N] = v
+ * (FP32, kept for the backward pass), y_bf16[M, N] = act(v), y_f32[M, N] =
+ * act(v), and z[m * ldz + n] = act(v) * scale[n] + shift[n] in FP64 (the
+ * de-normalised prediction written straight into a Newton state). */
+int vxg_mlp_linear(int64_t M, int32_t N, int32_t K, const void* x_bf16, const void* w_bf16,
+                   const float* bias, int32_t act, float* pre, void* y_bf16, float* y_f32,
+                   const float* scale, const float* shift, double* z, int64_t ldz,
+                   void* stream);
+
+/* Data gradient of a layer: dx[M, K] = (dy[M, N] W[N, K]) * gelu'(pre[M, K]),
+ * pre being the pre-activation of the layer's input (NULL: no activation). */
+int vxg_mlp_linear_dx(int64_t M, int32_t N, int32_t K, const void* dy_bf16, const void* w_bf16,
+                      const float* pre, void* dx_bf16, void* stream);
+
+/* Weight gradients of a layer: dw[N, K] = dy[M, N]^T x[M, K] (FP32,
+ * overwritten), db[N] = column sums of dy (NULL: skipped). */
+int vxg_mlp_linear_dw(int64_t M, int32_t N, int32_t K, const void* dy_bf16, const void* x_bf16,
+                      float* dw, float* db, void* stream);
+
+/* Mean squared error of y[M, N] against target rows (target[rows[m]], rows
+ * NULL: identity): *loss = sum (y - t)^2 / (M N), dy = 2 (y - t) / (M N) in
+ * BF16. scratch holds 256 floats. */
+int vxg_mlp_mse(int64_t M, int32_t N, const float* y, const float* target, const int64_t* rows,
+                void* dy_bf16, float* loss, float* scratch, void* stream);
+
+/* Adam step `step` (>= 1) on n FP32 master weights, with bias correction;
+ * w_bf16 (if not NULL) receives the rounded weights. step == 0 only
+ * rewrites w_bf16 from w. */
+int vxg_mlp_adam(int64_t n, float* w, void* w_bf16, const float* grad, float* m, float* v,
+                 float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+
 /* Kernels this library has launched since it was loaded (a diagnostic
  * counter; no counterpart in the reference). */
 uint64_t vxg_launch_count(void);

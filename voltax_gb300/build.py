@@ -18,7 +18,7 @@ OUT = HERE / "_lib"
 INCLUDE = HERE.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["stamp.cu", "factor.cu", "solve.cu", "newton.cu", "capi.cu", "fused.cu",
-           "factor_static.cu"]
+           "factor_static.cu", "mlp.cu"]
 
 
 def nvcc() -> str:
