@@ -56,6 +56,9 @@ class Workload:
             return wl.ring_oscillator(101)[0]
         if self.name == "grid100":
             return wl.power_grid(100, seed=seed)
+        if self.name == "ota_warm":
+            return wl.apply_ota_params(wl.ota_chain(OTA_STAGES),
+                                       wl.ota_params(instances, seed=OTA_TEST_SEED + seed))
         raise ValueError(self.name)
 
     def ic(self, circuit):
@@ -75,6 +78,8 @@ class Workload:
             return f"mirror_adder_mc{instances}"
         if self.name == "ring101":
             return f"ring_oscillator101_trap{n_t}"
+        if self.name == "ota_warm":
+            return f"ota_chain{OTA_STAGES}_dc_warm_start{instances}"
         return "power_grid100_dc"
 
 
@@ -83,7 +88,11 @@ WORKLOADS = {
                          ["s0", "s1", "s2", "s3", "co"], INSTANCES),
     "ring101": Workload("ring101", "transient", "trap", 2e-9, 2001, ["n0", "n50", "n100"], 1),
     "grid100": Workload("grid100", "dc", None, 0.0, 1, None, 1),
+    "ota_warm": Workload("ota_warm", "dc", None, 0.0, 1, None, 10000),
 }
+# learned warm start: 66-stage OTA chain (201 nodes), 200k training
+# operating points (parameter seed 1), 10k held-out instances (seed 2)
+OTA_STAGES, OTA_TRAIN, OTA_TRAIN_SEED, OTA_TEST_SEED = 66, 200_000, 1, 2
 
 
 def parse():
@@ -97,6 +106,8 @@ def parse():
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
+    ap.add_argument("--epochs", type=int, default=40, help="ota_warm: training epochs")
     a = ap.parse_args()
     w = WORKLOADS[a.workload]
     if a.instances is None:
@@ -231,6 +242,29 @@ def run_reference(a):
     print(json.dumps(line))
 
 
+def to_device(c, device, pin=False):
+    """The circuit with every parameter tensor on `device` (or pinned host)."""
+    out = c
+    for name in sorted(c.elements):
+        el = c.elements[name]
+        new = el.with_nodes(el.nodes)
+        for f in el.fields:
+            t = getattr(el, f)
+            setattr(new, f, t.pin_memory() if pin else t.to(device))
+        if hasattr(el, "value"):
+            new.value = el.value.map(lambda t: t.pin_memory() if pin else t.to(device))
+        if hasattr(el, "process"):
+            new.process = el.process
+        out = out.replace(name, new)
+    return out
+
+
+def h2d_bytes(c):
+    return sum(t.numel() * 8 for el in c.elements.values()
+               for t in ([getattr(el, f) for f in el.fields] +
+                         (el.value.params() if hasattr(el, "value") else [])))
+
+
 # ----------------------------------------------------------------- GPU arm
 def main():
     a = parse()
@@ -242,6 +276,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     w = WORKLOADS[a.workload]
     cpu = cpu_baseline(w, a.time_points, a.instances) if rank == 0 and not a.no_cpu else None
+    if w.name == "ota_warm":
+        main_warm(a, w, cpu)
+        return
 
     import torch
     import voltax_gb300 as vx
@@ -262,21 +299,6 @@ def main():
     ic = w.ic(circuit)
     out_nodes = ([circuit.node(n) for n in w.outputs] if w.outputs
                  else list(range(circuit.n_nodes)))
-
-    def to_device(c, device, pin=False):
-        out = c
-        for name in sorted(c.elements):
-            el = c.elements[name]
-            new = el.with_nodes(el.nodes)
-            for f in el.fields:
-                t = getattr(el, f)
-                setattr(new, f, t.pin_memory() if pin else t.to(device))
-            if hasattr(el, "value"):
-                new.value = el.value.map(lambda t: t.pin_memory() if pin else t.to(device))
-            if hasattr(el, "process"):
-                new.process = el.process
-            out = out.replace(name, new)
-        return out
 
     dev_circuit = to_device(circuit, dev)
     host_circuit = to_device(circuit, None, pin=True)
@@ -365,9 +387,7 @@ def main():
 
     # end to end through the public API: params from pinned host memory, output
     # node waveforms back to pinned host memory
-    h2d = sum(t.numel() * 8 for el in host_circuit.elements.values()
-              for t in ([getattr(el, f) for f in el.fields] +
-                        (el.value.params() if hasattr(el, "value") else [])))
+    h2d = h2d_bytes(host_circuit)
     out_host = torch.empty(tuple(s32.z[..., out_nodes].shape), dtype=torch.float64,
                            pin_memory=True)
 
@@ -400,6 +420,135 @@ def main():
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "roofline": roofline,
+    }
+    print(json.dumps(line))
+
+
+# --------------------------------------------------- learned warm start arm
+def main_warm(a, w, cpu):
+    """DC operating points of held-out OTA-chain instances from the MLP's
+    predicted guess (inference + Newton + fallback, one step) against Newton
+    from the default guess. The network is trained first (untimed) on
+    operating points the plain FP64 solver produces for other parameters."""
+    import torch
+    import voltax_gb300 as vx
+    from voltax_gb300 import _lib, warmstart, workloads
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    n_train = a.train or OTA_TRAIN
+    base = workloads.ota_chain(OTA_STAGES)
+
+    def make(P):
+        return workloads.apply_ota_params(base, P)
+
+    plain = vx.Options(precision="f64")
+    chosen = vx.Options(precision="f32")
+    # training data by the plain solver (default guess, gmin stepping)
+    Xtr = workloads.ota_params(n_train, seed=OTA_TRAIN_SEED + 1000 * rank)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Vtr, conv_tr, it_tr = warmstart.solve_dataset(make, Xtr, chunk=25000, options=plain)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    keep = conv_tr.cpu().numpy()
+    model = warmstart.WarmStartMLP(Xtr.shape[1], Vtr.shape[1], hidden=512, seed=0)
+    t0 = time.perf_counter()
+    hist = model.fit(Xtr[keep], Vtr[torch.as_tensor(keep, device=Vtr.device)],
+                     epochs=a.epochs, batch=1024, lr=2e-3, lr_final=2e-5)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+
+    X = workloads.ota_params(a.instances, seed=OTA_TEST_SEED + rank)
+    c_host = make(X)
+    c = to_device(c_host, dev)  # parameters resident in HBM for `value`
+    Xd = torch.as_tensor(X, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, k):
+        ms = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.sum(ms)) / 1e3
+
+    warm = lambda: warmstart.dc(c, Xd, model, options=chosen)  # noqa: E731
+    cold = lambda: vx.dc(c, options=chosen)  # noqa: E731
+    cold64 = lambda: vx.dc(c, options=plain)  # noqa: E731
+    for _ in range(a.warmup):
+        warm()
+    n0 = lib.vxg_launch_count()
+    with Clocks(local) as clk:
+        t_warm = timed(warm, a.steps)
+    launches = (lib.vxg_launch_count() - n0) // a.steps
+    cold()
+    t_cold = timed(cold, max(1, min(a.steps, 2)))
+    cold64()
+    t_cold64 = timed(cold64, max(1, min(a.steps, 2)))
+    B = a.instances
+    value = B * a.steps / t_warm
+    s_warm, s_cold, s_ref = warm(), cold(), cold64()
+    nv = c.layout.n_nodes
+    ref_v = s_ref.z[:, :nv]
+    scale = ref_v.abs().amax(1, keepdim=True)
+    rel = float(((s_warm.z[:, :nv] - ref_v).abs() / scale).max())
+    it_w = s_warm.iterations.double()
+    it_c = s_cold.iterations.double()
+
+    # end to end: parameters and the MLP inputs from pinned host memory, node
+    # voltages back to pinned host memory
+    host_c = to_device(c_host, None, pin=True)
+    Xh = torch.as_tensor(X).pin_memory()
+    out = torch.empty((B, nv), dtype=torch.float64, pin_memory=True)
+    h2d = Xh.numel() * 8 + h2d_bytes(host_c)
+
+    def e2e():
+        s = warmstart.dc(host_c, Xh.to(dev, non_blocking=True), model, options=chosen)
+        out.copy_(s.z[:, :nv], non_blocking=True)
+
+    e2e()
+    t_e2e = timed(e2e, a.steps)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * t_warm / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 LU + f64 residual/refinement; MLP bf16 x bf16 -> f32",
+        "data": "synthetic",
+        "config": {"workload": w.label(B, 1), "instances": B, "stages": OTA_STAGES,
+                   "nodes": nv, "train_instances": n_train, "epochs": a.epochs,
+                   "mlp": f"{Xtr.shape[1]}-512-512-{Vtr.shape[1]} GELU",
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "default_guess": {"value": B / (t_cold / max(1, min(a.steps, 2))),
+                          "unit": UNIT, "mean_newton_iters": float(it_c.mean()),
+                          "max_newton_iters": int(it_c.max())},
+        "plain_fp64_default_guess": {"value": B / (t_cold64 / max(1, min(a.steps, 2))),
+                                     "unit": UNIT},
+        "warm_start": {"mean_newton_iters": float(it_w.mean()),
+                       "max_newton_iters": int(it_w.max()),
+                       "iteration_reduction": float(it_c.mean() / it_w.mean()),
+                       "fallbacks": int((s_warm.iterations > chosen.direct_steps).sum()),
+                       "converged": bool(s_warm.converged.all())},
+        "match": {"max_rel_node_v_diff_vs_plain_fp64_default": rel},
+        "training": {"data_gen_s": gen_s, "data_gen_solves_per_s": n_train / gen_s,
+                     "data_mean_newton_iters": float(it_tr.double().mean()),
+                     "train_s": train_s, "loss_first_epoch": hist[0],
+                     "loss_last_epoch": hist[-1]},
+        "e2e": {"value": B * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(out.numel() * 8)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
     }
     print(json.dumps(line))
 

@@ -188,11 +188,14 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
   push(B_SN_BORD_PTR, d->sn_bord_ptr, nsn + 1);
   push(B_SN_BORD, d->sn_bord, d->sn_bord_ptr[nsn]);
   push(B_LV_PTR, d->lv_ptr, nl + 1);
-  std::vector<int> kmax(nl, 0);
+  std::vector<int> kmax(nl, 0), rmax(nl, 0);
   for (long long L = 0; L < nl; ++L)
-    for (long long q = d->lv_ptr[L]; q < d->lv_ptr[L + 1]; ++q)
+    for (long long q = d->lv_ptr[L]; q < d->lv_ptr[L + 1]; ++q) {
       kmax[L] = std::max(kmax[L], d->sn_k[d->lv_sn[q]]);
+      rmax[L] = std::max(rmax[L], d->sn_r[d->lv_sn[q]]);
+    }
   push(B_LV_KMAX, kmax.data(), nl);
+  push(B_LV_RMAX, rmax.data(), nl);
   push(B_LV_SN, d->lv_sn, d->lv_ptr[nl]);
   push(B_LV_SCHUR_OFF, d->lv_schur_off, d->lv_ptr[nl]);
   push(B_LV_BORD_OFF, d->lv_bord_off, d->lv_ptr[nl]);

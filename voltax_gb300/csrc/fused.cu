@@ -348,6 +348,20 @@ struct Instance {
 
   __device__ __forceinline__ const u16* sec(int k) const { return tb + A.bo.off[k]; }
 
+  // How a level's supernodes are factored and solved: one thread each
+  // (many tiny supernodes with short borders), one warp each (several
+  // supernodes), or the whole CTA (a lone supernode, or a few with wide
+  // borders whose Schur blocks need more than a warp).
+  enum { LV_TINY = 0, LV_WARP = 1, LV_CTA = 2 };
+  __device__ __forceinline__ int level_mode(int L) const {
+    const u16* lv_ptr = sec(B_LV_PTR);
+    const int n = lv_ptr[L + 1] - lv_ptr[L];
+    const int kmax = sec(B_LV_KMAX)[L], rmax = sec(B_LV_RMAX)[L];
+    if (kmax <= kTiny && n >= NT / 32 && rmax <= 8) return LV_TINY;
+    if (n >= 2 && (2 * n >= NT / 32 || rmax <= 16)) return LV_WARP;
+    return LV_CTA;
+  }
+
   // devices -> contribution slots (structure of arrays per group)
   __device__ void eval(const double* zz, double t, double cfc, double cqc, bool wf, bool wq,
                        bool wj) {
@@ -483,24 +497,25 @@ struct Instance {
     T* colb = sbuf + warp * 64;
     T* rowb = colb + 32;
     int* perm = ibuf + warp * 32;
-    const u16 *lv_ptr = sec(B_LV_PTR), *lv_kmax = sec(B_LV_KMAX), *lv_sn = sec(B_LV_SN);
+    const u16 *lv_ptr = sec(B_LV_PTR), *lv_sn = sec(B_LV_SN);
     const u16 *sch_off = sec(B_LV_SCHUR_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
     const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR), *st_tgt = sec(B_ST_TGT);
     const u16 *st_ptr = sec(B_ST_PTR), *st_src = sec(B_ST_SRC);
     for (int L = 0; L < A.n_levels; ++L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
-      if (lv_kmax[L] <= kTiny) {  // tiny supernodes: one thread each
+      const int mode = level_mode(L);
+      if (mode == LV_TINY) {
         for (int p = lo + threadIdx.x; p < hi; p += NT) {
           const int j = lv_sn[p];
           tiny_factor<T>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p]);
         }
-      } else if (hi - lo >= NW) {  // wide level: one warp per supernode
+      } else if (mode == LV_WARP) {
         for (int p = lo + warp; p < hi; p += NW) {
           const int j = lv_sn[p];
           sn_factor<T, false, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], colb,
                                   rowb, perm);
         }
-      } else {  // narrow level: the whole CTA on each supernode
+      } else {
         for (int p = lo; p < hi; ++p) {
           const int j = lv_sn[p];
           sn_factor<T, true, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], sbuf,
@@ -521,7 +536,7 @@ struct Instance {
   // in-place solve of xt
   __device__ void solve_t() {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const u16 *lv_ptr = sec(B_LV_PTR), *lv_kmax = sec(B_LV_KMAX), *lv_sn = sec(B_LV_SN);
+    const u16 *lv_ptr = sec(B_LV_PTR), *lv_sn = sec(B_LV_SN);
     const u16 *bord_off = sec(B_LV_BORD_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
     const u16 *sn_panel = sec(B_SN_PANEL), *piv_ptr = sec(B_SN_PIV_PTR), *pivs = sec(B_SN_PIV);
     const u16 *bord_ptr = sec(B_SN_BORD_PTR), *bords = sec(B_SN_BORD);
@@ -529,7 +544,7 @@ struct Instance {
     const u16* bt_src = sec(B_BT_SRC);
     for (int L = 0; L < A.n_levels; ++L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
-      if (lv_kmax[L] <= kTiny) {
+      if (level_mode(L) == LV_TINY) {
         for (int p = lo + threadIdx.x; p < hi; p += NT) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
@@ -594,7 +609,7 @@ struct Instance {
     }
     for (int L = A.n_levels - 1; L >= 0; --L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
-      if (lv_kmax[L] <= kTiny) {
+      if (level_mode(L) == LV_TINY) {
         for (int p = lo + threadIdx.x; p < hi; p += NT) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
