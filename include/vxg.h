@@ -238,7 +238,7 @@ int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
 
 /* Shared memory one instance needs in the fused persistent kernel
  * (vxg_fused_run); VXG_ERR_TOO_LARGE when the topology is not eligible
- * (a supernode wider than 32, several segments, or more shared memory than
+ * (a supernode wider than 128, several segments, or more shared memory than
  * one CTA may have). */
 int vxg_fused_smem(const vxg_handle* h, int32_t precision, size_t* bytes);
 

@@ -317,3 +317,24 @@ def test_ekv_transient_gradient_matches_finite_differences(method, engine):
     dn[k] -= eps
     fd = (float(loss(up)) - float(loss(dn))) / (2 * eps)
     assert np.isclose(g[k], fd, rtol=1e-5, atol=1e-9)
+
+
+def test_fused_wide_supernode_ota_chain_matches_generic_and_oracle():
+    """66-stage OTA chain: its root supernode is 66 wide, so the fused
+    kernel factors and solves it with the whole CTA (k > 32 path)."""
+    base = workloads.ota_chain(66)
+    P = workloads.ota_params(16, seed=5)
+    c = workloads.apply_ota_params(base, P)
+    st = symbolic.structure(c)
+    assert max(st.plan.k) == 66
+    fused = vx.dc(c, options=vx.Options(engine="fused", precision="f32"))
+    gen = vx.dc(c, options=vx.Options(engine="generic"))
+    assert bool(fused.converged.all()) and bool(gen.converged.all())
+    nv = c.layout.n_nodes
+    scale = gen.z[:, :nv].abs().amax(1, keepdim=True)
+    assert float(((fused.z[:, :nv] - gen.z[:, :nv]).abs() / scale).max()) <= 1e-9
+    for b in (0, 7):
+        zr, okr, itr = oa.dc(oa.System(c, st, st.plan, b))
+        assert okr
+        assert rel(fused.z[b, :nv].cpu().numpy(), zr[:nv]) <= 1e-9
+        assert int(gen.iterations[b]) == itr

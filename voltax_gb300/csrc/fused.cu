@@ -10,11 +10,13 @@
 // Nothing but parameters, time points and the output states touches global
 // memory; the topology tables are read through L1.
 //
-// Supernodes are factored one per warp (k <= 32: Gauss-Jordan with partial
-// pivoting on registers and shared memory), the supernodes of one level in
-// parallel across warps; Schur and border updates of a level are applied by
-// a second pass with one thread per target slot summing its sources in a
-// fixed order, so results are bitwise reproducible.
+// Each level's supernodes are factored one per thread (many tiny ones),
+// one per warp (several, k <= 32) or by the whole CTA (a lone supernode, or
+// any with k > 32, up to 128): Gauss-Jordan with partial pivoting in shared
+// memory, then Ub, the Schur block and Lb. Schur and border updates of a
+// level are applied by a second pass with one thread per target slot
+// summing its sources in a fixed order, so results are bitwise
+// reproducible.
 
 #include <algorithm>
 #include <cstring>
@@ -24,6 +26,7 @@
 namespace vxg {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kCtaK = 128;  // widest supernode the whole-CTA factorization takes
 
 struct FusedArgs {
   GroupTable gt;
@@ -90,7 +93,10 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
   L.xt = take(sizeof(T) * S);
   L.red = take(64 * sizeof(double));
-  L.sbuf = take(sizeof(T) * 2 * 32 * 8 + sizeof(int) * 32 * 8);  // per-warp col/row/perm
+  // per-warp column/row buffers and pivot records (8 warps); the whole-CTA
+  // factorization uses 2 * kCtaK of the values and kCtaK of the records
+  static_assert(2 * kCtaK <= 2 * 32 * 8 && kCtaK <= 32 * 8, "sbuf too small");
+  L.sbuf = take(sizeof(T) * 2 * 32 * 8 + sizeof(int) * 32 * 8);
   L.total = o;
   return L;
 }
@@ -140,11 +146,13 @@ __device__ int block_all(int ok, double* red) {
 
 // ------------------------------------------------------- supernode LDU
 // One supernode's block LDU by a group of threads: one warp (CTA = false,
-// the supernodes of a wide level in parallel) or the whole CTA (CTA = true,
-// the single supernodes of the top levels). k <= 32.
+// the supernodes of a wide level in parallel, k <= 32) or the whole CTA
+// (CTA = true, the lone supernodes of the top levels, k <= kCtaK).
 //   W  = F11^-1 by Gauss-Jordan with partial pivoting (row swaps recorded,
-//        undone as column swaps), two group barriers per pivot step;
-//   Ub = W F12 in place (one column per warp, shuffles across the column);
+//        undone as column swaps), two group barriers per pivot step; lane l
+//        owns columns l, l + 32, ...;
+//   Ub = W F12 in place (one column per warp, the column held in registers
+//        and broadcast by shuffles);
 //   S  = F21 Ub into Sout;  Lb = F21 W in place (one row per warp).
 template <bool CTA, int NT>
 __device__ __forceinline__ void group_sync() {
@@ -156,7 +164,8 @@ __device__ __forceinline__ void group_sync() {
 
 template <typename T, bool CTA, int NT>
 __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* perm) {
-  constexpr int GW = CTA ? NT / 32 : 1;  // warps in the group
+  constexpr int GW = CTA ? NT / 32 : 1;      // warps in the group
+  constexpr int KQ = CTA ? kCtaK / 32 : 1;   // columns per lane
   const int lane = threadIdx.x & 31;
   const int gw = CTA ? (threadIdx.x >> 5) : 0;  // warp index inside the group
   T* A = P;
@@ -164,8 +173,20 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
   T* F21 = F12 + k * r;
   for (int c = 0; c < k; ++c) {
     if (gw == 0) {
-      T v = (lane >= c && lane < k) ? tabs_(A[lane * k + c]) : T(-1);
-      int bi = lane;
+      // pivot: largest |A[i][c]| over i >= c, ties to the lower row
+      T v = T(-1);
+      int bi = k;
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const int i = lane + 32 * q;
+        if (i >= c && i < k) {
+          const T a = tabs_(A[i * k + c]);
+          if (a > v) {
+            v = a;
+            bi = i;
+          }
+        }
+      }
       for (int off = 16; off > 0; off >>= 1) {
         const T ov = __shfl_down_sync(kFull, v, off);
         const int oi = __shfl_down_sync(kFull, bi, off);
@@ -177,29 +198,42 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
       int p = __shfl_sync(kFull, bi, 0);
       if (p < c || p >= k) p = c;
       if (lane == 0) perm[c] = p;
-      if (p != c && lane < k) {
-        const T tmp = A[p * k + lane];
-        A[p * k + lane] = A[c * k + lane];
-        A[c * k + lane] = tmp;
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const int j = lane + 32 * q;
+        if (p != c && j < k) {
+          const T tmp = A[p * k + j];
+          A[p * k + j] = A[c * k + j];
+          A[c * k + j] = tmp;
+        }
       }
       __syncwarp();
-      if (lane < k) {
-        rowb[lane] = A[c * k + lane];
-        colb[lane] = (lane == c) ? T(0) : A[lane * k + c];
+      const T d = A[c * k + c];
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const int j = lane + 32 * q;
+        if (j < k) {
+          rowb[j] = ((j == c) ? T(1) : A[c * k + j]) / d;
+          colb[j] = (j == c) ? T(0) : A[j * k + c];
+        }
       }
     }
     group_sync<CTA, NT>();
-    const T d = rowb[c];
-    const T rc = lane < k ? ((lane == c) ? T(1) : rowb[lane]) / d : T(0);
-    if (lane < k)
-      for (int i = gw; i < k; i += GW) {
-        if (i == c) {
-          A[c * k + lane] = rc;
-        } else {
-          const T a = (lane == c) ? T(0) : A[i * k + lane];
-          A[i * k + lane] = a - colb[i] * rc;
+    for (int i = gw; i < k; i += GW) {
+      const T ci = colb[i];
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const int j = lane + 32 * q;
+        if (j < k) {
+          if (i == c) {
+            A[c * k + j] = rowb[j];
+          } else {
+            const T a = (j == c) ? T(0) : A[i * k + j];
+            A[i * k + j] = a - ci * rowb[j];
+          }
         }
       }
+    }
     group_sync<CTA, NT>();
   }
   // undo the row swaps as column swaps; one thread per row
@@ -214,15 +248,33 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
     }
   group_sync<CTA, NT>();
   if (r == 0) return;
-  // Ub = W F12: warp-strided columns, lane l holds F12[l][col]
+  // Ub = W F12: warp-strided columns; lane l holds F12[l + 32q][col]
   for (int col = gw; col < r; col += GW) {
-    const T v = lane < k ? F12[lane * r + col] : T(0);
-    T acc = T(0);
-    for (int l = 0; l < k; ++l) {
-      const T x = __shfl_sync(kFull, v, l);
-      if (lane < k) acc += A[lane * k + l] * x;
+    T v[KQ], acc[KQ];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int i = lane + 32 * q;
+      v[q] = i < k ? F12[i * r + col] : T(0);
+      acc[q] = T(0);
     }
-    if (lane < k) F12[lane * r + col] = acc;
+#pragma unroll
+    for (int qs = 0; qs < KQ; ++qs) {
+      const int l1 = min(32, k - 32 * qs);
+      for (int ll = 0; ll < l1; ++ll) {
+        const int l = 32 * qs + ll;
+        const T x = __shfl_sync(kFull, v[qs], ll);
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) {
+          const int i = lane + 32 * q;
+          if (i < k) acc[q] += A[i * k + l] * x;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int i = lane + 32 * q;
+      if (i < k) F12[i * r + col] = acc[q];
+    }
   }
   group_sync<CTA, NT>();
   // S = F21 Ub
@@ -235,11 +287,20 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
   group_sync<CTA, NT>();
   // Lb = F21 W, one row per warp
   for (int a = gw; a < r; a += GW) {
-    T acc = T(0);
-    if (lane < k)
-      for (int l = 0; l < k; ++l) acc += F21[a * k + l] * A[l * k + lane];
+    T acc[KQ];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int j = lane + 32 * q;
+      acc[q] = T(0);
+      if (j < k)
+        for (int l = 0; l < k; ++l) acc[q] += F21[a * k + l] * A[l * k + j];
+    }
     __syncwarp();
-    if (lane < k) F21[a * k + lane] = acc;
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int j = lane + 32 * q;
+      if (j < k) F21[a * k + j] = acc[q];
+    }
     __syncwarp();
   }
   group_sync<CTA, NT>();
@@ -357,6 +418,7 @@ struct Instance {
     const u16* lv_ptr = sec(B_LV_PTR);
     const int n = lv_ptr[L + 1] - lv_ptr[L];
     const int kmax = sec(B_LV_KMAX)[L], rmax = sec(B_LV_RMAX)[L];
+    if (kmax > 32) return LV_CTA;
     if (kmax <= kTiny && n >= NT / 32 && rmax <= 8) return LV_TINY;
     if (n >= 2 && (2 * n >= NT / 32 || rmax <= 16)) return LV_WARP;
     return LV_CTA;
@@ -519,7 +581,7 @@ struct Instance {
         for (int p = lo; p < hi; ++p) {
           const int j = lv_sn[p];
           sn_factor<T, true, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], sbuf,
-                                 sbuf + 32, ibuf);
+                                 sbuf + kCtaK, ibuf);
         }
       }
       __syncthreads();
@@ -572,6 +634,29 @@ struct Instance {
             xt[piv[i]] = acc;
           }
         }
+      } else if (sec(B_LV_KMAX)[L] > 32) {  // wide supernodes: the whole CTA on each
+        for (int p = lo; p < hi; ++p) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          const T* W = work + sn_panel[j];
+          const T* Lb = W + k * k + k * r;
+          const u16* piv = pivs + piv_ptr[j];
+          T* cb = scr + bord_off[p];
+          T* y = sbuf;
+          for (int l = threadIdx.x; l < k; l += NT) y[l] = xt[piv[l]];
+          __syncthreads();
+          for (int i = threadIdx.x; i < k + r; i += NT) {
+            T acc = T(0);
+            if (i < k) {
+              for (int l = 0; l < k; ++l) acc += W[i * k + l] * y[l];
+              xt[piv[i]] = acc;
+            } else {
+              for (int l = 0; l < k; ++l) acc += Lb[(i - k) * k + l] * y[l];
+              cb[i - k] = acc;
+            }
+          }
+          __syncthreads();
+        }
       } else {
         for (int p = lo + warp; p < hi; p += NT / 32) {
           const int j = lv_sn[p];
@@ -617,6 +702,20 @@ struct Instance {
           const u16* piv = pivs + piv_ptr[j];
           const u16* brd = bords + bord_ptr[j];
           for (int i = 0; i < k; ++i) {
+            T acc = T(0);
+            for (int a = 0; a < r; ++a) acc += Ub[i * r + a] * xt[brd[a]];
+            xt[piv[i]] -= acc;
+          }
+        }
+      } else if (sec(B_LV_KMAX)[L] > 32) {
+        for (int p = lo; p < hi; ++p) {
+          const int j = lv_sn[p];
+          const int k = sn_k[j], r = sn_r[j];
+          if (r == 0) continue;
+          const T* Ub = work + sn_panel[j] + k * k;
+          const u16* piv = pivs + piv_ptr[j];
+          const u16* brd = bords + bord_ptr[j];
+          for (int i = threadIdx.x; i < k; i += NT) {
             T acc = T(0);
             for (int a = 0; a < r; ++a) acc += Ub[i * r + a] * xt[brd[a]];
             xt[piv[i]] -= acc;
@@ -800,7 +899,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_consta
 }
 
 static int fused_eligible(const Topo& t, int precision, size_t* smem_out) {
-  if (t.kmax > 32 || t.n_seg != 1 || !t.d_blob) return VXG_ERR_TOO_LARGE;
+  if (t.kmax > kCtaK || t.n_seg != 1 || !t.d_blob) return VXG_ERR_TOO_LARGE;
   const int max_scr = (int)std::max(t.max_schur, t.max_bord);
   const size_t smem = precision == VXG_F32
                           ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
