@@ -201,9 +201,6 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
   push(B_LV_BORD_OFF, d->lv_bord_off, d->lv_ptr[nl]);
   const long long nst = d->lv_st_ptr[nl], nbt = d->lv_bt_ptr[nl];
   push(B_LV_ST_PTR, d->lv_st_ptr, nl + 1);
-  push(B_ST_TGT, d->st_tgt, nst);
-  push(B_ST_PTR, d->st_ptr, nst + 1);
-  push(B_ST_SRC, d->st_src, d->st_ptr[nst]);
   push(B_LV_BT_PTR, d->lv_bt_ptr, nl + 1);
   push(B_BT_TGT, d->bt_tgt, nbt);
   push(B_BT_PTR, d->bt_ptr, nbt + 1);
@@ -232,6 +229,9 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
   push(B_LONG_RES, lr.data(), (long long)lr.size());
   push(B_LONG_JAC, lj.data(), (long long)lj.size());
   push(B_LONG_ROW, lrow.data(), (long long)lrow.size());
+  push(B_ST_TGT, d->st_tgt, nst);
+  push(B_ST_PTR, d->st_ptr, nst + 1);
+  push(B_ST_SRC, d->st_src, d->st_ptr[nst]);
   b.off[B_COUNT] = (int)out.size();
   while (out.size() % 8) out.push_back(0);  // 16-byte granules for the copy
   b.len = (int)out.size();

@@ -45,6 +45,8 @@ struct FusedArgs {
   const long long *bt_ptr, *bt_src;
   const unsigned short* blob;  // 16-bit tables (global), staged into shared memory
   Blob bo;
+  int first_global;  // sections from this one on stay in global memory
+  int staged;        // table elements copied to shared memory (a multiple of 8)
   int B, mode, n_t, max_steps, refine, dc_first, gmin_steps, direct_steps;
   double rtol, atol, max_dv, gmin;
   const double* ts;
@@ -407,7 +409,9 @@ struct Instance {
   int* ibuf;
   const u16* tb;  // shared-memory tables
 
-  __device__ __forceinline__ const u16* sec(int k) const { return tb + A.bo.off[k]; }
+  __device__ __forceinline__ const u16* sec(int k) const {
+    return (k < A.first_global ? tb : A.blob) + A.bo.off[k];
+  }
 
   // How a level's supernodes are factored and solved: one thread each
   // (many tiny supernodes with short borders), one warp each (several
@@ -826,11 +830,11 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L =
-      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.bo.len);
+      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged);
   {  // stage the 16-bit tables once per CTA
     const uint4* src = reinterpret_cast<const uint4*>(A.blob);
     uint4* dst = reinterpret_cast<uint4*>(smem + L.blob);
-    for (int i = threadIdx.x; i < A.bo.len / 8; i += NT) dst[i] = src[i];
+    for (int i = threadIdx.x; i < A.staged / 8; i += NT) dst[i] = src[i];
   }
   Instance<T, NT> I{A, 0};
   I.tb = reinterpret_cast<const unsigned short*>(smem + L.blob);
@@ -898,22 +902,35 @@ __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_consta
   }
 }
 
-static int fused_eligible(const Topo& t, int precision, size_t* smem_out) {
+// Shared memory one instance needs with the first `staged` table elements on
+// chip. All tables are staged when they fit; otherwise the Schur gather
+// tables (the largest, read once per level) stay in global memory.
+static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
+                          int* first_global = nullptr, int* staged_out = nullptr) {
   if (t.kmax > kCtaK || t.n_seg != 1 || !t.d_blob) return VXG_ERR_TOO_LARGE;
   const int max_scr = (int)std::max(t.max_schur, t.max_bord);
-  const size_t smem = precision == VXG_F32
-                          ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
-                                                (int)t.n_jac_slots, (int)t.work, max_scr,
-                                                t.blob.len).total
-                          : fused_layout<double>(t.S, (int)t.nnz, (int)t.n_res_slots,
-                                                 (int)t.n_jac_slots, (int)t.work, max_scr,
-                                                 t.blob.len).total;
   int dev = 0, max_optin = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  *smem_out = smem;
-  if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
-  return VXG_OK;
+  const int options[2][2] = {{B_COUNT, t.blob.len},
+                             {B_ST_TGT, (t.blob.off[B_ST_TGT] + 7) / 8 * 8}};
+  for (int o = 0; o < 2; ++o) {
+    const int staged = options[o][1];
+    const size_t smem = precision == VXG_F32
+                            ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
+                                                  (int)t.n_jac_slots, (int)t.work, max_scr,
+                                                  staged).total
+                            : fused_layout<double>(t.S, (int)t.nnz, (int)t.n_res_slots,
+                                                   (int)t.n_jac_slots, (int)t.work, max_scr,
+                                                   staged).total;
+    *smem_out = smem;
+    if (smem <= (size_t)max_optin) {
+      if (first_global) *first_global = options[o][0];
+      if (staged_out) *staged_out = staged;
+      return VXG_OK;
+    }
+  }
+  return VXG_ERR_TOO_LARGE;
 }
 
 template <typename T, int NT>
@@ -962,10 +979,13 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
     return VXG_ERR_INVALID;
   const Topo& t = h->t;
   size_t smem = 0;
-  int st = fused_eligible(t, o->precision, &smem);
+  int first_global = B_COUNT, staged = 0;
+  int st = fused_eligible(t, o->precision, &smem, &first_global, &staged);
   if (st) return st;
   FusedArgs a;
   std::memset(&a, 0, sizeof(a));
+  a.first_global = first_global;
+  a.staged = staged;
   a.gt = make_table(t, params);
   a.S = t.S;
   a.nv = t.nv;

@@ -35,8 +35,10 @@ enum BlobSection {
   B_RES_PTR, B_RES_SRC, B_JAC_PTR, B_JAC_SRC, B_ROWS, B_INDICES, B_INDPTR, B_APOS,
   B_SN_K, B_SN_R, B_SN_PANEL, B_SN_PIV_PTR, B_SN_PIV, B_SN_BORD_PTR, B_SN_BORD,
   B_LV_PTR, B_LV_KMAX, B_LV_RMAX, B_LV_SN, B_LV_SCHUR_OFF, B_LV_BORD_OFF,
-  B_LV_ST_PTR, B_ST_TGT, B_ST_PTR, B_ST_SRC, B_LV_BT_PTR, B_BT_TGT, B_BT_PTR, B_BT_SRC,
-  B_NODES, B_LONG_RES, B_LONG_JAC, B_LONG_ROW, B_COUNT
+  B_LV_ST_PTR, B_LV_BT_PTR, B_BT_TGT, B_BT_PTR, B_BT_SRC,
+  B_NODES, B_LONG_RES, B_LONG_JAC, B_LONG_ROW,
+  B_ST_TGT, B_ST_PTR, B_ST_SRC,  // last: left in global memory when shared memory is short
+  B_COUNT
 };
 struct Blob {
   int off[B_COUNT + 1];
