@@ -56,7 +56,7 @@ class GroupParams(C.Structure):
 
 class NewtonOpts(C.Structure):
     _fields_ = [("max_steps", I32), ("rtol", F64), ("atol", F64), ("max_dv", F64),
-                ("precision", I32), ("refine", I32)]
+                ("precision", I32), ("refine", I32), ("block", I32)]
 
 
 SIGNATURES = {

@@ -24,6 +24,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
+from . import autotune
 from .runtime import engine_for, stream_ptr
 from .symbolic import structure
 
@@ -37,7 +38,12 @@ class Options:
     FP32 and recovers FP64 accuracy with `refine` refinement sweeps against
     the FP64 residual. `solver` is accepted for compatibility: every solve
     uses the supernodal GPU factorization (a circuit of at most ``2 * leaf``
-    unknowns is one dense supernode)."""
+    unknowns is one dense supernode).
+
+    `engine` picks the fused persistent kernel or the generic level kernels;
+    with ``"auto"`` and `autotune`, the faster one (and the fused kernel's
+    CTA width) is timed per topology and batch size (`autotune.choose`).
+    `block` pins the fused kernel's threads per CTA (0: library choice)."""
 
     max_steps: int = 100
     rtol: float = 1e-6
@@ -52,6 +58,8 @@ class Options:
     precision: str = "f64"
     refine: int = 1
     engine: str = "auto"
+    block: int = 0
+    autotune: bool = True
 
     def __post_init__(self):
         if self.engine not in ("auto", "fused", "generic"):
@@ -59,6 +67,8 @@ class Options:
         if self.solver not in ("auto", "dense", "sparse"):
             raise ValueError("solver must be 'auto', 'dense' or 'sparse', "
                              f"got {self.solver!r}")
+        if self.block not in (0, 128, 256, 512):
+            raise ValueError(f"block must be 0, 128, 256 or 512, got {self.block!r}")
         if self.precision not in ("f64", "f32"):
             raise ValueError(f"precision must be 'f64' or 'f32', got {self.precision!r}")
 
@@ -66,7 +76,7 @@ class Options:
         return L.NewtonOpts(self.max_steps if max_steps is None else max_steps, self.rtol,
                             self.atol, self.max_dv,
                             L.VXG_F32 if self.precision == "f32" else L.VXG_F64,
-                            self.refine)
+                            self.refine, self.block)
 
 
 class Solution:
@@ -131,7 +141,11 @@ class _Call:
         dev = self.eng.device
         self.conv = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
         self.iters = torch.zeros(self.n_inst, dtype=torch.int32, device=dev)
+        self.block = options.block
         self.fused = self._use_fused()
+        if self.fused and options.engine == "auto" and options.autotune and not options.block:
+            engine, self.block = autotune.choose(self)
+            self.fused = engine == "fused"
 
     def _use_fused(self) -> bool:
         if self.o.engine == "generic":
@@ -155,6 +169,7 @@ class _Call:
         conv = torch.empty((T, self.B), dtype=torch.int32, device=dev)
         iters = torch.empty((T, self.B), dtype=torch.int32, device=dev)
         nat = o.native()
+        nat.block = self.block
         L.check(self.eng.lib.vxg_fused_run(
             self.eng.handle, self.B, self.params, mode, T, ts_d.data_ptr(), z0.data_ptr(),
             int(dc_first), gm_d.data_ptr(), o.gmin_steps, o.direct_steps, o.gmin,

@@ -26,7 +26,8 @@
 namespace vxg {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kCtaK = 128;  // widest supernode the whole-CTA factorization takes
+constexpr int kCtaK = 128;    // widest supernode the whole-CTA factorization takes
+constexpr int kMaxWarps = 16;  // largest CTA: 512 threads
 
 struct FusedArgs {
   GroupTable gt;
@@ -95,10 +96,10 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
   L.xt = take(sizeof(T) * S);
   L.red = take(64 * sizeof(double));
-  // per-warp column/row buffers and pivot records (8 warps); the whole-CTA
+  // per-warp column/row buffers and pivot records; the whole-CTA
   // factorization uses 2 * kCtaK of the values and kCtaK of the records
-  static_assert(2 * kCtaK <= 2 * 32 * 8 && kCtaK <= 32 * 8, "sbuf too small");
-  L.sbuf = take(sizeof(T) * 2 * 32 * 8 + sizeof(int) * 32 * 8);
+  static_assert(2 * kCtaK <= 2 * 32 * kMaxWarps && kCtaK <= 32 * kMaxWarps, "sbuf too small");
+  L.sbuf = take(sizeof(T) * 2 * 32 * kMaxWarps + sizeof(int) * 32 * kMaxWarps);
   L.total = o;
   return L;
 }
@@ -409,7 +410,10 @@ struct Instance {
   int* ibuf;
   const u16* tb;  // shared-memory tables
 
-  __device__ __forceinline__ const u16* sec(int k) const {
+  // a staged table section (shared memory)
+  __device__ __forceinline__ const u16* sec(int k) const { return tb + A.bo.off[k]; }
+  // a Schur gather section: staged, or left in global memory
+  __device__ __forceinline__ const u16* gsec(int k) const {
     return (k < A.first_global ? tb : A.blob) + A.bo.off[k];
   }
 
@@ -565,8 +569,8 @@ struct Instance {
     int* perm = ibuf + warp * 32;
     const u16 *lv_ptr = sec(B_LV_PTR), *lv_sn = sec(B_LV_SN);
     const u16 *sch_off = sec(B_LV_SCHUR_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
-    const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR), *st_tgt = sec(B_ST_TGT);
-    const u16 *st_ptr = sec(B_ST_PTR), *st_src = sec(B_ST_SRC);
+    const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR), *st_tgt = gsec(B_ST_TGT);
+    const u16 *st_ptr = gsec(B_ST_PTR), *st_src = gsec(B_ST_SRC);
     for (int L = 0; L < A.n_levels; ++L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
       const int mode = level_mode(L);
@@ -856,7 +860,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_consta
   I.xt = reinterpret_cast<T*>(smem + L.xt);
   I.red = reinterpret_cast<double*>(smem + L.red);
   I.sbuf = reinterpret_cast<T*>(smem + L.sbuf);
-  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * 2 * 32 * 8);
+  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * 2 * 32 * kMaxWarps);
   const long long BS = (long long)A.B * A.S;
   for (int b = blockIdx.x; b < A.B; b += gridDim.x) {
     I.b = b;
@@ -1047,9 +1051,21 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   int dev = 0, sms = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  // few instances: wider CTAs shorten each instance's critical path
-  const bool wide = batch < 2 * sms;
-  if (o->precision == VXG_F32)
-    return wide ? launch_fused<float, 256>(a, smem, s) : launch_fused<float, 128>(a, smem, s);
-  return wide ? launch_fused<double, 256>(a, smem, s) : launch_fused<double, 128>(a, smem, s);
+  // CTA width: the caller's (an autotuned choice), else wider CTAs when few
+  // instances or few resident CTAs per SM leave warps idle
+  int nt = o->block;
+  if (nt == 0) {
+    int smem_sm = 0;
+    VXG_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                        dev));
+    const int fit = (int)(smem_sm / (smem + 1024));
+    nt = batch < 2 * sms ? 256 : fit <= 1 ? 512 : fit <= 2 ? 256 : 128;
+  }
+  const bool f32 = o->precision == VXG_F32;
+  switch (nt) {
+    case 128: return f32 ? launch_fused<float, 128>(a, smem, s) : launch_fused<double, 128>(a, smem, s);
+    case 256: return f32 ? launch_fused<float, 256>(a, smem, s) : launch_fused<double, 256>(a, smem, s);
+    case 512: return f32 ? launch_fused<float, 512>(a, smem, s) : launch_fused<double, 512>(a, smem, s);
+    default: return VXG_ERR_INVALID;
+  }
 }
