@@ -59,6 +59,8 @@ struct FusedArgs {
 };
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ inline int sbuf_values(int nw) { return 64 * nw > 2 * kCtaK ? 64 * nw : 2 * kCtaK; }
+__host__ __device__ inline int sbuf_records(int nw) { return 32 * nw > kCtaK ? 32 * nw : kCtaK; }
 
 // Shared-memory layout of one instance.
 struct FusedLayout {
@@ -67,7 +69,8 @@ struct FusedLayout {
 
 template <typename T>
 __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, int n_jac,
-                                                    int work, int max_scr, int blob_len) {
+                                                    int work, int max_scr, int blob_len,
+                                                    int nw) {
   // T is the panel type; the Jacobian contributions use the same type
   FusedLayout L;
   size_t o = 0;
@@ -96,10 +99,9 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
   L.xt = take(sizeof(T) * S);
   L.red = take(64 * sizeof(double));
-  // per-warp column/row buffers and pivot records; the whole-CTA
-  // factorization uses 2 * kCtaK of the values and kCtaK of the records
-  static_assert(2 * kCtaK <= 2 * 32 * kMaxWarps && kCtaK <= 32 * kMaxWarps, "sbuf too small");
-  L.sbuf = take(sizeof(T) * 2 * 32 * kMaxWarps + sizeof(int) * 32 * kMaxWarps);
+  // per-warp column/row buffers (64 values) and pivot records (32) of nw
+  // warps, or the whole CTA's (2 kCtaK values, kCtaK records)
+  L.sbuf = take(sizeof(T) * sbuf_values(nw) + sizeof(int) * sbuf_records(nw));
   L.total = o;
   return L;
 }
@@ -165,10 +167,9 @@ __device__ __forceinline__ void group_sync() {
     __syncwarp();
 }
 
-template <typename T, bool CTA, int NT>
+template <typename T, bool CTA, int NT, int KQ>  // KQ: columns per lane (k <= 32 KQ)
 __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* perm) {
-  constexpr int GW = CTA ? NT / 32 : 1;      // warps in the group
-  constexpr int KQ = CTA ? kCtaK / 32 : 1;   // columns per lane
+  constexpr int GW = CTA ? NT / 32 : 1;  // warps in the group
   const int lane = threadIdx.x & 31;
   const int gw = CTA ? (threadIdx.x >> 5) : 0;  // warp index inside the group
   T* A = P;
@@ -410,11 +411,20 @@ struct Instance {
   int* ibuf;
   const u16* tb;  // shared-memory tables
 
-  // a staged table section (shared memory)
+  // a staged table section (shared memory; the Schur gather sections may
+  // instead stay in global memory, see apply_schur)
   __device__ __forceinline__ const u16* sec(int k) const { return tb + A.bo.off[k]; }
-  // a Schur gather section: staged, or left in global memory
-  __device__ __forceinline__ const u16* gsec(int k) const {
-    return (k < A.first_global ? tb : A.blob) + A.bo.off[k];
+
+  // work[tgt] -= (sum of the level's Schur block entries aimed at it), one
+  // thread per target, sources in a fixed order
+  __device__ __forceinline__ void apply_schur(int t0, int t1, const u16* st_tgt,
+                                              const u16* st_ptr, const u16* st_src) {
+    for (int t = t0 + threadIdx.x; t < t1; t += NT) {
+      T acc = T(0);
+      const int p1 = st_ptr[t + 1];
+      for (int p = st_ptr[t]; p < p1; ++p) acc += scr[st_src[p]];
+      work[st_tgt[t]] -= acc;
+    }
   }
 
   // How a level's supernodes are factored and solved: one thread each
@@ -569,8 +579,7 @@ struct Instance {
     int* perm = ibuf + warp * 32;
     const u16 *lv_ptr = sec(B_LV_PTR), *lv_sn = sec(B_LV_SN);
     const u16 *sch_off = sec(B_LV_SCHUR_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
-    const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR), *st_tgt = gsec(B_ST_TGT);
-    const u16 *st_ptr = gsec(B_ST_PTR), *st_src = gsec(B_ST_SRC);
+    const u16 *sn_panel = sec(B_SN_PANEL), *st_lv = sec(B_LV_ST_PTR);
     for (int L = 0; L < A.n_levels; ++L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
       const int mode = level_mode(L);
@@ -582,23 +591,26 @@ struct Instance {
       } else if (mode == LV_WARP) {
         for (int p = lo + warp; p < hi; p += NW) {
           const int j = lv_sn[p];
-          sn_factor<T, false, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], colb,
+          sn_factor<T, false, NT, 1>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], colb,
                                   rowb, perm);
         }
       } else {
         for (int p = lo; p < hi; ++p) {
           const int j = lv_sn[p];
-          sn_factor<T, true, NT>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], sbuf,
-                                 sbuf + kCtaK, ibuf);
+          if (sn_k[j] <= 32)
+            sn_factor<T, true, NT, 1>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p],
+                                      sbuf, sbuf + kCtaK, ibuf);
+          else
+            sn_factor<T, true, NT, kCtaK / 32>(work + sn_panel[j], sn_k[j], sn_r[j],
+                                               scr + sch_off[p], sbuf, sbuf + kCtaK, ibuf);
         }
       }
       __syncthreads();
-      for (int t = st_lv[L] + threadIdx.x; t < st_lv[L + 1]; t += NT) {
-        T acc = T(0);
-        const int p1 = st_ptr[t + 1];
-        for (int p = st_ptr[t]; p < p1; ++p) acc += scr[st_src[p]];
-        work[st_tgt[t]] -= acc;
-      }
+      if (A.first_global > B_ST_TGT)  // tables in shared memory
+        apply_schur(st_lv[L], st_lv[L + 1], sec(B_ST_TGT), sec(B_ST_PTR), sec(B_ST_SRC));
+      else
+        apply_schur(st_lv[L], st_lv[L + 1], A.blob + A.bo.off[B_ST_TGT],
+                    A.blob + A.bo.off[B_ST_PTR], A.blob + A.bo.off[B_ST_SRC]);
       __syncthreads();
     }
   }
@@ -834,7 +846,7 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L =
-      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged);
+      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged, NT / 32);
   {  // stage the 16-bit tables once per CTA
     const uint4* src = reinterpret_cast<const uint4*>(A.blob);
     uint4* dst = reinterpret_cast<uint4*>(smem + L.blob);
@@ -860,7 +872,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_consta
   I.xt = reinterpret_cast<T*>(smem + L.xt);
   I.red = reinterpret_cast<double*>(smem + L.red);
   I.sbuf = reinterpret_cast<T*>(smem + L.sbuf);
-  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * 2 * 32 * kMaxWarps);
+  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * sbuf_values(NT / 32));
   const long long BS = (long long)A.B * A.S;
   for (int b = blockIdx.x; b < A.B; b += gridDim.x) {
     I.b = b;
@@ -920,13 +932,14 @@ static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
                              {B_ST_TGT, (t.blob.off[B_ST_TGT] + 7) / 8 * 8}};
   for (int o = 0; o < 2; ++o) {
     const int staged = options[o][1];
+    // sized for the widest CTA; narrower CTAs need slightly less
     const size_t smem = precision == VXG_F32
                             ? fused_layout<float>(t.S, (int)t.nnz, (int)t.n_res_slots,
                                                   (int)t.n_jac_slots, (int)t.work, max_scr,
-                                                  staged).total
+                                                  staged, kMaxWarps).total
                             : fused_layout<double>(t.S, (int)t.nnz, (int)t.n_res_slots,
                                                    (int)t.n_jac_slots, (int)t.work, max_scr,
-                                                   staged).total;
+                                                   staged, kMaxWarps).total;
     *smem_out = smem;
     if (smem <= (size_t)max_optin) {
       if (first_global) *first_global = options[o][0];
@@ -938,8 +951,10 @@ static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
 }
 
 template <typename T, int NT>
-static int launch_fused(const FusedArgs& a, size_t smem, cudaStream_t s) {
+static int launch_fused(const FusedArgs& a, cudaStream_t s) {
   auto kern = fused_kernel<T, NT>;
+  const size_t smem = fused_layout<T>(a.S, a.nnz, a.n_res, a.n_jac, a.work, a.max_scr, a.staged,
+                                      NT / 32).total;
   VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 0, per_sm = 0, smem_sm = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
@@ -1063,9 +1078,9 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   }
   const bool f32 = o->precision == VXG_F32;
   switch (nt) {
-    case 128: return f32 ? launch_fused<float, 128>(a, smem, s) : launch_fused<double, 128>(a, smem, s);
-    case 256: return f32 ? launch_fused<float, 256>(a, smem, s) : launch_fused<double, 256>(a, smem, s);
-    case 512: return f32 ? launch_fused<float, 512>(a, smem, s) : launch_fused<double, 512>(a, smem, s);
+    case 128: return f32 ? launch_fused<float, 128>(a, s) : launch_fused<double, 128>(a, s);
+    case 256: return f32 ? launch_fused<float, 256>(a, s) : launch_fused<double, 256>(a, s);
+    case 512: return f32 ? launch_fused<float, 512>(a, s) : launch_fused<double, 512>(a, s);
     default: return VXG_ERR_INVALID;
   }
 }
