@@ -92,12 +92,20 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.dz = take(d * S);
   L.res = take(d * S);
   L.data = take(sizeof(T) * nnz);
+  // The device contributions (written by the evaluation, read by the
+  // assembly) and the panels, Schur scratch and solve vector (written after
+  // the assembly, read until the solve ends) are never live at the same
+  // time, so they share one region.
+  const size_t shared_at = o;
   L.cf = take(d * n_res);
   L.cq = take(d * n_res);
   L.cj = take(sizeof(T) * n_jac);
+  const size_t contrib_end = o;
+  o = shared_at;
   L.work = take(sizeof(T) * work);
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
   L.xt = take(sizeof(T) * S);
+  if (o < contrib_end) o = contrib_end;
   L.red = take(64 * sizeof(double));
   // per-warp column/row buffers (64 values) and pivot records (32) of nw
   // warps, or the whole CTA's (2 kCtaK values, kCtaK records)
@@ -223,6 +231,13 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
       }
     }
     group_sync<CTA, NT>();
+    T rj[KQ];  // this lane's entries of the scaled pivot row
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int j = lane + 32 * q;
+      rj[q] = j < k ? rowb[j] : T(0);
+    }
+#pragma unroll 4
     for (int i = gw; i < k; i += GW) {
       const T ci = colb[i];
 #pragma unroll
@@ -230,10 +245,10 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
         const int j = lane + 32 * q;
         if (j < k) {
           if (i == c) {
-            A[c * k + j] = rowb[j];
+            A[c * k + j] = rj[q];
           } else {
             const T a = (j == c) ? T(0) : A[i * k + j];
-            A[i * k + j] = a - ci * rowb[j];
+            A[i * k + j] = a - ci * rj[q];
           }
         }
       }
@@ -429,8 +444,9 @@ struct Instance {
 
   // How a level's supernodes are factored and solved: one thread each
   // (many tiny supernodes with short borders), one warp each (several
-  // supernodes), or the whole CTA (a lone supernode, or a few with wide
-  // borders whose Schur blocks need more than a warp).
+  // supernodes, or a lone one with a short border), or the whole CTA
+  // (supernodes wider than 32, or a few with wide borders whose Schur
+  // blocks need more than a warp).
   enum { LV_TINY = 0, LV_WARP = 1, LV_CTA = 2 };
   __device__ __forceinline__ int level_mode(int L) const {
     const u16* lv_ptr = sec(B_LV_PTR);
@@ -438,6 +454,7 @@ struct Instance {
     const int kmax = sec(B_LV_KMAX)[L], rmax = sec(B_LV_RMAX)[L];
     if (kmax > 32) return LV_CTA;
     if (kmax <= kTiny && n >= NT / 32 && rmax <= 8) return LV_TINY;
+    if (n == 1 && rmax <= 32) return LV_WARP;  // no CTA barriers per pivot step
     if (n >= 2 && (2 * n >= NT / 32 || rmax <= 16)) return LV_WARP;
     return LV_CTA;
   }
@@ -522,7 +539,6 @@ struct Instance {
   // time step the state is still z_prev, so q(z_prev) is taken from this
   // evaluation instead of a separate one.
   __device__ void assemble_system(int mode, double gmin, double h, bool first) {
-    for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
     assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
     // Jacobian values in the panel type: FP64 in the plain form; FP32 in the
     // chosen form, where they feed the FP32 factorization and the FP64
@@ -554,6 +570,9 @@ struct Instance {
     }
     if (first && mode != VXG_MODE_DC)
       for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
+    __syncthreads();
+    // the panels overlay the contributions consumed above
+    for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
     __syncthreads();
     const u16* apos = sec(B_APOS);
     for (int e = threadIdx.x; e < A.nnz; e += NT) work[apos[e]] = data[e];
@@ -842,8 +861,14 @@ struct Instance {
   }
 };
 
+// Threads per SM the register allocation is sized for (resident CTAs x NT).
+#ifndef VXG_FUSED_THREADS_PER_SM
+#define VXG_FUSED_THREADS_PER_SM 512
+#endif
+
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) fused_kernel(const __grid_constant__ FusedArgs A) {
+__global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
+    fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L =
       fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged, NT / 32);
