@@ -98,8 +98,11 @@ typedef struct {
   const int64_t* jac_src; /* slot ids, ascending within each entry */
   /* independent sub-circuits (segments) inside the topology */
   int32_t n_seg;
-  const int32_t* seg_ptr;  /* n_seg+1 unknown offsets */
+  const int32_t* seg_ptr;  /* n_seg+1 offsets into seg_idx */
   const int32_t* seg_of;   /* S: segment of each unknown */
+  const int32_t* seg_idx;  /* S: the unknowns of segment s, ascending, are
+                              seg_idx[seg_ptr[s] .. seg_ptr[s+1]); NULL means
+                              the identity (segment s = unknowns seg_ptr[s] ..) */
   /* supernodes: unpadded panels F11 (k*k) | F12 (k*r) | F21 (r*k) */
   int32_t n_sn;
   const int32_t* sn_k;

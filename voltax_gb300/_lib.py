@@ -39,7 +39,7 @@ class TopologyDesc(C.Structure):
         ("diag", PI64), ("n_groups", I32), ("groups", C.POINTER(GroupDesc)),
         ("n_res_slots", I64), ("res_ptr", PI64), ("res_src", PI64),
         ("n_jac_slots", I64), ("jac_ptr", PI64), ("jac_src", PI64),
-        ("n_seg", I32), ("seg_ptr", PI32), ("seg_of", PI32),
+        ("n_seg", I32), ("seg_ptr", PI32), ("seg_of", PI32), ("seg_idx", PI32),
         ("n_sn", I32), ("sn_k", PI32), ("sn_r", PI32), ("sn_panel", PI64),
         ("sn_piv_ptr", PI64), ("sn_piv", PI32), ("sn_bord_ptr", PI64), ("sn_bord", PI32),
         ("work", I64), ("a_pos", PI64),

@@ -133,7 +133,7 @@ static int upload(X** dst, const Y* src, size_t n) {
 
 static void free_topo(Topo& t) {
   void* ptrs[] = {t.indptr, t.tptr, t.tent, t.diag, t.indices, t.rows, t.res_ptr, t.res_src,
-                  t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
+                  t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.seg_idx, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
                   t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
                   t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
                   t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax,
@@ -281,6 +281,16 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
   UP(jac_src, d->jac_src, d->jac_ptr[nnz]);
   UP(seg_ptr, d->seg_ptr, d->n_seg + 1);
   UP(seg_of, d->seg_of, S);
+  {
+    std::vector<int32_t> ident;
+    const int32_t* idx = d->seg_idx;
+    if (!idx) {
+      ident.resize((size_t)S);
+      for (long long i = 0; i < S; ++i) ident[(size_t)i] = (int32_t)i;
+      idx = ident.data();
+    }
+    UP(seg_idx, idx, S);
+  }
   UP(sn_k, d->sn_k, d->n_sn);
   UP(sn_r, d->sn_r, d->n_sn);
   UP(sn_panel, d->sn_panel, d->n_sn);

@@ -166,8 +166,11 @@ __device__ int block_all(int ok, double* red) {
 // the supernodes of a wide level in parallel, k <= 32) or the whole CTA
 // (CTA = true, the lone supernodes of the top levels, k <= kCtaK).
 //   W  = F11^-1 by Gauss-Jordan with partial pivoting (row swaps recorded,
-//        undone as column swaps), two group barriers per pivot step; lane l
-//        owns columns l, l + 32, ...;
+//        undone as column swaps): with rows in registers (warp_gj) for a
+//        warp, or in shared memory with two barriers per pivot step for the
+//        CTA, lane l owning columns l, l + 32, ... (measured: the register
+//        form is the faster one only when other warps have their own
+//        supernodes to factor);
 //   Ub = W F12 in place (one column per warp, the column held in registers
 //        and broadcast by shuffles);
 //   S  = F21 Ub into Sout;  Lb = F21 W in place (one row per warp).
@@ -267,17 +270,14 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
   T* A = P;
   T* F12 = P + k * k;
   T* F21 = F12 + k * r;
-  if (KQ == 1) {  // k <= 32: one warp, rows in registers
-    if (gw == 0) {
-      if (k <= 8)
-        warp_gj<T, 8>(A, k, rowb, perm);
-      else if (k <= 16)
-        warp_gj<T, 16>(A, k, rowb, perm);
-      else
-        warp_gj<T, 32>(A, k, rowb, perm);
-    }
-    group_sync<CTA, NT>();
-  } else {
+  if (!CTA) {  // one warp per supernode (k <= 32): rows in registers
+    if (k <= 8)
+      warp_gj<T, 8>(A, k, rowb, perm);
+    else if (k <= 16)
+      warp_gj<T, 16>(A, k, rowb, perm);
+    else
+      warp_gj<T, 32>(A, k, rowb, perm);
+  } else {  // the whole CTA: shared-memory Gauss-Jordan, rows over warps
   for (int c = 0; c < k; ++c) {
     if (gw == 0) {
       // pivot: largest |A[i][c]| over i >= c, ties to the lower row

@@ -58,7 +58,7 @@ struct Topo {
   long long n_res_slots, n_jac_slots, n_dev;
   long long *res_ptr, *res_src, *jac_ptr, *jac_src;
   int n_seg;
-  int *seg_ptr, *seg_of;
+  int *seg_ptr, *seg_of, *seg_idx;
   int n_sn;
   int *sn_k, *sn_r, *sn_piv, *sn_bord;
   long long *sn_panel, *sn_piv_ptr, *sn_bord_ptr, *a_pos;

@@ -52,7 +52,7 @@ __global__ void newton_init_kernel(int n, const int* __restrict__ mask, int* __r
 template <int NT>
 __global__ void __launch_bounds__(NT)
     newton_update_kernel(int S, int nv, int n_seg, const int* __restrict__ seg_ptr,
-                         double* __restrict__ z, const double* __restrict__ dz,
+                         const int* __restrict__ seg_idx, double* __restrict__ z, const double* __restrict__ dz,
                          int* __restrict__ active, int* __restrict__ converged,
                          int* __restrict__ iters, double max_dv, double rtol, double atol,
                          int* __restrict__ n_active) {
@@ -68,8 +68,9 @@ __global__ void __launch_bounds__(NT)
   // max |dz| over node voltages; NaN propagates as in jnp.max
   double m = 0.0;
   int has_nan = 0;
-  const int nhi = min(hi, nv);
-  for (int i = lo + threadIdx.x; i < nhi; i += NT) {
+  for (int q = lo + threadIdx.x; q < hi; q += NT) {
+    const int i = seg_idx[q];
+    if (i >= nv) continue;  // node voltages only
     const double v = fabs(db[i]);
     if (isnan(v)) has_nan = 1;
     else m = fmax(m, v);
@@ -94,7 +95,8 @@ __global__ void __launch_bounds__(NT)
   const double qd = max_dv / (dv_max + 1e-300);
   const double scale = isnan(qd) ? qd : fmin(1.0, qd);
   int ok = 1;
-  for (int i = lo + threadIdx.x; i < hi; i += NT) {
+  for (int q = lo + threadIdx.x; q < hi; q += NT) {
+    const int i = seg_idx[q];
     const double d = db[i];
     const double zn = zb[i] + scale * d;
     if (!(fabs(d) <= atol + rtol * fabs(zn))) ok = 0;
@@ -331,7 +333,8 @@ int launch_update(const Topo& t, int B, double* z, const double* dz, int* active
                   int* n_active, cudaStream_t s) {
   const int n = B * t.n_seg;
   if (!n) return VXG_OK;
-  newton_update_kernel<256><<<n, 256, 0, s>>>(t.S, t.nv, t.n_seg, t.seg_ptr, z, dz, active,
+  newton_update_kernel<256><<<n, 256, 0, s>>>(t.S, t.nv, t.n_seg, t.seg_ptr, t.seg_idx, z, dz,
+                                              active,
                                               converged, iters, max_dv, rtol, atol, n_active);
   VXG_LAUNCHED();
   return VXG_OK;

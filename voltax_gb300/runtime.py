@@ -43,7 +43,7 @@ def tptr(t: torch.Tensor | None):
 class Tables:
     """All host index arrays of one topology (numpy, kept alive for ctypes)."""
 
-    def __init__(self, circuit, st: Structure, plan: Plan, seg_ptr=None):
+    def __init__(self, circuit, st: Structure, plan: Plan):
         self.st, self.plan = st, plan
         S, nnz = st.size, st.nnz
         self.S, self.nnz, self.nv = S, nnz, st.n_nodes
@@ -94,12 +94,15 @@ class Tables:
         self.res_ptr, self.res_src = self._pull(cat(res_tgt), cat(res_id), S)
         self.jac_ptr, self.jac_src = self._pull(cat(jac_tgt), cat(jac_id), nnz)
 
-        # ---- segments
-        if seg_ptr is None:
-            seg_ptr = np.array([0, S])
-        self.seg_ptr = i32(seg_ptr)
-        self.n_seg = len(seg_ptr) - 1
-        self.seg_of = i32(np.repeat(np.arange(self.n_seg), np.diff(seg_ptr)))
+        # ---- segments (independent sub-circuits, Circuit.with_segments)
+        seg_of = None if circuit is None else circuit.unknown_segments()
+        if seg_of is None:
+            seg_of = np.zeros(S, dtype=np.int32)
+        self.seg_of = i32(seg_of)
+        self.n_seg = int(self.seg_of.max()) + 1 if S else 1
+        counts = np.bincount(self.seg_of, minlength=self.n_seg)
+        self.seg_ptr = i32(np.concatenate([[0], np.cumsum(counts)]))
+        self.seg_idx = i32(np.argsort(self.seg_of, kind="stable"))
 
         # ---- plan
         self.sn_k = i32(plan.k)
@@ -162,6 +165,7 @@ class Tables:
                                                _ptr(self.jac_src, L.I64))
         d.n_seg, d.seg_ptr, d.seg_of = (self.n_seg, _ptr(self.seg_ptr, L.I32),
                                         _ptr(self.seg_of, L.I32))
+        d.seg_idx = _ptr(self.seg_idx, L.I32)
         d.n_sn = len(self.sn_k)
         d.sn_k, d.sn_r, d.sn_panel = (_ptr(self.sn_k, L.I32), _ptr(self.sn_r, L.I32),
                                       _ptr(self.sn_panel, L.I64))
@@ -184,10 +188,10 @@ class Tables:
 class Engine:
     """A topology resident on the GPU (one ``vxg_handle``)."""
 
-    def __init__(self, circuit, st: Structure, plan: Plan, seg_ptr=None):
+    def __init__(self, circuit, st: Structure, plan: Plan):
         self.device = cuda_device()
         self.lib = L.load()
-        self.tables = Tables(circuit, st, plan, seg_ptr)
+        self.tables = Tables(circuit, st, plan)
         self.st, self.plan = st, plan
         self.S, self.nnz, self.nv = st.size, st.nnz, st.n_nodes
         self.n_seg = self.tables.n_seg
@@ -259,11 +263,12 @@ def engine_for(st: Structure, circuit=None, plan: Plan | None = None) -> Engine:
     """The cached `Engine` of a structure and plan (default ``st.plan``),
     with the device tables of `circuit` when stamping is needed."""
     plan = st.plan if plan is None else plan
-    key = (id(st), id(plan), _kinds(circuit))
+    segs = None if circuit is None else circuit.node_segment
+    key = (id(st), id(plan), _kinds(circuit), None if segs is None else hash(segs))
     eng = _ENGINES.get(key)
     if eng is None or eng.st is not st or eng.plan is not plan:
         if circuit is None:  # linear algebra only: reuse any engine of this plan
-            for (sid, pid, _), e in list(_ENGINES.items()):
+            for (sid, pid, _, _), e in list(_ENGINES.items()):
                 if sid == id(st) and pid == id(plan) and e.st is st and e.plan is plan:
                     return e
         eng = Engine(circuit, st, plan)

@@ -7,6 +7,8 @@ All draws use ``numpy.random.default_rng(seed)``.
   1.0 V pads at the 4 corners and at every 25th node of a clockwise walk of
   the border starting at the top-left corner (100 x 100: 19 pads, 10,019
   unknowns). Structure follows voltax/benchmarks/benchmark_power_grid.py:30-66.
+* `power_grid_batch(sides)`: an uneven batch of such grids as one circuit
+  of independent segments (`Circuit.with_segments`).
 * `ring_oscillator(stages)`: CMOS ring of EKV inverters (NMOS w=1u, PMOS
   w=2u, l=0.13u), VDD 1.2 V, 5 fF per stage; `ring_initial_state` gives the
   alternating rail pattern with a 0.1 V kick on node 0.
@@ -37,11 +39,9 @@ def grid_pads(n: int, every: int = 25) -> list[tuple[int, int]]:
     return sorted(sites)
 
 
-def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
-               sink_max: float = 1e-3, vpad: float = 1.0):
-    rng = np.random.default_rng(seed)
-    b = CircuitBuilder()
-    node = lambda i, j: f"n{i}_{j}"  # noqa: E731
+def _grid_into(b: CircuitBuilder, n: int, rng, sigma: float, sink_max: float, vpad: float,
+               prefix: str = "") -> None:
+    node = lambda i, j: f"{prefix}n{i}_{j}"  # noqa: E731
     edges = []
     for i in range(n):
         for j in range(n):
@@ -51,13 +51,38 @@ def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
                 edges.append((node(i, j), node(i + 1, j)))
     g = np.exp(rng.normal(0.0, sigma, len(edges)))
     for k, (a, c) in enumerate(edges):
-        b.resistor(a, c, 1.0 / g[k], name=f"R{k}")
+        b.resistor(a, c, 1.0 / g[k], name=f"{prefix}R{k}")
     sinks = rng.uniform(0.0, sink_max, n * n)
     for p in range(n * n):
-        b.isource(node(p // n, p % n), "0", sinks[p], name=f"I{p}")
+        b.isource(node(p // n, p % n), "0", sinks[p], name=f"{prefix}I{p}")
     for k, (i, j) in enumerate(grid_pads(n)):
-        b.vsource(node(i, j), "0", vpad, name=f"Vpad{k}")
+        b.vsource(node(i, j), "0", vpad, name=f"{prefix}Vpad{k}")
+
+
+def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
+               sink_max: float = 1e-3, vpad: float = 1.0):
+    b = CircuitBuilder()
+    _grid_into(b, n, np.random.default_rng(seed), sigma, sink_max, vpad)
     return b.build()
+
+
+def power_grid_batch(sides, seed: int = 0, sigma: float = 0.3, sink_max: float = 1e-3,
+                     vpad: float = 1.0):
+    """An uneven batch of grids as one circuit of independent segments:
+    grid k (nodes ``g{k}_n{i}_{j}``) is `power_grid` ``(sides[k],
+    seed + k)``, and segment k is its nodes and pad currents."""
+    b = CircuitBuilder()
+    for k, n in enumerate(sides):
+        _grid_into(b, int(n), np.random.default_rng(seed + k), sigma, sink_max, vpad,
+                   prefix=f"g{k}_")
+    c = b.build()
+    seg = [int(name[1:name.index("_")]) for name in c.layout.node_names]
+    return c.with_segments(seg)
+
+
+def grid_sides(count: int, lo: int, hi: int, seed: int = 0) -> list[int]:
+    """Mesh sides drawn uniformly from {lo, ..., hi}."""
+    return [int(x) for x in np.random.default_rng(seed).integers(lo, hi + 1, count)]
 
 
 def ring_oscillator(stages: int = 101, cload: float = 5e-15):
