@@ -59,6 +59,9 @@ class Workload:
         if self.name == "ota_warm":
             return wl.apply_ota_params(wl.ota_chain(OTA_STAGES),
                                        wl.ota_params(instances, seed=OTA_TEST_SEED + seed))
+        if self.name == "grids":
+            return wl.power_grid_batch(wl.grid_sides(instances, *GRID_SIDES, seed=seed),
+                                       seed=seed)
         raise ValueError(self.name)
 
     def ic(self, circuit):
@@ -80,6 +83,8 @@ class Workload:
             return f"ring_oscillator101_trap{n_t}"
         if self.name == "ota_warm":
             return f"ota_chain{OTA_STAGES}_dc_warm_start{instances}"
+        if self.name == "grids":
+            return f"power_grid_batch{instances}_sides{GRID_SIDES[0]}-{GRID_SIDES[1]}_dc_adjoint"
         return "power_grid100_dc"
 
 
@@ -89,7 +94,10 @@ WORKLOADS = {
     "ring101": Workload("ring101", "transient", "trap", 2e-9, 2001, ["n0", "n50", "n100"], 1),
     "grid100": Workload("grid100", "dc", None, 0.0, 1, None, 1),
     "ota_warm": Workload("ota_warm", "dc", None, 0.0, 1, None, 10000),
+    "grids": Workload("grids", "dc", None, 0.0, 1, None, 32),
 }
+# uneven batch: `instances` grids of side U{50..120} in one segmented circuit
+GRID_SIDES = (50, 120)
 # learned warm start: 66-stage OTA chain (201 nodes), 200k training
 # operating points (parameter seed 1), 10k held-out instances (seed 2)
 OTA_STAGES, OTA_TRAIN, OTA_TRAIN_SEED, OTA_TEST_SEED = 66, 200_000, 1, 2
@@ -210,6 +218,8 @@ def run_reference(a):
     per_thread = 4 if w.analysis == "transient" and w.name == "adder_mc" else 1
     if w.name == "grid100":
         per_thread = 8
+    if w.name == "grids":
+        cores = min(cores, 2)  # each system is the whole batch
     ts = w.times(a.time_points)
     systems, z0 = _cpu_systems(w, a.instances, cores * per_thread)
 
@@ -278,6 +288,9 @@ def main():
     cpu = cpu_baseline(w, a.time_points, a.instances) if rank == 0 and not a.no_cpu else None
     if w.name == "ota_warm":
         main_warm(a, w, cpu)
+        return
+    if w.name == "grids":
+        main_grids(a, w, cpu)
         return
 
     import torch
@@ -546,6 +559,112 @@ def main_warm(a, w, cpu):
                      "loss_last_epoch": hist[-1]},
         "e2e": {"value": B * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(out.numel() * 8)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------- uneven grid batch arm
+def main_grids(a, w, cpu):
+    """An uneven batch of power grids in one segmented circuit: DC of every
+    grid (one solve per grid), and the adjoint of each grid's largest IR drop
+    with respect to all segment conductances (one transposed solve for the
+    batch)."""
+    import torch
+    import voltax_gb300 as vx
+    from voltax_gb300 import _lib, symbolic
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    t0 = time.perf_counter()
+    circuit = w.circuit(a.instances, seed=0)
+    st = symbolic.structure(circuit)
+    plan_s = time.perf_counter() - t0
+    n_grids = a.instances
+    c_dev = to_device(circuit, dev)
+    segs = torch.as_tensor(circuit.unknown_segments()[: circuit.n_nodes], device=dev,
+                           dtype=torch.long)
+    chosen = vx.Options(precision="f32")
+    plain = vx.Options(precision="f64")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, k):
+        ms = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.sum(ms)) / 1e3
+
+    def drops(v):
+        """largest IR drop (1 V - v) of each grid, by segment"""
+        d = torch.full((n_grids,), -float("inf"), dtype=v.dtype, device=v.device)
+        return d.scatter_reduce(0, segs, 1.0 - v, reduce="amax")
+
+    def adjoint(opts):
+        el = c_dev.elements["Resistor"]
+        e2 = el.with_nodes(el.nodes)
+        e2.log_r = el.log_r.detach().clone().requires_grad_(True)
+        sol = vx.dc(c_dev.replace("Resistor", e2), options=opts)
+        drops(sol.z[: circuit.n_nodes]).sum().backward()
+        return e2.log_r.grad
+
+    fwd = lambda: vx.dc(c_dev, options=chosen)  # noqa: E731
+    for _ in range(a.warmup):
+        fwd()
+    n0 = lib.vxg_launch_count()
+    with Clocks(local) as clk:
+        t_fwd = timed(fwd, a.steps)
+    launches = (lib.vxg_launch_count() - n0) // a.steps
+    vx.dc(c_dev, options=plain)
+    t_plain = timed(lambda: vx.dc(c_dev, options=plain), max(1, min(a.steps, 2)))
+    adjoint(chosen)
+    t_adj = timed(lambda: adjoint(chosen), max(1, min(a.steps, 2)))
+    s32, s64 = fwd(), vx.dc(c_dev, options=plain)
+    nv = circuit.n_nodes
+    match = float((s32.z[:nv] - s64.z[:nv]).abs().max())
+    g32, g64 = adjoint(chosen), adjoint(plain)
+    grad_rel = float((g32 - g64).norm() / g64.norm())
+    host_c = to_device(circuit, None, pin=True)
+    out = torch.empty(nv, dtype=torch.float64, pin_memory=True)
+
+    def e2e():
+        s = vx.dc(host_c, options=chosen)
+        out.copy_(s.z[:nv], non_blocking=True)
+
+    e2e()
+    t_e2e = timed(e2e, a.steps)
+    sides = [int(round((np.sum(circuit.unknown_segments()[:nv] == k)) ** 0.5))
+             for k in range(n_grids)]
+    line = {
+        "metric": METRIC, "value": n_grids * a.steps / t_fwd, "unit": UNIT, "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_fwd / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 LU + f64 residual/refinement", "data": "synthetic",
+        "config": {"workload": w.label(n_grids, 1), "grids": n_grids, "sides": sides,
+                   "unknowns": circuit.size, "nnz": st.nnz,
+                   "factor_entries": int(st.plan.stats["factor_entries"]),
+                   "largest_supernode": int(st.plan.stats["largest_supernode"]),
+                   "host_plan_s": plan_s,
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "plain_fp64": {"value": n_grids / (t_plain / max(1, min(a.steps, 2))), "unit": UNIT},
+        "adjoint": {"value": n_grids / (t_adj / max(1, min(a.steps, 2))), "unit":
+                    "grids/s (DC + transposed solve + d max-drop / d log r)",
+                    "rel_diff_vs_fp64": grad_rel},
+        "match": {"max_abs_node_v_diff_vs_fp64": match,
+                  "converged": bool(s32.converged.all()),
+                  "newton_iters": [int(x) for x in s32.iterations.reshape(-1)[:4]]},
+        "e2e": {"value": n_grids * a.steps / t_e2e, "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d_bytes(host_c)), "d2h_bytes_per_step": nv * 8},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,

@@ -419,7 +419,8 @@ def make_plan(st: Structure, leaf: int | None = None) -> Plan:
         panel[1:] = np.cumsum(sizes)[:-1]
     work = int(sizes.sum())
     # border position lookup: (supernode, unknown) -> index in its border
-    bkeys = np.concatenate([i * S + b for i, b in enumerate(borders)]) \
+    bkeys = np.concatenate([np.int64(i) * S + np.asarray(b, np.int64)
+                            for i, b in enumerate(borders)]) \
         if nsn else np.zeros(0, np.int64)
     bidx = np.concatenate([np.arange(len(b)) for b in borders]) \
         if nsn else np.zeros(0, np.int64)
@@ -427,7 +428,7 @@ def make_plan(st: Structure, leaf: int | None = None) -> Plan:
     bkeys, bidx = bkeys[border_order], bidx[border_order]
 
     def bpos(o, v):
-        key = o * S + v
+        key = np.asarray(o, np.int64) * S + np.asarray(v, np.int64)
         q = np.searchsorted(bkeys, key)
         qc = np.minimum(q, max(len(bkeys) - 1, 0))
         if len(bkeys) == 0 or not np.all(bkeys[qc] == key):
