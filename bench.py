@@ -193,16 +193,20 @@ def _cpu_run(w, sysm, z0, ts):
 def cpu_baseline(w, n_t, instances, min_seconds=10.0):
     """The compiled CPU restatement (oracle/cvx.c), one thread, whole
     instances until `min_seconds` have passed."""
-    systems, z0 = _cpu_systems(w, instances, min(instances, 64))
+    # the grid batch is one circuit holding `instances` grids (segments)
+    per_run = instances if w.name == "grids" else 1
+    systems, z0 = _cpu_systems(w, instances, 1 if per_run > 1 else min(instances, 64))
     ts = w.times(n_t)
     _cpu_run(w, systems[0], z0, ts[:3])
     solves, t0, i = 0, time.perf_counter(), 0
     while time.perf_counter() - t0 < min_seconds and i < 10000:
         _cpu_run(w, systems[i % len(systems)], z0, ts)
-        solves += len(ts)
+        solves += len(ts) * per_run
         i += 1
     secs = time.perf_counter() - t0
     what = "DC solve" if w.analysis == "dc" else f"DC + {len(ts) - 1} {w.method.upper()} steps"
+    if per_run > 1:
+        what = f"DC solve of all {per_run} grids"
     return {"value": solves / secs, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"{i} whole instances ({what} each) on 1 thread, {secs:.1f} s; "
                       "compiled C restatement oracle/cvx.c"}

@@ -109,7 +109,8 @@ def schur_targets(plan, S):
     (the targets of voltax/sparse.py:514-527 in the unpadded layout)."""
     k, r, panel = plan.k, plan.r, plan.panel
     sn_of, pos_in = plan.sn_of, plan.pos_in
-    bkeys = np.concatenate([i * S + b for i, b in enumerate(plan.borders)])
+    bkeys = np.concatenate([np.int64(i) * S + np.asarray(b, np.int64)
+                            for i, b in enumerate(plan.borders)])
     bidx = np.concatenate([np.arange(len(b)) for b in plan.borders])
     order = np.argsort(bkeys)
     bkeys, bidx = bkeys[order], bidx[order]
@@ -122,11 +123,12 @@ def schur_targets(plan, S):
         up = su < sv
         o = su[up]
         out[up] = panel[o] + k[o] * k[o] + pos_in[u[up]] * r[o] + \
-            bidx[np.searchsorted(bkeys, o * S + v[up])]
+            bidx[np.searchsorted(bkeys, np.asarray(o, np.int64) * S + np.asarray(v[up], np.int64))]
         lo = su > sv
         o = sv[lo]
         out[lo] = panel[o] + k[o] * k[o] + k[o] * r[o] + \
-            bidx[np.searchsorted(bkeys, o * S + u[lo])] * k[o] + pos_in[v[lo]]
+            bidx[np.searchsorted(bkeys, np.asarray(o, np.int64) * S + np.asarray(u[lo], np.int64))] * k[o] + \
+                pos_in[v[lo]]
         return out
 
     ptr, tg = [0], []

@@ -72,7 +72,7 @@ def padded_plan(size, supernodes, borders, classes, rows, indices) -> PaddedPlan
     work = off
     bsn = np.repeat(np.arange(nsn), r)
     bvar = np.concatenate(borders) if nsn else np.zeros(0, np.int64)
-    bkeys = bsn * S + bvar
+    bkeys = np.asarray(bsn, np.int64) * S + np.asarray(bvar, np.int64)
     order = np.argsort(bkeys)
     bkeys = bkeys[order]
     bidx = np.concatenate([np.arange(x) for x in r])[order]
@@ -80,7 +80,7 @@ def padded_plan(size, supernodes, borders, classes, rows, indices) -> PaddedPlan
     def bpos(o, v):
         if len(bidx) == 0:
             return np.zeros(np.shape(o), np.int64)
-        qq = np.searchsorted(bkeys, o * S + v)
+        qq = np.searchsorted(bkeys, np.asarray(o, np.int64) * S + np.asarray(v, np.int64))
         return bidx[np.minimum(qq, len(bidx) - 1)]
 
     def position(u, v):
