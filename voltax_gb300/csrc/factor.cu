@@ -55,16 +55,19 @@ __global__ void __launch_bounds__(NT)
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* A = reinterpret_cast<T*>(smem_raw);  // k*k
-  T* col = A + k * k;                     // k
-  T* tA = col + k;                        // kTile*k
+  T* col = A + k * k;                     // k: pivot column
+  T* rowb = col + k;                      // k: scaled pivot row
+  T* tA = rowb + k;                       // kTile*k
   T* tB = tA + kTile * k;                 // k*kTile
   int* perm = reinterpret_cast<int*>(tB + k * kTile);
-  __shared__ int s_piv;
 
   for (int i = threadIdx.x; i < k * k; i += NT) A[i] = F11[i];
   __syncthreads();
 
-  // ---- Gauss-Jordan inverse with partial pivoting (row swaps recorded)
+  // ---- Gauss-Jordan inverse with partial pivoting (row swaps recorded).
+  // Warp 0 picks the pivot, swaps the rows and stages the pivot column and
+  // the scaled pivot row; then every warp updates its rows: two barriers
+  // per pivot step.
   for (int c = 0; c < k; ++c) {
     if (warp == 0) {
       T best = T(-1);
@@ -84,46 +87,46 @@ __global__ void __launch_bounds__(NT)
           bi = oi;
         }
       }
-      if (lane == 0) {
-        s_piv = bi;
-        perm[c] = bi;
+      const int p = __shfl_sync(0xffffffffu, bi, 0);
+      if (lane == 0) perm[c] = p;
+      if (p != c)
+        for (int jj = lane; jj < k; jj += 32) {
+          const T tmp = A[p * k + jj];
+          A[p * k + jj] = A[c * k + jj];
+          A[c * k + jj] = tmp;
+        }
+      __syncwarp();
+      const T d = A[c * k + c];
+      for (int jj = lane; jj < k; jj += 32) {
+        rowb[jj] = ((jj == c) ? T(1) : A[c * k + jj]) / d;
+        col[jj] = (jj == c) ? T(0) : A[jj * k + c];
       }
     }
     __syncthreads();
-    const int p = s_piv;
-    if (p != c)
-      for (int jj = threadIdx.x; jj < k; jj += NT) {
-        const T tmp = A[p * k + jj];
-        A[p * k + jj] = A[c * k + jj];
-        A[c * k + jj] = tmp;
-      }
-    __syncthreads();
-    const T d = A[c * k + c];
-    for (int i = threadIdx.x; i < k; i += NT) col[i] = (i == c) ? T(0) : A[i * k + c];
-    __syncthreads();
-    for (int jj = threadIdx.x; jj < k; jj += NT)
-      A[c * k + jj] = ((jj == c) ? T(1) : A[c * k + jj]) / d;
-    __syncthreads();
     for (int i = warp; i < k; i += NW) {
-      if (i == c) continue;
       const T f = col[i];
       for (int jj = lane; jj < k; jj += 32) {
-        const T a = (jj == c) ? T(0) : A[i * k + jj];
-        A[i * k + jj] = a - f * A[c * k + jj];
+        if (i == c) {
+          A[c * k + jj] = rowb[jj];
+        } else {
+          const T a = (jj == c) ? T(0) : A[i * k + jj];
+          A[i * k + jj] = a - f * rowb[jj];
+        }
       }
     }
     __syncthreads();
   }
-  for (int c = k - 1; c >= 0; --c) {
-    const int p = perm[c];
-    if (p != c)
-      for (int i = threadIdx.x; i < k; i += NT) {
+  // undo the row swaps as column swaps: one thread per row, all swaps in order
+  for (int i = threadIdx.x; i < k; i += NT)
+    for (int c = k - 1; c >= 0; --c) {
+      const int p = perm[c];
+      if (p != c) {
         const T tmp = A[i * k + c];
         A[i * k + c] = A[i * k + p];
         A[i * k + p] = tmp;
       }
-    __syncthreads();
-  }
+    }
+  __syncthreads();
   for (int i = threadIdx.x; i < k * k; i += NT) F11[i] = A[i];
   if (r == 0) return;
 
@@ -189,7 +192,7 @@ __global__ void schur_apply_kernel(int B, long long ntgt, const long long* __res
 }
 
 size_t factor_smem_bytes(int k, size_t es) {
-  return (size_t)(k * k + k + 2 * kTile * k) * es + (size_t)k * sizeof(int) + 16;
+  return (size_t)(k * k + 2 * k + 2 * kTile * k) * es + (size_t)k * sizeof(int) + 16;
 }
 
 template <typename T>
