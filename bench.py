@@ -393,9 +393,18 @@ def main():
     step_s = t32 / a.steps
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_per_iter * total_iters / step_s / 1e9
+    # DRAM traffic of one fused launch: the packed parameter rows read once per
+    # instance, the states written per time point, converged + iterations. An
+    # ncu capture of 512 instances x 21 points read 5.87 MB = the packed rows
+    # (profiles/fused_kernel_adder_mc512_v4.md); its 6.4 MB of states stayed
+    # in L2, at this size they do not.
+    traffic = None
+    if engine_used == "fused":
+        packed = sum(t.numel() * 8 for t in _Call(dev_circuit, opts32).keep)
+        traffic = packed + B * len(ts) * (8 * st.size + 8)
     roofline = {"bound": "hbm", "kernel": "fused_kernel<float>" if engine_used == "fused"
                 else "factor/solve level kernels", "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                 "peak_source": "measured" if peaks else "fallback",
                 "algorithmic_bytes_per_launch": bytes_per_iter * total_iters,
                 "newton_iterations_per_launch": total_iters,
