@@ -36,6 +36,31 @@ __device__ __forceinline__ T tabs(T x) {
   return x < T(0) ? -x : x;
 }
 
+// C[a][j] = sum_l X[a*ldx + l] * Y[l*ldy + j] for a < nr, j < nc <= 32 (lane
+// = column), handed to store(a, j, value). Each warp carries four rows at a
+// time in independent accumulators (one Y load per four FMAs); every sum
+// runs over l in ascending order.
+template <typename T, int NT, typename Store>
+__device__ __forceinline__ void tile_product(int nr, int nc, int k, const T* X, int ldx,
+                                             const T* Y, int ldy, Store store) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane >= nc) return;
+  for (int a0 = warp; a0 < nr; a0 += 4 * NW) {
+    const int na = min(4, (nr - a0 + NW - 1) / NW);
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+    for (int l = 0; l < k; ++l) {
+      const T y = Y[l * ldy + lane];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q < na) acc[q] += X[(a0 + q * NW) * ldx + l] * y;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (q < na) store(a0 + q * NW, lane, acc[q]);
+  }
+}
+
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT)
     factor_level_kernel(const int* __restrict__ lv_sn, const long long* __restrict__ schur_off,
@@ -136,12 +161,9 @@ __global__ void __launch_bounds__(NT)
     for (int i = warp; i < k; i += NW)
       for (int jj = lane; jj < tw; jj += 32) tB[i * kTile + jj] = F12[(long long)i * r + c0 + jj];
     __syncthreads();
-    for (int i = warp; i < k; i += NW)
-      for (int jj = lane; jj < tw; jj += 32) {
-        T acc = T(0);
-        for (int l = 0; l < k; ++l) acc += A[i * k + l] * tB[l * kTile + jj];
-        F12[(long long)i * r + c0 + jj] = acc;
-      }
+    tile_product<T, NT>(k, tw, k, A, k, tB, kTile, [&](int i, int jj, T v) {
+      F12[(long long)i * r + c0 + jj] = v;
+    });
     __syncthreads();
   }
 
@@ -157,20 +179,15 @@ __global__ void __launch_bounds__(NT)
         for (int jj = lane; jj < tw; jj += 32)
           tB[i * kTile + jj] = F12[(long long)i * r + c0 + jj];
       __syncthreads();
-      for (int a = warp; a < tr; a += NW)
-        for (int jj = lane; jj < tw; jj += 32) {
-          T acc = T(0);
-          for (int l = 0; l < k; ++l) acc += tA[a * k + l] * tB[l * kTile + jj];
-          Sout[(long long)(a0 + a) * r + c0 + jj] = acc;
-        }
+      tile_product<T, NT>(tr, tw, k, tA, k, tB, kTile, [&](int a, int jj, T v) {
+        Sout[(long long)(a0 + a) * r + c0 + jj] = v;
+      });
       __syncthreads();
     }
-    for (int a = warp; a < tr; a += NW)
-      for (int jj = lane; jj < k; jj += 32) {
-        T acc = T(0);
-        for (int l = 0; l < k; ++l) acc += tA[a * k + l] * A[l * k + jj];
-        F21[(long long)(a0 + a) * k + jj] = acc;
-      }
+    for (int j0 = 0; j0 < k; j0 += 32)
+      tile_product<T, NT>(tr, min(32, k - j0), k, tA, k, A + j0, k, [&](int a, int jj, T v) {
+        F21[(long long)(a0 + a) * k + j0 + jj] = v;
+      });
     __syncthreads();
   }
 }
@@ -215,7 +232,14 @@ static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scr
     const size_t smem = factor_smem_bytes(kmax, sizeof(T));
     if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
     dim3 grid((unsigned)(hi - lo), (unsigned)B);
-    if (kmax > 48) {
+    if (kmax > 80) {
+      auto kern = factor_level_kernel<T, 512>;
+      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+      kern<<<grid, 512, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
+                                   t.sn_panel, work, ws, scratch, ss);
+      VXG_LAUNCHED();
+    } else if (kmax > 48) {
       auto kern = factor_level_kernel<T, 256>;
       VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
