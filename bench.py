@@ -54,6 +54,8 @@ class Workload:
             return wl.mirror_adder_mc(instances, seed=seed)
         if self.name == "ring101":
             return wl.ring_oscillator(101)[0]
+        if self.name == "ring101_l1":
+            return wl.ring_oscillator_level1(101)[0]
         if self.name == "grid100":
             return wl.power_grid(100, seed=seed)
         if self.name == "ota_warm":
@@ -69,6 +71,9 @@ class Workload:
         if self.name == "ring101":
             from voltax_gb300 import workloads as wl
             return wl.ring_initial_state(circuit, [f"n{k}" for k in range(101)])
+        if self.name == "ring101_l1":
+            from voltax_gb300 import workloads as wl
+            return wl.ring_level1_initial_state(circuit, [f"n{k}" for k in range(1, 102)])
         return "dc"
 
     def times(self, n_t=None):
@@ -81,6 +86,8 @@ class Workload:
             return f"mirror_adder_mc{instances}"
         if self.name == "ring101":
             return f"ring_oscillator101_trap{n_t}"
+        if self.name == "ring101_l1":
+            return f"ring_oscillator101_level1_be{n_t}"
         if self.name == "ota_warm":
             return f"ota_chain{OTA_STAGES}_dc_warm_start{instances}"
         if self.name == "grids":
@@ -93,6 +100,11 @@ WORKLOADS = {
                          ["s0", "s1", "s2", "s3", "co"], INSTANCES),
     "ring101": Workload("ring101", "transient", "trap", 2e-9, 2001, ["n0", "n50", "n100"], 1),
     "grid100": Workload("grid100", "dc", None, 0.0, 1, None, 1),
+    # voltax's own ring benchmark (benchmarks/benchmark_sparse.py:143-176): exact
+    # Level 1, backward Euler, 3445 steps over 0.3 ns (uniform here; the
+    # reference steps on ngspice's accepted points)
+    "ring101_l1": Workload("ring101_l1", "transient", "be", 0.3e-9, 3446,
+                           ["n1", "n51", "n101"], 1),
     "ota_warm": Workload("ota_warm", "dc", None, 0.0, 1, None, 10000),
     "grids": Workload("grids", "dc", None, 0.0, 1, None, 32),
 }
@@ -427,11 +439,14 @@ def main():
 
     if rank != 0:
         return
+    # voltax publishes this one workload: 499 us per step on one CPU thread
+    # (benchmarks/README.md:217), i.e. 2004 Newton solves/s
+    vs_baseline = value / (1.0 / 499e-6) if w.name == "ring101_l1" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * t32 / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 LU + f64 residual/refinement",
-        "data": "synthetic",
+        "scaling": "weak", "vs_baseline": vs_baseline,
+        "dtype": "f32 LU + f64 residual/refinement", "data": "synthetic",
         "config": {"workload": w.label(B, len(ts)), "instances": B,
                    "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,

@@ -53,8 +53,11 @@ enum {
   VXG_KIND_CAPACITOR = 1,   /* Capacitor                 [c]                    */
   VXG_KIND_VSOURCE = 2,     /* VoltageSource             [waveform rows]        */
   VXG_KIND_ISOURCE = 3,     /* CurrentSource             [waveform rows]        */
-  VXG_KIND_EKV = 4          /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w,
+  VXG_KIND_EKV = 4,         /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w,
                                      1/n, 1/(2 vt), c_ox n vt, -(n-1)/n] */
+  VXG_KIND_L1 = 5           /* Level1MOSFET [sign, kp W/L, vth, dvth, lam, gamma, phi,
+                                     smooth, cov_w, sqrt(phi), 1/(2 sqrt(phi)),
+                                     1/smooth or 0] */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 
@@ -66,6 +69,7 @@ enum {
 };
 
 #define VXG_MAX_GROUPS 32
+#define VXG_MAX_PARAM_ROWS 13 /* parameter rows of one group */
 
 /* One element group (voltax/circuit.py:30-159 layout, voltax/element.py:66-131). */
 typedef struct {

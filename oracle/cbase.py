@@ -63,7 +63,7 @@ def lib():
 
 
 KINDS = {"Resistor": 0, "Conductance": 0, "Capacitor": 1, "VoltageSource": 2,
-         "CurrentSource": 3, "EKVMOSFET": 4}
+         "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5}
 WAVES = {"Constant": 0, "Step": 1, "Pulse": 2}
 
 
@@ -100,6 +100,15 @@ def _rows_of(el, b):
         full = lambda x: torch.as_tensor(x, dtype=torch.float64).expand(n)  # noqa: E731
         return [full(sign), i_spec, full(p.vth), inst(el.dvth).expand(n), full(nn), full(vt),
                 full(p.lam), torch.exp(torch.as_tensor(p.log_cox).double()) * w * l,
+                torch.exp(torch.as_tensor(p.log_cov).double()) * w]
+    if name == "Level1MOSFET":  # voltax/elements/mosfet.py:208-257
+        p = el.process
+        w, l = torch.exp(inst(el.log_w)), torch.exp(inst(el.log_l))
+        kp = torch.exp(torch.as_tensor(p.log_kp).double())
+        sign = 1.0 if el.polarity == "n" else -1.0
+        full = lambda x: torch.as_tensor(x, dtype=torch.float64).expand(n)  # noqa: E731
+        return [full(sign), kp * (w / l), full(p.vth), inst(el.dvth).expand(n), full(p.lam),
+                full(p.gamma), full(p.phi), full(float(el.smooth)),
                 torch.exp(torch.as_tensor(p.log_cov).double()) * w]
     raise NotImplementedError(name)
 

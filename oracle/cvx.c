@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4 };
+enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5 };
 enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
 enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
 
@@ -164,6 +164,87 @@ static void ekv(const cvx_group* g, int d, const double* v, double cf, double cq
   }
 }
 
+/* Level 1 MOSFET (voltax/elements/mosfet.py:208-257); max/min split the
+ * derivative 1/2 : 1/2 at a tie, as jnp.maximum / jnp.minimum do. Rows: sign,
+ * kp W/L, vth, dvth, lam, gamma, phi, smooth, cov W (then derived rows). */
+static double tie_gt(double a, double b) { return a > b ? 1.0 : (a == b ? 0.5 : 0.0); }
+
+static void l1_vt(double vsb, double vt0, double gamma, double phi, double* vt, double* dvt) {
+  if (gamma == 0.0) { *vt = vt0; *dvt = 0.0; return; }
+  const double sphi = sqrt(phi);
+  double root, droot;
+  if (vsb >= 0.0) {
+    root = sqrt(phi + fmax(vsb, 0.0));
+    droot = tie_gt(vsb, 0.0) * 0.5 / root;
+  } else {
+    const double lin = sphi + vsb / (2.0 * sphi);
+    root = fmax(lin, 0.0);
+    droot = tie_gt(lin, 0.0) / (2.0 * sphi);
+  }
+  *vt = vt0 + gamma * (root - sphi);
+  *dvt = gamma * droot;
+}
+
+static void l1_side(double vgs, double vds, double vt, double k, double lam, double s,
+                    double* f, double* fgs, double* fds) {
+  const double x = vgs - vt;
+  double vov, dvov;
+  if (s > 0.0) {
+    double sp, sg;
+    softplus2(x / s, &sp, &sg);
+    vov = s * sp;
+    dvov = sg;
+  } else {
+    vov = fmax(x, 0.0);
+    dvov = tie_gt(x, 0.0);
+  }
+  const double vde = fmin(vds, vov);
+  const double dde_ds = tie_gt(vov, vds), dde_dov = tie_gt(vds, vov);
+  const double m = 1.0 + lam * vds;
+  *f = k * (vov - 0.5 * vde) * vde * m;
+  const double df_ov = k * vde * m, df_de = k * (vov - vde) * m;
+  *fgs = (df_ov + df_de * dde_dov) * dvov;
+  *fds = k * (vov - 0.5 * vde) * vde * lam + df_de * dde_ds;
+}
+
+static void level1(const cvx_group* g, int d, const double* v, double cf, double cq,
+                   double* I, double* Q, double* J) {
+  const double* p = g->params;
+  const int n = g->n;
+  const double sign = p[d], k = p[n + d], vt0 = p[2 * n + d] + p[3 * n + d];
+  const double lam = p[4 * n + d], gamma = p[5 * n + d], phi = p[6 * n + d];
+  const double sm = p[7 * n + d], cov_w = p[8 * n + d];
+  const double vd = sign * v[0], vg = sign * v[1], vs = sign * v[2], vb = sign * v[3];
+  const double vds = vd - vs;
+  const double dp = tie_gt(vds, 0.0), dn = tie_gt(-vds, 0.0);
+  double vtf, dvtf, vtr, dvtr, F, Fgs, Fds, R, Rgs, Rds;
+  l1_vt(vs - vb, vt0, gamma, phi, &vtf, &dvtf);
+  l1_vt(vd - vb, vt0, gamma, phi, &vtr, &dvtr);
+  l1_side(vg - vs, fmax(vds, 0.0), vtf, k, lam, sm, &F, &Fgs, &Fds);
+  l1_side(vg - vd, fmax(-vds, 0.0), vtr, k, lam, sm, &R, &Rgs, &Rds);
+  const double ids = F - R;
+  const double gi[4] = {Fds * dp + Rgs + Rds * dn + Rgs * dvtr, Fgs - Rgs,
+                        -Fgs - Fds * dp - Fgs * dvtf - Rds * dn, Fgs * dvtf - Rgs * dvtr};
+  I[0] = sign * ids;
+  I[1] = 0.0;
+  I[2] = sign * -ids;
+  I[3] = 0.0;
+  const double q_gs = cov_w * (v[1] - v[2]), q_gd = cov_w * (v[1] - v[0]);
+  Q[0] = -q_gd;
+  Q[1] = q_gs + q_gd;
+  Q[2] = -q_gs;
+  Q[3] = 0.0;
+  const double dq0[4] = {cov_w, -cov_w, 0.0, 0.0};
+  const double dq1[4] = {-cov_w, 2.0 * cov_w, -cov_w, 0.0};
+  const double dq2[4] = {0.0, -cov_w, cov_w, 0.0};
+  for (int kk = 0; kk < 4; ++kk) {
+    J[0 * 4 + kk] = cf * gi[kk] + cq * dq0[kk];
+    J[1 * 4 + kk] = cq * dq1[kk];
+    J[2 * 4 + kk] = cf * -gi[kk] + cq * dq2[kk];
+    J[3 * 4 + kk] = 0.0;
+  }
+}
+
 /* f (cf_on), q and the CSR Jacobian (cf df + cq dq + gmin on node diagonals) */
 static void stamp(const cvx_sys* s, const double* z, double t, double cf, double cq,
                   double gmin, double* f, double* q, double* data) {
@@ -216,6 +297,9 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
         }
         case K_EKV:
           ekv(g, d, u, cf, cq, data != 0, I, Q, J);
+          break;
+        case K_L1:
+          level1(g, d, u, cf, cq, I, Q, J);
           break;
       }
       for (int i = 0; i < m; ++i) {

@@ -8,6 +8,7 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * Conductance         voltax/elements/behavioral.py:78-99
 * VoltageSource       voltax/elements/sources.py:85-87
 * CurrentSource       voltax/elements/sources.py:110-112
+* Level1MOSFET        voltax/elements/mosfet.py:208-257
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
                       ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
 * Constant/Step/Pulse voltax/signals.py:58-114
@@ -64,6 +65,15 @@ def signal_value(sig, t, b):
     raise NotImplementedError(name)
 
 
+def _jmax(a, b):
+    """max with the derivative split 1/2 : 1/2 at a tie (jnp.maximum)."""
+    return torch.where(a > b, a, torch.where(a < b, b, 0.5 * (a + b)))
+
+
+def _jmin(a, b):
+    return torch.where(a < b, a, torch.where(a > b, b, 0.5 * (a + b)))
+
+
 class GroupModel:
     """One element group of one circuit instance."""
 
@@ -72,7 +82,7 @@ class GroupModel:
         self.name = type(el).__name__
         self.T = len(el.terminals)
         self.K = el.n_internal
-        self.has_charges = self.name in ("Capacitor", "EKVMOSFET")
+        self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -101,10 +111,11 @@ class GroupModel:
         if name == "CurrentSource":
             i = torch.broadcast_to(signal_value(el.value, t, b), v.shape[:1])
             return torch.stack([i, -i], -1), None
-        if name == "EKVMOSFET":
+        if name in ("EKVMOSFET", "Level1MOSFET"):
             s = self._sign()
             vd, vg, vs, vb = (s * v[..., k] for k in range(4))
-            ids = self._drain_current(vd, vg, vs, vb)
+            ids = (self._drain_current(vd, vg, vs, vb) if name == "EKVMOSFET"
+                   else self._l1_current(vd, vg, vs, vb))
             zero = torch.zeros_like(ids)
             return s * torch.stack([ids, zero, -ids, zero], -1), None
         raise NotImplementedError(name)
@@ -137,6 +148,14 @@ class GroupModel:
             q_gs, q_gd = cov * (vg - vs), cov * (vg - vd)
             overlap = torch.stack([-q_gd, q_gs + q_gd, -q_gs, torch.zeros_like(q_gs)], -1)
             return s * (intrinsic + overlap), None
+        if name == "Level1MOSFET":  # overlap charges only (mosfet.py:255-257)
+            s = self._sign()
+            vd, vg, vs, vb = (s * v[..., k] for k in range(4))
+            w = torch.exp(_inst(el.log_w, b))
+            cov = torch.exp(_np(el.process.log_cov)) * w
+            q_gs, q_gd = cov * (vg - vs), cov * (vg - vd)
+            overlap = torch.stack([-q_gd, q_gs + q_gd, -q_gs, torch.zeros_like(q_gs)], -1)
+            return s * overlap, None
         return None, None
 
     def _sign(self):
@@ -150,6 +169,38 @@ class GroupModel:
         i_f = softplus((vp - (vs - vb)) / (2 * vt)) ** 2
         i_r = softplus((vp - (vd - vb)) / (2 * vt)) ** 2
         return i_f, i_r
+
+    # Level 1 (mosfet.py:229-253). jnp.maximum / jnp.minimum give each side
+    # half the derivative at a tie; _jmax / _jmin do the same under torch AD.
+    def _l1_threshold(self, vsb):
+        el, b = self.el, self.b
+        p = el.process
+        phi, gamma = _np(p.phi), _np(p.gamma)
+        sphi = torch.sqrt(torch.as_tensor(phi, dtype=F64))
+        zero = torch.zeros_like(vsb)
+        reverse = torch.sqrt(phi + _jmax(vsb, zero))
+        forward = _jmax(sphi + _jmin(vsb, zero) / (2 * sphi), zero)
+        root = torch.where(vsb >= 0, reverse, forward)
+        return _np(p.vth) + _inst(el.dvth, b) + gamma * (root - sphi)
+
+    def _l1_forward(self, vgs, vds, vth):
+        el, b = self.el, self.b
+        p, sm = el.process, el.smooth
+        k = torch.exp(_np(p.log_kp)) * torch.exp(_inst(el.log_w, b)) / torch.exp(
+            _inst(el.log_l, b))
+        if sm > 0:
+            vov = sm * softplus((vgs - vth) / sm)
+        else:
+            vov = _jmax(vgs - vth, torch.zeros_like(vgs))
+        vde = _jmin(vds, vov)
+        return k * (vov - 0.5 * vde) * vde * (1.0 + _np(p.lam) * vds)
+
+    def _l1_current(self, vd, vg, vs, vb):
+        vds = vd - vs
+        zero = torch.zeros_like(vds)
+        fwd = self._l1_forward(vg - vs, _jmax(vds, zero), self._l1_threshold(vs - vb))
+        rev = self._l1_forward(vg - vd, _jmax(-vds, zero), self._l1_threshold(vd - vb))
+        return fwd - rev
 
     def _drain_current(self, vd, vg, vs, vb):
         el, b = self.el, self.b

@@ -44,6 +44,8 @@ CIRCUITS = {
     "grid": lambda: workloads.power_grid(10, seed=3),
     "adder": lambda: workloads.mirror_adder(2),
     "ring": lambda: workloads.ring_oscillator(9)[0],
+    "ring_l1": lambda: workloads.ring_oscillator_level1(5, gamma=0.3)[0],
+    "ring_l1_smooth": lambda: workloads.ring_oscillator_level1(5, smooth=0.02, gamma=0.3)[0],
 }
 LINEAR = ("rc_ladder", "grid")
 
@@ -164,6 +166,61 @@ def test_ring_transient_matches_oracle(method, precision, engine):
     assert np.max(np.abs(v[:, : c.n_nodes] - vr[:, : c.n_nodes])) < 1e-9
     if precision == "f64":
         assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("engine", ENGINES)
+def test_level1_ring_transient_matches_oracle(precision, engine):
+    """The reference's own ring benchmark circuit (exact Level 1, body
+    effect on, backward Euler): node voltages and Newton iterations."""
+    c, nodes = workloads.ring_oscillator_level1(9, gamma=0.3)
+    z0 = workloads.ring_level1_initial_state(c, nodes)
+    ts = np.linspace(0.0, 40e-12, 41)
+    sol = vx.transient(c, ts, ic=z0, method="be",
+                       options=vx.Options(precision=precision, engine=engine))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic=z0.numpy(), method="be")
+    assert bool(sol.converged.all()) and okr.all()
+    v = sol.z.cpu().numpy()
+    assert np.max(np.abs(v[:, : c.n_nodes] - zr[:, : c.n_nodes])) < 1e-9
+    if precision == "f64":
+        assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+def test_level1_dc_gradient_matches_finite_differences():
+    """Parameter VJP of the Level-1 kernel (dual numbers) through the DC
+    adjoint: d v(out) / d (dvth, log W) of an inverter with body effect."""
+    import functools
+    from voltax_gb300.elements import Level1MOSFET, MOSProcess
+    b = CircuitBuilder(nmos=MOSProcess.nmos(gamma=0.4), pmos=MOSProcess.pmos(gamma=0.4),
+                       mos_model=functools.partial(Level1MOSFET, smooth=0.02))
+    b.vsource("vdd", "0", 1.2, name="Vdd")
+    b.vsource("in", "0", 0.55, name="Vin")
+    b.resistor("vdd", "src", 2e3, name="Rs")
+    b.nmos("out", "in", "src2", "0", w=2e-6, name="Mn")
+    b.resistor("src2", "0", 1e3, name="Rdeg")
+    b.pmos("out", "in", "vdd", "vdd", w=2e-6, name="Mp")
+    c = b.build()
+    out = c.node("out")
+
+    def v_out(c2):
+        return vx.dc(c2).z[out]
+
+    for gname in ("Level1MOSFET_n", "Level1MOSFET_p"):
+        el = c.elements[gname]
+        for field in ("dvth", "log_w"):
+            e2 = el.with_nodes(el.nodes)
+            setattr(e2, field, getattr(el, field).clone().requires_grad_(True))
+            v_out(c.replace(gname, e2)).backward()
+            g = getattr(e2, field).grad.numpy()
+            h = 1e-6
+            e_p = el.with_nodes(el.nodes)
+            setattr(e_p, field, getattr(el, field).clone() + h)
+            e_m = el.with_nodes(el.nodes)
+            setattr(e_m, field, getattr(el, field).clone() - h)
+            fd = (float(v_out(c.replace(gname, e_p))) -
+                  float(v_out(c.replace(gname, e_m)))) / (2 * h)
+            np.testing.assert_allclose(g.sum(), fd, rtol=1e-5, atol=1e-9)
 
 
 def test_rc_ladder_recorded_values_on_gpu():

@@ -149,6 +149,7 @@ def _cases():
         "grid": lambda: workloads.power_grid(10, seed=3),
         "adder": lambda: workloads.mirror_adder(2),
         "ring": lambda: workloads.ring_oscillator(9)[0],
+        "ring_l1": lambda: workloads.ring_oscillator_level1(9, gamma=0.3)[0],
     }
 
 
@@ -217,7 +218,8 @@ def test_power_grid_dc_matches_superlu():
     np.testing.assert_allclose(z, ref, rtol=1e-9, atol=1e-12)
 
 
-@pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap")])
+@pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap"),
+                                         ("ring_l1", "be")])
 def test_compiled_baseline_matches_oracle(name, method):
     """oracle/cvx.c (the timed CPU baseline) equals the torch restatement."""
     from oracle import cbase
@@ -227,6 +229,9 @@ def test_compiled_baseline_matches_oracle(name, method):
     z0 = None
     if name == "ring":
         z0 = workloads.ring_initial_state(c, [f"n{k}" for k in range(9)]).numpy()
+    if name == "ring_l1":
+        z0 = workloads.ring_level1_initial_state(
+            c, [f"n{k}" for k in range(1, 10)]).numpy()
     zc, okc, itc = cbase.CSystem(c, st, st.plan).run(ts, z0=z0, method=method,
                                                       dc_first=z0 is None)
     zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc" if z0 is None else z0,
@@ -234,3 +239,34 @@ def test_compiled_baseline_matches_oracle(name, method):
     assert okc.all() and okr.all()
     assert np.array_equal(itc[1:], itr[1:])
     np.testing.assert_allclose(zc, zr, rtol=1e-10, atol=1e-12)
+
+
+def _l1(v, **kw):
+    m = od.GroupModel(el.Level1MOSFET((0, 1, 2, 3), **kw))
+    return m.currents(torch.tensor([v], dtype=torch.float64), None, 0.0)[0][0, 0].item()
+
+
+def test_level1_exact_square_law_and_body_effect():
+    """voltax tests/test_elements.py:222-231 (known answers)."""
+    p = el.MOSProcess.nmos(kp=100e-6, vth=0.5, lam=0.02, gamma=0.4, phi=0.7)
+    kw = dict(w=4e-6, l=1e-6, process=p, smooth=0.0)
+    k = 100e-6 * 4
+    assert np.isclose(_l1([2.0, 1.5, 0.0, 0.0], **kw), 0.5 * k * 1.0 * (1 + 0.04))
+    assert np.isclose(_l1([0.2, 1.5, 0.0, 0.0], **kw), k * (1.0 - 0.1) * 0.2 * 1.004)
+    assert _l1([1.0, 0.4, 0.0, 0.0], **kw) == 0.0
+    vth_body = 0.5 + 0.4 * (np.sqrt(0.7 + 0.5) - np.sqrt(0.7))
+    assert np.isclose(_l1([3.0, 2.0, 0.5, 0.0], **kw),
+                      0.5 * k * (1.5 - vth_body) ** 2 * (1 + 0.02 * 2.5))
+
+
+def test_level1_reverse_mode_smooth_and_pmos_mirror():
+    p = el.MOSProcess.nmos(kp=100e-6, vth=0.5, lam=0.02)
+    kw = dict(w=4e-6, l=1e-6, process=p, smooth=0.0)
+    # drain and source swap for vds < 0
+    assert np.isclose(_l1([0.0, 1.5, 0.3, 0.0], **kw), -_l1([0.3, 1.5, 0.0, 0.0], **kw))
+    # smoothing only matters near cutoff
+    assert np.isclose(_l1([1.0, 1.5, 0.0, 0.0], **{**kw, "smooth": 0.02}),
+                      _l1([1.0, 1.5, 0.0, 0.0], **kw), rtol=1e-6)
+    assert _l1([1.0, 0.5, 0.0, 0.0], **{**kw, "smooth": 0.02}) > 0.0
+    pm = dict(kw, polarity="p", process=el.MOSProcess.pmos(kp=100e-6, vth=0.5, lam=0.02))
+    assert np.isclose(_l1([-1.0, -1.5, 0.0, 0.0], **pm), -_l1([1.0, 1.5, 0.0, 0.0], **kw))

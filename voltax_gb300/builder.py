@@ -19,7 +19,7 @@ from .signals import Constant, Signal
 
 _PREFIX = {
     el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
-    el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M",
+    el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
 }
 
 
@@ -44,9 +44,10 @@ class CircuitBuilder:
     """
 
     def __init__(self, nmos: el.MOSProcess | None = None,
-                 pmos: el.MOSProcess | None = None):
+                 pmos: el.MOSProcess | None = None, mos_model=el.EKVMOSFET):
         self.nmos_process = nmos or el.MOSProcess.nmos()
         self.pmos_process = pmos or el.MOSProcess.pmos()
+        self.mos_model = mos_model  # EKVMOSFET, Level1MOSFET or a partial of one
         self._devices: list[tuple[str, Element, str | None]] = []
         self._names: set[str] = set()
         self._nodes: dict[str, None] = {}
@@ -112,14 +113,14 @@ class CircuitBuilder:
 
     def nmos(self, d, g, s, b=None, w=1e-6, l=0.13e-6, name=None, group=None,
              process=None, dvth=0.0) -> str:
-        dev = el.EKVMOSFET((d, g, s, s if b is None else b), w, l,
-                           process or self.nmos_process, "n", dvth)
+        dev = self.mos_model((d, g, s, s if b is None else b), w, l,
+                             process or self.nmos_process, "n", dvth)
         return self.add(dev, name, group)
 
     def pmos(self, d, g, s, b=None, w=1e-6, l=0.13e-6, name=None, group=None,
              process=None, dvth=0.0) -> str:
-        dev = el.EKVMOSFET((d, g, s, s if b is None else b), w, l,
-                           process or self.pmos_process, "p", dvth)
+        dev = self.mos_model((d, g, s, s if b is None else b), w, l,
+                             process or self.pmos_process, "p", dvth)
         return self.add(dev, name, group)
 
     # ---------------------------------------------------------------- build

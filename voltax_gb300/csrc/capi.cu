@@ -250,6 +250,10 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
   if (!d || !out || d->size <= 0 || d->n_groups < 0 || d->n_groups > VXG_MAX_GROUPS ||
       d->n_seg <= 0 || d->n_levels < 0)
     return VXG_ERR_INVALID;
+  for (int i = 0; i < d->n_groups; ++i)
+    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_L1 ||
+        d->groups[i].n_params < 0 || d->groups[i].n_params > VXG_MAX_PARAM_ROWS)
+      return VXG_ERR_INVALID;
   *out = nullptr;
   vxg_handle* h = new (std::nothrow) vxg_handle;
   if (!h) return VXG_ERR_ALLOC;

@@ -403,6 +403,128 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
   }
 }
 
+// Level 1 (Shichman-Hodges) MOSFET, smoothed (voltax/elements/mosfet.py:208-257):
+// I = F(vg - vs, max(vds, 0), vt(vs - vb)) - F(vg - vd, max(-vds, 0), vt(vd - vb)),
+// F = k (vov - vde/2) vde (1 + lam vds), vov = s softplus((vgs - vt)/s) (or
+// max(vgs - vt, 0) when s = 0), vde = min(vds, vov); vt with the body effect
+// linearised for a forward-biased bulk; overlap charges only. Like
+// jnp.maximum / jnp.minimum, max and min split the derivative 1/2 : 1/2 at
+// a tie (vds = 0 is a tie at every symmetric bias point).
+__device__ __forceinline__ double tie_gt(double a, double b) {  // d max(a, b) / da
+  return a > b ? 1.0 : (a == b ? 0.5 : 0.0);
+}
+
+// threshold and d threshold / d vsb
+__device__ __forceinline__ void l1_vt(double vsb, double vt0, double gamma, double phi,
+                                     double sphi, double inv2sphi, double* vt, double* dvt) {
+  if (gamma == 0.0) {
+    *vt = vt0;
+    *dvt = 0.0;
+    return;
+  }
+  double root, droot;
+  if (vsb >= 0.0) {
+    root = sqrt(phi + fmax(vsb, 0.0));
+    droot = tie_gt(vsb, 0.0) * 0.5 / root;
+  } else {
+    const double lin = sphi + vsb * inv2sphi;
+    root = fmax(lin, 0.0);
+    droot = tie_gt(lin, 0.0) * inv2sphi;
+  }
+  *vt = vt0 + gamma * (root - sphi);
+  *dvt = gamma * droot;
+}
+
+// F and its partials in (vgs, vds) (d/dvt = -d/dvgs)
+__device__ __forceinline__ void l1_side(double vgs, double vds, double vt, double k, double lam,
+                                       double s, double inv_s, double* f, double* fgs,
+                                       double* fds) {
+  const double x = vgs - vt;
+  double vov, dvov;
+  if (s > 0.0) {
+    double sp, sg;
+    softplus_and_sigmoid(x * inv_s, &sp, &sg);
+    vov = s * sp;
+    dvov = sg;
+  } else {
+    vov = fmax(x, 0.0);
+    dvov = tie_gt(x, 0.0);
+  }
+  const double vde = fmin(vds, vov);
+  const double dde_ds = tie_gt(vov, vds), dde_dov = tie_gt(vds, vov);
+  const double m = 1.0 + lam * vds;
+  *f = k * (vov - 0.5 * vde) * vde * m;
+  const double df_ov = k * vde * m, df_de = k * (vov - vde) * m;
+  *fgs = (df_ov + df_de * dde_dov) * dvov;
+  *fds = k * (vov - 0.5 * vde) * vde * lam + df_de * dde_ds;
+}
+
+template <typename JT>
+__device__ __forceinline__ void l1_soa(const GroupDev& g, int b, int d, const double* u,
+                                       double cf, double cq, bool wf, bool wq, bool wj,
+                                       double* fo, double* qo, JT* jo) {
+  const int n = g.n;
+  const bool neg = prm(g, 0, b, d) < 0.0;
+  const double cov_w = prm(g, 8, b, d);
+  const bool need_i = wf || (wj && cf != 0.0);
+  double I = 0.0, gd = 0.0, gg = 0.0, gs = 0.0, gb = 0.0;
+  if (need_i) {
+    const double k = prm(g, 1, b, d), vt0 = prm(g, 2, b, d) + prm(g, 3, b, d);
+    const double lam = prm(g, 4, b, d), gamma = prm(g, 5, b, d), phi = prm(g, 6, b, d);
+    const double sm = prm(g, 7, b, d), sphi = prm(g, 9, b, d), inv2sphi = prm(g, 10, b, d);
+    const double inv_s = prm(g, 11, b, d);
+    const double vd = neg ? -u[0] : u[0], vg = neg ? -u[1] : u[1];
+    const double vs = neg ? -u[2] : u[2], vb = neg ? -u[3] : u[3];
+    const double vds = vd - vs;
+    const double dp = tie_gt(vds, 0.0), dn = tie_gt(-vds, 0.0);
+    double vtf, dvtf, vtr, dvtr, F, Fgs, Fds, R, Rgs, Rds;
+    l1_vt(vs - vb, vt0, gamma, phi, sphi, inv2sphi, &vtf, &dvtf);
+    l1_vt(vd - vb, vt0, gamma, phi, sphi, inv2sphi, &vtr, &dvtr);
+    l1_side(vg - vs, fmax(vds, 0.0), vtf, k, lam, sm, inv_s, &F, &Fgs, &Fds);
+    l1_side(vg - vd, fmax(-vds, 0.0), vtr, k, lam, sm, inv_s, &R, &Rgs, &Rds);
+    I = F - R;
+    gd = Fds * dp + Rgs + Rds * dn + Rgs * dvtr;
+    gg = Fgs - Rgs;
+    gs = -Fgs - Fds * dp - Fgs * dvtf - Rds * dn;
+    gb = Fgs * dvtf - Rgs * dvtr;
+  }
+  if (wf) {
+    fo[0 * n + d] = neg ? -I : I;
+    fo[1 * n + d] = 0.0;
+    fo[2 * n + d] = neg ? I : -I;
+    fo[3 * n + d] = 0.0;
+  }
+  if (wq) {
+    const double q_gs = cov_w * (u[1] - u[2]), q_gd = cov_w * (u[1] - u[0]);
+    qo[0 * n + d] = -q_gd;
+    qo[1 * n + d] = q_gs + q_gd;
+    qo[2 * n + d] = -q_gs;
+    qo[3 * n + d] = 0.0;
+  }
+  if (!wj) return;
+  const JT ji[4] = {(JT)gd, (JT)gg, (JT)gs, (JT)gb};
+  const JT cw = (JT)cov_w;
+  const JT dq0[4] = {cw, -cw, JT(0), JT(0)};
+  const JT dq1[4] = {-cw, JT(2) * cw, -cw, JT(0)};
+  const JT dq2[4] = {JT(0), -cw, cw, JT(0)};
+  const JT cfj = (JT)cf, cqj = (JT)cq;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    JT r0 = cf != 0.0 ? cfj * ji[j] : JT(0);
+    JT r2 = cf != 0.0 ? cfj * -ji[j] : JT(0);
+    JT r1 = JT(0);
+    if (cq != 0.0) {
+      r0 = r0 + cqj * dq0[j];
+      r1 = r1 + cqj * dq1[j];
+      r2 = r2 + cqj * dq2[j];
+    }
+    jo[(0 * 4 + j) * n + d] = r0;
+    jo[(1 * 4 + j) * n + d] = r1;
+    jo[(2 * 4 + j) * n + d] = r2;
+    jo[(3 * 4 + j) * n + d] = JT(0);
+  }
+}
+
 // Evaluate device d of group g (instance b) reading state zz; write its slots.
 // fo/qo/jo point at the group's first slot in each contribution array.
 // u: the device's local unknowns (terminal voltages, then internals).
@@ -494,6 +616,9 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
     }
     case VXG_KIND_EKV:
       ekv_soa<JT>(g, b, d, u, cf, cq, wf, wq, wj, fo, qo, jo);
+      break;
+    case VXG_KIND_L1:
+      l1_soa<JT>(g, b, d, u, cf, cq, wf, wq, wj, fo, qo, jo);
       break;
   }
 }

@@ -183,6 +183,33 @@ __device__ Dual dwave(int wave, const Dual* p, double t) {
 }
 
 // Outputs (cf I + cq Q) of one device with dual parameters.
+// max / min with the derivative split 1/2 : 1/2 at a tie (jnp.maximum)
+__device__ __forceinline__ Dual dmax_tie(Dual a, Dual b) {
+  if (a.v > b.v) return a;
+  if (a.v < b.v) return b;
+  return {a.v, 0.5 * (a.d + b.d)};
+}
+__device__ __forceinline__ Dual dmin_tie(Dual a, Dual b) {
+  if (a.v < b.v) return a;
+  if (a.v > b.v) return b;
+  return {a.v, 0.5 * (a.d + b.d)};
+}
+
+// Level 1 threshold and one side of the drain current in parameter duals
+// (voltax/elements/mosfet.py:229-247)
+__device__ Dual l1_dual_vt(double vsb, Dual vt0, Dual gamma, Dual phi) {
+  if (gamma.v == 0.0 && gamma.d == 0.0) return vt0;
+  const Dual sphi = dsqrt(phi);
+  const Dual root = vsb >= 0.0 ? dsqrt(phi + mk(fmax(vsb, 0.0)))
+                               : dmax_tie(sphi + mk(fmin(vsb, 0.0)) / (2.0 * sphi), mk(0.0));
+  return vt0 + gamma * (root - sphi);
+}
+__device__ Dual l1_dual_side(Dual vgs, Dual vds, Dual vt, Dual k, Dual lam, double s) {
+  const Dual vov = s > 0.0 ? s * dsoftplus((vgs - vt) / mk(s)) : dmax_tie(vgs - vt, mk(0.0));
+  const Dual vde = dmin_tie(vds, vov);
+  return k * (vov - 0.5 * vde) * vde * (1.0 + lam * vds);
+}
+
 __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, double t,
                              double cf, double cq, Dual* out) {
   for (int i = 0; i < g.m; ++i) out[i] = mk(0.0);
@@ -247,6 +274,30 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
         out[1] = out[1] + cq * (sign * (q_g + (q_gs + q_gd)));
         out[2] = out[2] + cq * (sign * (q_s - q_gs));
         out[3] = out[3] + cq * (sign * q_b);
+      }
+      break;
+    }
+    case VXG_KIND_L1: {
+      const double sign = p[0].v;
+      const Dual k = p[1], vt0 = p[2] + p[3], lam = p[4], gamma = p[5], phi = p[6];
+      const double s = p[7].v;
+      const Dual cov_w = p[8];
+      const double vd = sign * u[0], vg = sign * u[1], vs = sign * u[2], vb = sign * u[3];
+      if (cf != 0.0) {
+        const Dual vds = mk(vd - vs);
+        const Dual f = l1_dual_side(mk(vg - vs), dmax_tie(vds, mk(0.0)),
+                                    l1_dual_vt(vs - vb, vt0, gamma, phi), k, lam, s);
+        const Dual r = l1_dual_side(mk(vg - vd), dmax_tie(-vds, mk(0.0)),
+                                    l1_dual_vt(vd - vb, vt0, gamma, phi), k, lam, s);
+        const Dual ids = f - r;
+        out[0] = cf * (sign * ids);
+        out[2] = cf * (sign * (-ids));
+      }
+      if (cq != 0.0) {
+        const Dual q_gs = cov_w * mk(u[1] - u[2]), q_gd = cov_w * mk(u[1] - u[0]);
+        out[0] = out[0] + cq * (-q_gd);
+        out[1] = out[1] + cq * (q_gs + q_gd);
+        out[2] = out[2] + cq * (-q_gs);
       }
       break;
     }

@@ -36,6 +36,7 @@ KIND_CAPACITOR = 1
 KIND_VSOURCE = 2
 KIND_ISOURCE = 3
 KIND_EKV = 4
+KIND_L1 = 5
 
 
 def _t(x) -> torch.Tensor:
@@ -457,5 +458,46 @@ class EKVMOSFET(Element):
                 full(-(p.n - 1.0) / p.n)]
 
 
+class Level1MOSFET(EKVMOSFET):
+    """Shichman-Hodges (SPICE Level 1) square-law MOSFET, smoothed
+    (mosfet.py:208-257); terminals ``(d, g, s, b)``.
+
+    ``I_ds = kp (W/L) (v_ov v_ds - v_ds^2/2)`` in triode and
+    ``kp (W/L) v_ov^2 / 2`` in saturation, times ``(1 + lam v_ds)``, with
+    ``v_ov = smooth softplus((v_gs - v_t)/smooth)`` (``smooth=0``: the exact
+    SPICE model), drain and source swapped for ``v_ds < 0``, the body effect
+    ``gamma (sqrt(phi + v_sb) - sqrt(phi))`` linearised under forward bias,
+    and overlap charges only.
+
+    Kernel parameter rows (per device): sign, kp W/L, vth, dvth, lam, gamma,
+    phi, smooth, cov W, then the derived sqrt(phi), 1/(2 sqrt(phi)) and
+    1/smooth (0 when smooth = 0).
+    """
+
+    static = ("polarity", "smooth")
+    kind = KIND_L1
+
+    def __init__(self, nodes, w=1e-6, l=0.13e-6, process: MOSProcess | None = None,
+                 polarity: str = "n", dvth=0.0, smooth: float = 0.02):
+        super().__init__(nodes, w, l, process, polarity, dvth)
+        self.smooth = float(smooth)
+
+    def gpu_params(self):
+        p = self.process
+        w, l = self.w, self.l
+        k = p.kp * (w / l)
+        shape = k.shape
+
+        def full(x):
+            return _t(x).expand(shape)
+
+        sphi = torch.sqrt(p.phi)
+        # rows 9-11 are derived from rows 6 and 7 so the kernel multiplies
+        # instead of dividing; gradients flow through rows 0-8
+        return [full(self.sign), k, full(p.vth), self.dvth.expand(shape), full(p.lam),
+                full(p.gamma), full(p.phi), full(self.smooth), p.cov * w, full(sphi),
+                full(0.5 / sphi), full(1.0 / self.smooth if self.smooth > 0 else 0.0)]
+
+
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
-                 EKVMOSFET)
+                 EKVMOSFET, Level1MOSFET)

@@ -12,6 +12,8 @@ All draws use ``numpy.random.default_rng(seed)``.
 * `ring_oscillator(stages)`: CMOS ring of EKV inverters (NMOS w=1u, PMOS
   w=2u, l=0.13u), VDD 1.2 V, 5 fF per stage; `ring_initial_state` gives the
   alternating rail pattern with a 0.1 V kick on node 0.
+* `ring_oscillator_level1(stages)`: the reference's own ring benchmark
+  circuit (exact Level-1 devices) with its alternating initial state.
 * `mirror_adder_mc(instances)`: 4-bit ripple-carry adder of 28-transistor
   mirror full adders, per-device ``dvth ~ N(0, 30 mV)`` and
   ``log W += N(0, 0.05)``; A and B step 0000 -> 1111 with 20 ps edges.
@@ -19,10 +21,13 @@ All draws use ``numpy.random.default_rng(seed)``.
 
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 import torch
 
 from .builder import CircuitBuilder
+from .elements import Level1MOSFET, MOSProcess
 from .library import cmos
 from .signals import Step
 
@@ -99,6 +104,30 @@ def ring_initial_state(circuit, nodes, kick: float = 0.1) -> torch.Tensor:
     """Alternating rails (node k at VDD for odd k) with node 0 at `kick`."""
     v = {"vdd": VDD, **{nd: VDD * (k % 2) for k, nd in enumerate(nodes)}}
     v[nodes[0]] = kick
+    return circuit.state(v=v)
+
+
+def ring_oscillator_level1(stages: int = 101, smooth: float = 0.0, gamma: float = 0.0,
+                           cload: float = 5e-15):
+    """The ring of voltax/benchmarks/benchmark_ring_oscillator.py:52-64:
+    exact Level-1 inverters (``smooth=0``; NMOS kp 400 uA/V^2, PMOS
+    200 uA/V^2, vth 0.4 V, lam 0.04/V, overlap 0.3 nF/m; W 0.4 / 0.8 um,
+    L 0.13 um), 5 fF per stage, VDD 1.2 V; nodes ``n1 .. n<stages>``."""
+    extra = dict(vth=0.4, lam=0.04, cov=0.3e-9, gamma=gamma)
+    b = CircuitBuilder(nmos=MOSProcess.nmos(kp=400e-6, **extra),
+                       pmos=MOSProcess.pmos(kp=200e-6, **extra),
+                       mos_model=functools.partial(Level1MOSFET, smooth=smooth))
+    b.vsource("vdd", "0", VDD, name="Vdd")
+    nodes = [f"n{k}" for k in range(1, stages + 1)]
+    cmos.ring_oscillator(b, nodes, "vdd", wn=0.4e-6, wp=0.8e-6)
+    for nd in nodes:
+        b.capacitor(nd, "0", cload)
+    return b.build(), nodes
+
+
+def ring_level1_initial_state(circuit, nodes) -> torch.Tensor:
+    """Alternating 0.9 / 0.1 VDD (voltax/benchmarks/benchmark_ring_oscillator.py:44-49)."""
+    v = {"vdd": VDD, **{nd: (0.9 if k % 2 == 0 else 0.1) * VDD for k, nd in enumerate(nodes)}}
     return circuit.state(v=v)
 
 
