@@ -1,0 +1,119 @@
+"""dc_sweep (continuation) and time_grid, after voltax tests/test_analysis.py:262-308."""
+
+import numpy as np
+import pytest
+import torch
+
+import voltax_gb300 as vx
+from voltax_gb300.builder import CircuitBuilder
+from voltax_gb300.signals import Pulse
+
+
+def _rc_pulse():
+    b = CircuitBuilder()
+    b.vsource("in", "0", Pulse(0, 1, delay=1e-9, rise=1e-11, fall=1e-11, width=4e-9,
+                               period=10e-9), name="Vin")
+    b.resistor("in", "out", 1e3, name="R1")
+    b.capacitor("out", "0", 1e-13, name="C1")
+    return b.build()
+
+
+def test_time_grid_resolves_edges():
+    """voltax tests/test_analysis.py:291-302 (the grid part)."""
+    grid = vx.time_grid(_rc_pulse(), 6e-9, dt_max=0.5e-9)
+    steps = np.diff(grid)
+    assert grid[0] == 0 and np.isclose(grid[-1], 6e-9) and steps.max() <= 0.5e-9 * (1 + 1e-12)
+    assert np.all(steps > 0)
+    on_ramp = (grid >= 1e-9) & (grid <= 1.01e-9)
+    assert on_ramp.sum() >= 11  # >= 10 steps across the 10 ps edge
+    assert len(grid) < 200
+
+
+def _crossing(t, y, level, after=-np.inf):
+    for i in range(len(t) - 1):
+        if t[i + 1] <= after:
+            continue
+        a, b = y[i] - level, y[i + 1] - level
+        if a == 0 or a * b < 0:
+            return t[i] + (t[i + 1] - t[i]) * (a / (a - b))
+    return np.nan
+
+
+@pytest.mark.gpu
+def test_time_grid_transient_delay_matches_fine_grid():
+    """voltax tests/test_analysis.py:303-308: the 50 % delay on the refined
+    grid equals the one on a uniform 100 fs grid within 0.5 %."""
+    c = _rc_pulse()
+    grid = vx.time_grid(c, 6e-9, dt_max=0.5e-9)
+
+    def delay(ts):
+        sol = vx.transient(c, ts, method="trap")
+        vin, vout = sol.v("in").cpu().numpy(), sol.v("out").cpu().numpy()
+        t0 = _crossing(ts, vin, 0.5)
+        return _crossing(ts, vout, 0.5, after=t0) - t0
+
+    fine = np.linspace(0, 6e-9, 60001)
+    assert np.isclose(delay(grid), delay(fine), rtol=5e-3)
+
+
+def _rc_ladder():
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.resistor("in", "a", 1e3, name="R1")
+    b.resistor("a", "out", 2e3, name="R2")
+    b.resistor("out", "0", 1e4, name="Rload")
+    return b.build()
+
+
+@pytest.mark.gpu
+def test_dc_sweep_with_callable_and_gradient():
+    """voltax tests/test_analysis.py:276-288."""
+    c = _rc_ladder()
+
+    def out_sum(log_r):
+        sweep = vx.dc_sweep(c, [1e3, 1e4],
+                            lambda cc, r: cc.set("Rload", r=r * torch.exp(log_r)))
+        return sweep.v("out").sum()
+
+    expected = sum(r / (r + 3e3) for r in (1e3, 1e4))
+    x = torch.zeros((), dtype=torch.float64, requires_grad=True)
+    val = out_sum(x)
+    assert np.isclose(float(val), expected)
+    val.backward()
+    h = 1e-6
+    fd = (float(out_sum(torch.tensor(h, dtype=torch.float64))) -
+          float(out_sum(torch.tensor(-h, dtype=torch.float64)))) / (2 * h)
+    assert np.isclose(float(x.grad), fd, rtol=1e-5)
+
+
+def _latch():
+    """Cross-coupled CMOS inverters; the input drives node a through 600 Ohm,
+    so the latch keeps its state until the input overpowers it (the oracle
+    switches between 0.9 and 1.0 V going up, 0.4 and 0.3 V going down)."""
+    b = CircuitBuilder()
+    b.vsource("vdd", "0", 1.2, name="Vdd")
+    b.vsource("in", "0", 0.0, name="Vin")
+    b.resistor("in", "a", 600.0, name="Rin")
+    from voltax_gb300.library import cmos
+    cmos.inverter(b, "a", "q", "vdd")
+    cmos.inverter(b, "q", "a", "vdd")
+    return b.build()
+
+
+@pytest.mark.gpu
+def test_dc_sweep_follows_branches_and_shows_hysteresis():
+    """voltax tests/test_analysis.py:262-273 with a CMOS latch."""
+    c = _latch()
+    vin = np.linspace(0.0, 1.2, 49)
+    up = vx.dc_sweep(c, vin, "Vin")
+    down = vx.dc_sweep(c, vin[::-1], "Vin", guess=up.z[-1])
+    assert bool(up.converged.all()) and bool(down.converged.all())
+    assert np.allclose(up.t.numpy(), vin)
+    q_up, q_down = up.v("q").cpu().numpy(), down.v("q").cpu().numpy()[::-1]
+    assert q_up[0] > 1.1 and q_up[-1] < 0.1  # the input wins at both ends
+    mid = len(vin) // 2
+    assert q_up[mid] > 1.0 and q_down[mid] < 0.2  # two stable states at VDD/2
+    # every point is a DC operating point of its own input (no branch mixing)
+    for k in (5, mid, 40):
+        s = vx.dc(c.set("Vin", value=float(vin[k])), guess=up.z[k])
+        assert float((s.z - up.z[k]).abs().max()) < 1e-9

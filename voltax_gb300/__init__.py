@@ -8,7 +8,7 @@ refactorization under a reused symbolic plan, and level-scheduled
 """
 
 from . import library, signals, sparse, workloads  # noqa: F401
-from .analysis import Options, Solution, dc, transient  # noqa: F401
+from .analysis import Options, Solution, dc, dc_sweep, time_grid, transient  # noqa: F401
 from .builder import CircuitBuilder  # noqa: F401
 from .circuit import Circuit, Layout  # noqa: F401
 from .elements import (VT_300K, Capacitor, Conductance, CurrentSource,  # noqa: F401

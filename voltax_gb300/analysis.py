@@ -467,3 +467,65 @@ def transient(circuit, ts, ic="dc", method: str = "be",
     if circuit.batch == 1:
         return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])
     return Solution(tt, z_out.permute(1, 0, 2), conv.T.bool(), circuit.layout, iters.T)
+
+
+# =============================================================================
+# Sweeps and time grids
+# =============================================================================
+
+
+def dc_sweep(circuit, values, apply, t: float = 0.0, guess=None,
+             options: Options = Options()) -> Solution:
+    """DC sweep with continuation (SPICE ``.dc``, voltax/analysis.py:530-568):
+    point k starts Newton from point k-1's operating point, so one solution
+    branch is followed (hysteresis shows when sweeping up and down).
+
+    `apply` is a source name (its DC value is set) or ``fn(circuit, value)``.
+    Returns a `Solution` whose ``t`` holds the sweep values and whose ``z``
+    has the sweep axis first. Each point is one Newton launch on the GPU,
+    warm-started from the previous state left on the device."""
+    if isinstance(apply, str):
+        device = apply
+        apply = lambda c, v: c.set(device, value=v)  # noqa: E731
+    vals = torch.as_tensor(np.asarray(values, dtype=np.float64))
+    z = guess
+    zs, oks, its = [], [], []
+    for v in vals:
+        sol = dc(apply(circuit, float(v)), t, guess=z, options=options)
+        z = sol.z
+        zs.append(sol.z)
+        oks.append(sol.converged)
+        its.append(sol.iterations)
+    return Solution(vals, torch.stack(zs), torch.stack(oks), circuit.layout,
+                    torch.stack(its))
+
+
+def time_grid(circuit, t_stop: float, dt_max: float, dt_min: float | None = None,
+              ramp_points: int = 10, growth: float = 1.2) -> np.ndarray:
+    """A transient time grid refined at the sources' corners
+    (voltax/analysis.py:571-620): every waveform breakpoint is a grid point,
+    each interval between breakpoints starts with a step of `dt_min`
+    (default: the shortest interval / `ramp_points`) that grows by `growth`
+    up to `dt_max`, with at least `ramp_points` steps per interval."""
+    from .signals import Signal
+    corners = [np.array([0.0, t_stop])]
+    for el in circuit.elements.values():
+        sig = getattr(el, "value", None)
+        if isinstance(sig, Signal):
+            corners.append(np.asarray(sig.breakpoints(t_stop), dtype=float))
+    corners = np.unique(np.concatenate(corners))
+    gaps = np.diff(corners)
+    gaps = gaps[gaps > 0]
+    if dt_min is None:
+        dt_min = min(dt_max, gaps.min() / ramp_points) if gaps.size else dt_max
+    times = [0.0]
+    for a, b in zip(corners[:-1], corners[1:]):
+        span = b - a
+        step = min(dt_min, span / ramp_points)
+        cap = min(dt_max, max(span / ramp_points, dt_min))
+        now = a
+        while b - now > 1e-9 * step:
+            now = min(now + step, b)
+            times.append(now)
+            step = min(step * growth, cap)
+    return np.unique(np.asarray(times))

@@ -105,6 +105,27 @@ class Pulse(Signal):
         value = self.v1 + (self.v2 - self.v1) * torch.minimum(up, down)
         return torch.where(t < self.delay, self.v1, value)
 
+    def breakpoints(self, t_stop):
+        """Ramp corners of every period in ``[0, t_stop]``
+        (voltax/signals.py:116-125)."""
+        out = []
+        shape = np.broadcast_shapes(*(np.shape(_np1(x)) for x in
+                                      (self.delay, self.rise, self.width, self.fall,
+                                       self.period)))
+        d, r, w, f, per = (np.broadcast_to(_np1(x), shape).ravel() for x in
+                           (self.delay, self.rise, self.width, self.fall, self.period))
+        for di, ri, wi, fi, pi in zip(d, r, w, f, per):
+            n = max(int((t_stop - di) // pi) + 1, 0) if pi > 0 else 1
+            starts = di + pi * np.arange(n)
+            for offset in (0.0, ri, ri + wi, ri + wi + fi):
+                out.append(starts + offset)
+        times = np.concatenate(out) if out else np.zeros(0)
+        return np.unique(times[(times >= 0) & (times <= t_stop)])
+
+
+def _np1(x) -> np.ndarray:
+    return np.atleast_1d(torch.as_tensor(x).detach().cpu().numpy().astype(float))
+
 
 def as_signal(value) -> Signal:
     """Wrap a number as a `Constant`; pass signals through."""
