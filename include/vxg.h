@@ -55,9 +55,12 @@ enum {
   VXG_KIND_ISOURCE = 3,     /* CurrentSource             [waveform rows]        */
   VXG_KIND_EKV = 4,         /* EKVMOSFET [sign, i_spec, vth, dvth, n, vt, lam, c_ox, cov_w,
                                      1/n, 1/(2 vt), c_ox n vt, -(n-1)/n] */
-  VXG_KIND_L1 = 5           /* Level1MOSFET [sign, kp W/L, vth, dvth, lam, gamma, phi,
+  VXG_KIND_L1 = 5,          /* Level1MOSFET [sign, kp W/L, vth, dvth, lam, gamma, phi,
                                      smooth, cov_w, sqrt(phi), 1/(2 sqrt(phi)),
                                      1/smooth or 0] */
+  VXG_KIND_DIODE = 6,       /* Diode        [is, 1/(n vt), tt, cj]                  */
+  VXG_KIND_INDUCTOR = 7,    /* Inductor     [l, rs], one internal (the current)     */
+  VXG_KIND_VCCS = 8         /* VCCS         [gm], terminals (p, n, cp, cn)          */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 

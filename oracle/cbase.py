@@ -63,7 +63,8 @@ def lib():
 
 
 KINDS = {"Resistor": 0, "Conductance": 0, "Capacitor": 1, "VoltageSource": 2,
-         "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5}
+         "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5, "Diode": 6, "Inductor": 7,
+         "VCCS": 8}
 WAVES = {"Constant": 0, "Step": 1, "Pulse": 2}
 
 
@@ -101,6 +102,14 @@ def _rows_of(el, b):
         return [full(sign), i_spec, full(p.vth), inst(el.dvth).expand(n), full(nn), full(vt),
                 full(p.lam), torch.exp(torch.as_tensor(p.log_cox).double()) * w * l,
                 torch.exp(torch.as_tensor(p.log_cov).double()) * w]
+    if name == "Diode":
+        full = lambda x: inst(x).expand(n)  # noqa: E731
+        return [torch.exp(full(el.log_is)), 1.0 / (full(el.n) * full(el.vt)), full(el.tt),
+                full(el.cj)]
+    if name == "Inductor":
+        return [torch.exp(inst(el.log_l)).expand(n), inst(el.rs).expand(n)]
+    if name == "VCCS":
+        return [inst(el.gm).expand(n)]
     if name == "Level1MOSFET":  # voltax/elements/mosfet.py:208-257
         p = el.process
         w, l = torch.exp(inst(el.log_w)), torch.exp(inst(el.log_l))

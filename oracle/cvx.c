@@ -20,7 +20,8 @@
 #include <stdlib.h>
 #include <string.h>
 
-enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5 };
+enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5,
+       K_DIODE = 6, K_IND = 7, K_VCCS = 8 };
 enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
 enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
 
@@ -301,6 +302,33 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
         case K_L1:
           level1(g, d, u, cf, cq, I, Q, J);
           break;
+        case K_DIODE: { /* rows: is, 1/(n vt), tt, cj */
+          const double* p = g->params;
+          const int n = g->n;
+          const double is = p[d], inv = p[n + d], tt = p[2 * n + d], cj = p[3 * n + d];
+          const double v = u[0] - u[1], x = v * inv, e = exp(fmin(x, 40.0));
+          const double ex = x > 40.0 ? e * (1.0 + x - 40.0) : e;
+          const double dex = x == 40.0 ? 0.5 * e : e;
+          const double i = is * (ex - 1.0), gi = is * dex * inv;
+          I[0] = i; I[1] = -i;
+          Q[0] = tt * i + cj * v; Q[1] = -Q[0];
+          const double a = cf * gi + cq * (tt * gi + cj);
+          J[0] = a; J[1] = -a; J[2] = -a; J[3] = a;
+          break;
+        }
+        case K_IND: { /* rows: l, rs; local unknowns (vp, vn, i) */
+          const double l = g->params[d], rs = g->params[g->n + d];
+          I[0] = u[2]; I[1] = -u[2]; I[2] = rs * u[2] - (u[0] - u[1]);
+          Q[2] = l * u[2];
+          J[2] = cf; J[5] = -cf; J[6] = -cf; J[7] = cf; J[8] = cf * rs + cq * l;
+          break;
+        }
+        case K_VCCS: {
+          const double gm = g->params[d], i = gm * (u[2] - u[3]);
+          I[0] = i; I[1] = -i;
+          J[2] = cf * gm; J[3] = -cf * gm; J[6] = -cf * gm; J[7] = cf * gm;
+          break;
+        }
       }
       for (int i = 0; i < m; ++i) {
         if (row[i] < 0) continue;

@@ -9,6 +9,9 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * VoltageSource       voltax/elements/sources.py:85-87
 * CurrentSource       voltax/elements/sources.py:110-112
 * Level1MOSFET        voltax/elements/mosfet.py:208-257
+* Diode               voltax/elements/semiconductor.py:17-70
+* Inductor            voltax/elements/passive.py:62-87
+* VCCS                voltax/elements/controlled.py:46-60
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
                       ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
 * Constant/Step/Pulse voltax/signals.py:58-114
@@ -82,7 +85,8 @@ class GroupModel:
         self.name = type(el).__name__
         self.T = len(el.terminals)
         self.K = el.n_internal
-        self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET")
+        self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET", "Diode",
+                                         "Inductor")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -111,6 +115,17 @@ class GroupModel:
         if name == "CurrentSource":
             i = torch.broadcast_to(signal_value(el.value, t, b), v.shape[:1])
             return torch.stack([i, -i], -1), None
+        if name == "Diode":
+            i = self._diode_current(v[..., 0] - v[..., 1])
+            return torch.stack([i, -i], -1), None
+        if name == "Inductor":  # passive.py:62-87
+            i = x[..., 0]
+            rs = _inst(el.rs, b)
+            return torch.stack([i, -i], -1), (rs * i - (v[..., 0] - v[..., 1]))[..., None]
+        if name == "VCCS":  # controlled.py:46-60
+            i = _inst(el.gm, b) * (v[..., 2] - v[..., 3])
+            z = torch.zeros_like(i)
+            return torch.stack([i, -i, z, z], -1), None
         if name in ("EKVMOSFET", "Level1MOSFET"):
             s = self._sign()
             vd, vg, vs, vb = (s * v[..., k] for k in range(4))
@@ -148,6 +163,12 @@ class GroupModel:
             q_gs, q_gd = cov * (vg - vs), cov * (vg - vd)
             overlap = torch.stack([-q_gd, q_gs + q_gd, -q_gs, torch.zeros_like(q_gs)], -1)
             return s * (intrinsic + overlap), None
+        if name == "Diode":  # q = tt i + cj v (semiconductor.py:68-70)
+            vd = v[..., 0] - v[..., 1]
+            q = _inst(el.tt, b) * self._diode_current(vd) + _inst(el.cj, b) * vd
+            return torch.stack([q, -q], -1), None
+        if name == "Inductor":
+            return None, (torch.exp(_inst(el.log_l, b)) * x[..., 0])[..., None]
         if name == "Level1MOSFET":  # overlap charges only (mosfet.py:255-257)
             s = self._sign()
             vd, vg, vs, vb = (s * v[..., k] for k in range(4))
@@ -169,6 +190,15 @@ class GroupModel:
         i_f = softplus((vp - (vs - vb)) / (2 * vt)) ** 2
         i_r = softplus((vp - (vd - vb)) / (2 * vt)) ** 2
         return i_f, i_r
+
+    def _diode_current(self, vd):
+        """is (explin(vd / (n vt)) - 1), explin linear above 40
+        (semiconductor.py:17-24, 62-63)."""
+        el, b = self.el, self.b
+        u = vd / (_inst(el.n, b) * _inst(el.vt, b))
+        e = torch.exp(_jmin(u, torch.full_like(u, 40.0)))
+        ex = torch.where(u > 40.0, e * (1.0 + u - 40.0), e)
+        return torch.exp(_inst(el.log_is, b)) * (ex - 1.0)
 
     # Level 1 (mosfet.py:229-253). jnp.maximum / jnp.minimum give each side
     # half the derivative at a tie; _jmax / _jmin do the same under torch AD.

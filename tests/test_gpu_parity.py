@@ -47,6 +47,24 @@ CIRCUITS = {
     "ring_l1": lambda: workloads.ring_oscillator_level1(5, gamma=0.3)[0],
     "ring_l1_smooth": lambda: workloads.ring_oscillator_level1(5, smooth=0.02, gamma=0.3)[0],
 }
+def mixed_circuit():
+    """A pulse through R and a series-RL into C, a diode (junction and
+    diffusion charge) to a load, and a VCCS sensing the capacitor."""
+    from voltax_gb300.signals import Pulse
+    b = CircuitBuilder()
+    b.vsource("in", "0", Pulse(0.0, 1.0, delay=5e-12, rise=10e-12, fall=10e-12,
+                               width=60e-12, period=200e-12), name="Vin")
+    b.resistor("in", "a", 50.0, name="R1")
+    b.inductor("a", "b", 2e-9, rs=5.0, name="L1")
+    b.capacitor("b", "0", 0.5e-12, name="C1")
+    b.diode("b", "c", name="D1", is_=1e-14, n=1.2, cj=0.1e-12, tt=2e-12)
+    b.resistor("c", "0", 200.0, name="R2")
+    b.vccs("d", "0", "b", "0", 2e-3, name="G1")
+    b.resistor("d", "0", 1e3, name="R3")
+    return b.build()
+
+
+CIRCUITS["mixed"] = mixed_circuit
 LINEAR = ("rc_ladder", "grid")
 
 
@@ -221,6 +239,43 @@ def test_level1_dc_gradient_matches_finite_differences():
             fd = (float(v_out(c.replace(gname, e_p))) -
                   float(v_out(c.replace(gname, e_m)))) / (2 * h)
             np.testing.assert_allclose(g.sum(), fd, rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize("method", ["be", "trap"])
+@pytest.mark.parametrize("engine", ENGINES)
+def test_mixed_devices_transient_matches_oracle(method, engine):
+    """Inductor, diode (with charges) and VCCS through a pulse transient."""
+    c = mixed_circuit()
+    ts = np.linspace(0.0, 150e-12, 61)
+    sol = vx.transient(c, ts, ic="dc", method=method, options=vx.Options(engine=engine))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc", method=method)
+    assert bool(sol.converged.all()) and okr.all()
+    v = sol.z.cpu().numpy()
+    scale = max(1.0, np.abs(zr).max())
+    assert np.max(np.abs(v - zr)) < 1e-9 * scale
+    assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+def test_mixed_devices_dc_gradient_matches_finite_differences():
+    """Parameter VJP of the diode, inductor and VCCS kernels (dual numbers)."""
+    c = mixed_circuit().set("Vin", v1=0.8)
+    out = c.node("d")
+    cases = [("Diode", "log_is"), ("Diode", "n"), ("VCCS", "gm"), ("Resistor", "log_r")]
+    for gname, field in cases:
+        el = c.elements[gname]
+        e2 = el.with_nodes(el.nodes)
+        setattr(e2, field, getattr(el, field).clone().requires_grad_(True))
+        vx.dc(c.replace(gname, e2)).z[out].backward()
+        g = getattr(e2, field).grad.numpy().sum()
+        h = 1e-6
+        vals = []
+        for sgn in (1, -1):
+            e3 = el.with_nodes(el.nodes)
+            setattr(e3, field, getattr(el, field).clone() + sgn * h)
+            vals.append(float(vx.dc(c.replace(gname, e3)).z[out]))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-9), (gname, field)
 
 
 def test_rc_ladder_recorded_values_on_gpu():

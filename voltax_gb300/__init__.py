@@ -12,7 +12,7 @@ from .analysis import Options, Solution, dc, dc_sweep, time_grid, transient  # n
 from .builder import CircuitBuilder  # noqa: F401
 from .circuit import Circuit, Layout  # noqa: F401
 from .elements import (VT_300K, Capacitor, Conductance, CurrentSource,  # noqa: F401
-                       EKVMOSFET, Element, Level1MOSFET, MOSProcess, Resistor,
-                       VoltageSource)
+                       VCCS, Diode, EKVMOSFET, Element, Inductor, Level1MOSFET,
+                       MOSProcess, Resistor, VoltageSource)
 
 __version__ = "0.1.0"

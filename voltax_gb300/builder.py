@@ -20,6 +20,7 @@ from .signals import Constant, Signal
 _PREFIX = {
     el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
     el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
+    el.Inductor: "L", el.Diode: "D", el.VCCS: "G",
 }
 
 
@@ -104,6 +105,15 @@ class CircuitBuilder:
 
     def capacitor(self, p, n, c, name=None, group=None) -> str:
         return self.add(el.Capacitor((p, n), c), name, group)
+
+    def inductor(self, p, n, l, rs=0.0, name=None, group=None) -> str:
+        return self.add(el.Inductor((p, n), l, rs), name, group)
+
+    def diode(self, a, k, name=None, group=None, **params) -> str:
+        return self.add(el.Diode((a, k), **params), name, group)
+
+    def vccs(self, p, n, cp, cn, gm, name=None, group=None) -> str:
+        return self.add(el.VCCS((p, n, cp, cn), gm), name, group)
 
     def vsource(self, p, n, value=0.0, name=None, group=None) -> str:
         return self.add(el.VoltageSource((p, n), value), name, group)

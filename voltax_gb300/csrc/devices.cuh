@@ -620,6 +620,84 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
     case VXG_KIND_L1:
       l1_soa<JT>(g, b, d, u, cf, cq, wf, wq, wj, fo, qo, jo);
       break;
+    case VXG_KIND_DIODE: {  // voltax/elements/semiconductor.py:17-70
+      const double i_s = prm(g, 0, b, d), inv_nvt = prm(g, 1, b, d);
+      const double tt = prm(g, 2, b, d), cj = prm(g, 3, b, d);
+      const double v = u[0] - u[1], x = v * inv_nvt;
+      const double e = exp(fmin(x, 40.0));
+      // explin and its derivative (min splits 1/2 : 1/2 at x = 40, as jnp does)
+      const double ex = x > 40.0 ? e * (1.0 + x - 40.0) : e;
+      const double dex = x > 40.0 ? e : (x == 40.0 ? 0.5 * e : e);
+      const double i = i_s * (ex - 1.0);
+      const double q = tt * i + cj * v;
+      if (wf) {
+        fo[d] = i;
+        fo[n + d] = -i;
+      }
+      if (wq) {
+        qo[d] = q;
+        qo[n + d] = -q;
+      }
+      if (wj) {
+        const double gi = i_s * dex * inv_nvt;
+        const JT a = (JT)(cf * gi + cq * (tt * gi + cj));
+        jo[d] = a;
+        jo[n + d] = -a;
+        jo[2 * n + d] = -a;
+        jo[3 * n + d] = a;
+      }
+      break;
+    }
+    case VXG_KIND_INDUCTOR: {  // voltax/elements/passive.py:62-87; u = (vp, vn, i)
+      const double l = prm(g, 0, b, d), rs = prm(g, 1, b, d);
+      if (wf) {
+        fo[d] = u[2];
+        fo[n + d] = -u[2];
+        fo[2 * n + d] = rs * u[2] - (u[0] - u[1]);
+      }
+      if (wq) {
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+        qo[2 * n + d] = l * u[2];
+      }
+      if (wj) {  // rows (p, n, branch), cols (vp, vn, i)
+        const JT a = (JT)cf;
+        jo[0 * n + d] = JT(0);
+        jo[1 * n + d] = JT(0);
+        jo[2 * n + d] = a;
+        jo[3 * n + d] = JT(0);
+        jo[4 * n + d] = JT(0);
+        jo[5 * n + d] = -a;
+        jo[6 * n + d] = -a;
+        jo[7 * n + d] = a;
+        jo[8 * n + d] = (JT)(cf * rs + cq * l);
+      }
+      break;
+    }
+    case VXG_KIND_VCCS: {  // voltax/elements/controlled.py:46-60
+      const double gm = prm(g, 0, b, d);
+      const double i = gm * (u[2] - u[3]);
+      if (wf) {
+        fo[d] = i;
+        fo[n + d] = -i;
+        fo[2 * n + d] = 0.0;
+        fo[3 * n + d] = 0.0;
+      }
+      if (wq) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) qo[e * n + d] = 0.0;
+      }
+      if (wj) {
+        const JT a = (JT)(cf * gm);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) jo[e * n + d] = JT(0);
+        jo[2 * n + d] = a;
+        jo[3 * n + d] = -a;
+        jo[6 * n + d] = -a;
+        jo[7 * n + d] = a;
+      }
+      break;
+    }
   }
 }
 

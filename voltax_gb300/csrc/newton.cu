@@ -277,6 +277,31 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
       }
       break;
     }
+    case VXG_KIND_DIODE: {
+      const Dual i_s = p[0], inv_nvt = p[1], tt = p[2], cj = p[3];
+      const double v = u[0] - u[1];
+      const Dual x = mk(v) * inv_nvt;
+      const Dual e = dexp(x.v > 40.0 ? mk(40.0) : x);
+      const Dual ex = x.v > 40.0 ? e * (1.0 + (x - mk(40.0))) : e;
+      const Dual i = i_s * (ex - mk(1.0));
+      out[0] = cf * i;
+      out[1] = cf * (-i);
+      if (cq != 0.0) {
+        const Dual q = tt * i + cj * mk(v);
+        out[0] = out[0] + cq * q;
+        out[1] = out[1] + cq * (-q);
+      }
+      break;
+    }
+    case VXG_KIND_INDUCTOR:
+      out[2] = cf * (p[1] * mk(u[2])) + cq * (p[0] * mk(u[2]));
+      break;
+    case VXG_KIND_VCCS: {
+      const Dual i = p[0] * mk(u[2] - u[3]);
+      out[0] = cf * i;
+      out[1] = cf * (-i);
+      break;
+    }
     case VXG_KIND_L1: {
       const double sign = p[0].v;
       const Dual k = p[1], vt0 = p[2] + p[3], lam = p[4], gamma = p[5], phi = p[6];

@@ -37,6 +37,9 @@ KIND_VSOURCE = 2
 KIND_ISOURCE = 3
 KIND_EKV = 4
 KIND_L1 = 5
+KIND_DIODE = 6
+KIND_INDUCTOR = 7
+KIND_VCCS = 8
 
 
 def _t(x) -> torch.Tensor:
@@ -499,5 +502,76 @@ class Level1MOSFET(EKVMOSFET):
                 full(0.5 / sphi), full(1.0 / self.smooth if self.smooth > 0 else 0.0)]
 
 
+class Inductor(Element):
+    """Inductor with series resistance (passive.py:62-87). Internal unknown:
+    the branch current ``i`` (``p -> n``); ``l di/dt + rs i - (v_p - v_n) = 0``.
+
+    Kernel parameter rows: l, rs."""
+
+    terminals = ("p", "n")
+    n_internal = 1
+    internal_names = ("i",)
+    fields = ("log_l", "rs")
+    kind = KIND_INDUCTOR
+    has_charges = True
+
+    def __init__(self, nodes, l, rs=0.0):
+        self.nodes = self._devices(nodes)
+        self.log_l = self._log_per_device(l)
+        self.rs = self._per_device(rs)
+
+    @property
+    def l(self):
+        return torch.exp(self.log_l)
+
+    def gpu_params(self):
+        return [torch.exp(self.log_l), self.rs.expand(self.log_l.shape)]
+
+
+class Diode(Element):
+    """Shockley diode (semiconductor.py:27-70): ``i = is (explin(v/(n vt)) - 1)``
+    with ``explin`` continuing ``exp`` linearly above 40, ``q = tt i + cj v``,
+    ``v = v_anode - v_cathode``.
+
+    Kernel parameter rows: is, 1/(n vt), tt, cj."""
+
+    terminals = ("a", "k")
+    fields = ("log_is", "n", "cj", "tt", "vt")
+    kind = KIND_DIODE
+    has_charges = True
+
+    def __init__(self, nodes, is_=1e-14, n=1.0, cj=0.0, tt=0.0, vt=VT_300K):
+        self.nodes = self._devices(nodes)
+        self.log_is = self._log_per_device(is_)
+        self.n = self._per_device(n)
+        self.cj = self._per_device(cj)
+        self.tt = self._per_device(tt)
+        self.vt = self._per_device(vt)
+
+    def gpu_params(self):
+        i_s = torch.exp(self.log_is)
+        shape = i_s.shape
+        return [i_s, (1.0 / (self.n * self.vt)).expand(shape), self.tt.expand(shape),
+                self.cj.expand(shape)]
+
+
+class VCCS(Element):
+    """Voltage-controlled current source (controlled.py:46-60):
+    ``i = gm (v_cp - v_cn)`` flowing ``p -> n`` through the source.
+
+    Kernel parameter rows: gm."""
+
+    terminals = ("p", "n", "cp", "cn")
+    fields = ("gm",)
+    kind = KIND_VCCS
+
+    def __init__(self, nodes, gm):
+        self.nodes = self._devices(nodes)
+        self.gm = self._per_device(gm)
+
+    def gpu_params(self):
+        return [self.gm]
+
+
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
-                 EKVMOSFET, Level1MOSFET)
+                 EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS)
