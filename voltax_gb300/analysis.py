@@ -487,7 +487,7 @@ def dc_sweep(circuit, values, apply, t: float = 0.0, guess=None,
     if isinstance(apply, str):
         device = apply
         apply = lambda c, v: c.set(device, value=v)  # noqa: E731
-    vals = torch.as_tensor(np.asarray(values, dtype=np.float64))
+    vals = torch.as_tensor(np.array(values, dtype=np.float64))  # a copy: any strides
     z = guess
     zs, oks, its = [], [], []
     for v in vals:
