@@ -44,7 +44,8 @@ enum {
 /* ---- numeric formats of the factorization ------------------------------ */
 enum {
   VXG_F64 = 0, /* plain form: FP64 panels, FP64 solves                       */
-  VXG_F32 = 1  /* chosen form: FP32 panels and solves + FP64 refinement     */
+  VXG_F32 = 1, /* chosen form: FP32 panels and solves + FP64 refinement     */
+  VXG_C128 = 2 /* complex FP64 panels (AC small-signal; sizes only)         */
 };
 
 /* ---- device kinds (kernel parameter rows in brackets) ------------------ */
@@ -329,6 +330,22 @@ int vxg_mlp_mse(int64_t M, int32_t N, const float* y, const float* target, const
  * rewrites w_bf16 from w. */
 int vxg_mlp_adam(int64_t n, float* w, void* w_bf16, const float* grad, float* m, float* v,
                  float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+
+/* ---- AC small-signal analysis (voltax/analysis.py:483-524) ---------------
+ * A(w) = G + j w C on the topology's pattern, one instance per angular
+ * frequency w = omega[f]; G, C: the FP64 CSR values of df/dz and dq/dz at
+ * the operating point (vxg_eval with (cf, cq) = (1, 0) and (0, 1)), shared by
+ * all frequencies. Factors are complex FP64 (interleaved re, im; size from
+ * vxg_factor_size with VXG_C128), factored under the same plan and pivoting
+ * rule (largest |re| + |im| in the block column). Workspace: vxg_workspace_size
+ * with VXG_C128. */
+int vxg_ac_factor(const vxg_handle* h, int32_t n_freq, const double* G, const double* C,
+                  const double* omega, void* factors, void* workspace, void* stream);
+
+/* x[f] = A(w_f)^-1 b[f] for every frequency; b and x complex (interleaved),
+ * b[f] at b + 2 * f * b_stride (b_stride 0: one right-hand side for all). */
+int vxg_ac_solve(const vxg_handle* h, int32_t n_freq, const void* factors, const double* b,
+                 int64_t b_stride, double* x, void* workspace, void* stream);
 
 /* Kernels this library has launched since it was loaded (a diagnostic
  * counter; no counterpart in the reference). */

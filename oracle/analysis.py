@@ -145,3 +145,41 @@ def dc_adjoint(sys: System, z, g, t=0.0, opts: Options = Options()):
     """``lam`` with ``J(z)^T lam = g`` (voltax/analysis.py:282-288)."""
     _, jac = sys.dc_pair(t, opts.gmin)
     return sys.solve(jac(z), g, transpose=True)
+
+
+def ac(sys: System, freqs, z_op, t=0.0):
+    """Small-signal AC (voltax/analysis.py:494-524): ``(G + j 2 pi f C) z = -b``
+    with dense complex LAPACK solves; ``G``, ``C`` the stamped Jacobians of
+    f and q at the operating point ``z_op``, ``b`` the sources' stimulus."""
+    c, st = sys.c, sys.st
+    n = st.size
+    G = np.zeros((n, n))
+    Cm = np.zeros((n, n))
+    rows = np.repeat(np.arange(n), np.diff(st.indptr))
+    G[rows, st.indices] = stamp.jacobian(c, st, z_op, t, 1.0, 0.0, sys.b)
+    Cm[rows, st.indices] = stamp.jacobian(c, st, z_op, t, 0.0, 1.0, sys.b)
+    b = _ac_stimulus(c)
+    return np.stack([np.linalg.solve(G + 2j * np.pi * f * Cm, -b) for f in freqs])
+
+
+def _ac_stimulus(c):
+    """voltax/circuit.py:204-207 with sources.py:85-115: a voltage source
+    adds ``-ac e^{j phase}`` to its branch equation, a current source drives
+    ``ac e^{j phase}`` from p to n."""
+    b = np.zeros(c.layout.size, dtype=complex)
+    for name, n, k, off in c.layout.groups:
+        el = c.elements[name]
+        if type(el).__name__ not in ("VoltageSource", "CurrentSource") or n == 0:
+            continue
+        ac = np.broadcast_to(np.asarray(el.ac, dtype=float), (n,))
+        ph = np.broadcast_to(np.asarray(el.ac_phase, dtype=float), (n,))
+        phasor = ac * np.exp(1j * np.pi / 180.0 * ph)
+        if type(el).__name__ == "VoltageSource":
+            b[off + np.arange(n) * k] -= phasor
+        else:
+            nodes = np.asarray(el.nodes, dtype=np.int64).reshape(n, -1)
+            for col, sgn in ((0, 1.0), (1, -1.0)):
+                for d in range(n):
+                    if nodes[d, col] >= 0:
+                        b[nodes[d, col]] += sgn * phasor[d]
+    return b

@@ -1,0 +1,83 @@
+"""AC small-signal analysis (voltax/analysis.py:483-524) on the GPU against
+closed forms and the oracle's dense complex solves."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import analysis as oa
+
+pytestmark = pytest.mark.gpu
+
+
+def _rc(R=1e3, C=1e-7):
+    from voltax_gb300.builder import CircuitBuilder
+    b = CircuitBuilder()
+    b.vsource("in", "0", 0.0, ac=1.0, name="Vin")
+    b.resistor("in", "out", R, name="R1")
+    b.capacitor("out", "0", C, name="C1")
+    return b.build()
+
+
+def test_rc_lowpass_closed_form():
+    import voltax_gb300 as vx
+    R, C = 1e3, 1e-7
+    f = np.logspace(1, 6, 41)
+    sol = vx.ac(_rc(R, C), f)
+    w = 2 * np.pi * f * R * C
+    h = sol.v("out").cpu().numpy()
+    np.testing.assert_allclose(np.abs(h), 1 / np.sqrt(1 + w ** 2), rtol=1e-12)
+    np.testing.assert_allclose(np.angle(h), -np.arctan(w), rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(sol.db("out").cpu().numpy(),
+                               -10 * np.log10(1 + w ** 2), atol=1e-10)
+    # the stimulus source's branch current: i = -(v_in - v_out)/R through the source
+    i = sol.i("Vin").cpu().numpy()
+    np.testing.assert_allclose(i, -(1 - h) / R, rtol=1e-10)
+
+
+def test_phase_unwrapped_through_four_poles():
+    """voltax tests/test_analysis.py:240-249, buffered by VCCS stages
+    (gm = -1 mS into 1 kOhm: gain +1)."""
+    import voltax_gb300 as vx
+    from voltax_gb300.builder import CircuitBuilder
+    b = CircuitBuilder()
+    b.vsource("in", "0", 0.0, ac=1.0, name="Vin")
+    for k in range(4):
+        b.resistor("in" if k == 0 else f"b{k}", f"n{k}", 1e3, name=f"R{k}")
+        b.capacitor(f"n{k}", "0", 1e-9, name=f"C{k}")
+        b.vccs(f"b{k + 1}", "0", f"n{k}", "0", -1e-3, name=f"G{k}")
+        b.resistor(f"b{k + 1}", "0", 1e3, name=f"RL{k}")
+    sol = vx.ac(b.build(), np.logspace(3, 8, 200))
+    ph = sol.phase("b4").numpy()
+    assert ph[-1] < -300
+    assert np.all(np.diff(ph) < 1.0)
+
+
+@pytest.mark.parametrize("name", ["mixed", "ota"])
+def test_ac_matches_oracle(name):
+    import voltax_gb300 as vx
+    from voltax_gb300 import symbolic, workloads
+    if name == "ota":
+        c = workloads.ota_chain(6)
+        c = c.replace("VoltageSource", _with_ac(c.elements["VoltageSource"],
+                                                 c.layout.device("Vin")[1]))
+    else:
+        from circuits import mixed_circuit
+        c = mixed_circuit()
+        c = c.replace("VoltageSource_Pulse", _with_ac(c.elements["VoltageSource_Pulse"], 0))
+    f = np.logspace(6, 11, 17)
+    sol = vx.ac(c, f)
+    st = symbolic.structure(c)
+    z_op = sol.op.z.cpu().numpy()
+    ref = oa.ac(oa.System(c, st, st.plan), f, z_op)
+    z = sol.z.cpu().numpy()
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    assert np.max(np.abs(z - ref) / scale) < 1e-10
+
+
+def _with_ac(el, idx):
+    e = el.with_nodes(el.nodes)
+    ac = torch.zeros(el.size, dtype=torch.float64)
+    ac[idx] = 1.0
+    e.ac, e.ac_phase = ac, torch.full((el.size,), 30.0, dtype=torch.float64)
+    return e

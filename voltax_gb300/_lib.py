@@ -13,7 +13,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvxg.so"
 
 VXG_OK, VXG_ERR_INVALID, VXG_ERR_CUDA, VXG_ERR_TOO_LARGE, VXG_ERR_ALLOC = range(5)
-VXG_F64, VXG_F32 = 0, 1
+VXG_F64, VXG_F32, VXG_C128 = 0, 1, 2
 VXG_MODE_DC, VXG_MODE_BE, VXG_MODE_TRAP = 0, 1, 2
 VXG_ACT_NONE, VXG_ACT_GELU = 0, 1
 MAX_GROUPS = 32
@@ -82,6 +82,8 @@ SIGNATURES = {
                        C.POINTER(NewtonOpts), P, P, P, P], I32),
     "vxg_factor_static": ([P, I32, I32, P, P, P], I32),
     "vxg_launch_count": ([], C.c_uint64),
+    "vxg_ac_factor": ([P, I32, P, P, P, P, P, P], I32),
+    "vxg_ac_solve": ([P, I32, P, P, I64, P, P, P], I32),
     "vxg_mlp_normalize": ([I64, I32, P, I64, P, P, P, P, P], I32),
     "vxg_mlp_linear": ([I64, I32, I32, P, P, P, I32, P, P, P, P, P, P, I64, P], I32),
     "vxg_mlp_linear_dx": ([I64, I32, I32, P, P, P, P, P], I32),

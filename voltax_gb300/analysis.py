@@ -529,3 +529,77 @@ def time_grid(circuit, t_stop: float, dt_max: float, dt_min: float | None = None
             times.append(now)
             step = min(step * growth, cap)
     return np.unique(np.asarray(times))
+
+
+# =============================================================================
+# AC small-signal analysis
+# =============================================================================
+
+
+class ACSolution:
+    """Result of `ac` (voltax/analysis.py:142-178): complex phasors
+    ``z`` of shape ``(F, S)`` at the frequencies ``freqs`` (Hz)."""
+
+    def __init__(self, freqs, z, op, layout):
+        self.freqs, self.z, self.op, self.layout = freqs, z, op, layout
+
+    def v(self, node: str | None = None):
+        if node is None:
+            return self.z[..., : self.layout.n_nodes]
+        idx = self.layout.node(node)
+        if idx < 0:
+            return torch.zeros(self.z.shape[:-1], dtype=self.z.dtype, device=self.z.device)
+        return self.z[..., idx]
+
+    def i(self, device: str, which: str | None = None):
+        return self.z[..., self.layout.internal(device, which)]
+
+    def db(self, node: str):
+        """``20 log10 |v(node)|``."""
+        return 20 * torch.log10(self.v(node).abs())
+
+    def phase(self, node: str, unwrap: bool = True):
+        """Phase of `v(node)` in degrees, unwrapped along frequency."""
+        ang = torch.angle(self.v(node)).cpu().numpy()
+        if unwrap:
+            ang = np.unwrap(ang, axis=0)
+        return torch.as_tensor(np.rad2deg(ang))
+
+
+def ac(circuit, freqs, op: Solution | None = None, options: Options = Options(),
+       max_factor_bytes: float = 2e9) -> ACSolution:
+    """Small-signal AC analysis around the DC operating point
+    (voltax/analysis.py:494-524): solves ``(G + j 2 pi f C) z = -b`` for every
+    frequency, ``b`` the sources' ``ac`` / ``ac_phase`` stimulus.
+
+    ``G`` and ``C`` are stamped once at the operating point; the frequencies
+    are the batch of one complex factorization + solve launch sequence
+    (`vxg_ac_factor` / `vxg_ac_solve`) under the circuit's own plan, in
+    chunks whose factors fit `max_factor_bytes`."""
+    if circuit.batch != 1:
+        raise ValueError("ac() takes one circuit instance")
+    op = dc(circuit, options=options) if op is None else op
+    st = structure(circuit)
+    eng = engine_for(st, circuit)
+    from . import sparse
+    t0 = float(op.t)
+    G = sparse.jacobian(circuit, op.z, t0, 1.0, 0.0, structure=st).contiguous()
+    Cq = sparse.jacobian(circuit, op.z, t0, 0.0, 1.0, structure=st).contiguous()
+    b = torch.as_tensor(-circuit.ac_stimulus(), dtype=torch.complex128)
+    rhs = torch.view_as_real(b).contiguous().to(eng.device)
+    f = np.asarray(freqs, dtype=np.float64).reshape(-1)
+    omega = torch.as_tensor(2 * np.pi * f, dtype=torch.float64, device=eng.device)
+    chunk = max(1, int(max_factor_bytes // max(16 * eng.tables.work, 1)))
+    out = []
+    for s0 in range(0, len(f), chunk):
+        F = min(chunk, len(f) - s0)
+        fac = eng.factor_buffer(F, L.VXG_C128)
+        ws = eng.workspace(F, L.VXG_C128)
+        L.check(eng.lib.vxg_ac_factor(eng.handle, F, G.data_ptr(), Cq.data_ptr(),
+                                      omega[s0:s0 + F].data_ptr(), fac.data_ptr(),
+                                      ws.data_ptr(), stream_ptr()), "vxg_ac_factor")
+        x = torch.empty((F, eng.S, 2), dtype=torch.float64, device=eng.device)
+        L.check(eng.lib.vxg_ac_solve(eng.handle, F, fac.data_ptr(), rhs.data_ptr(), 0,
+                                     x.data_ptr(), ws.data_ptr(), stream_ptr()), "vxg_ac_solve")
+        out.append(torch.view_as_complex(x))
+    return ACSolution(torch.as_tensor(f), torch.cat(out), op, circuit.layout)

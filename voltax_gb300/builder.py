@@ -115,11 +115,11 @@ class CircuitBuilder:
     def vccs(self, p, n, cp, cn, gm, name=None, group=None) -> str:
         return self.add(el.VCCS((p, n, cp, cn), gm), name, group)
 
-    def vsource(self, p, n, value=0.0, name=None, group=None) -> str:
-        return self.add(el.VoltageSource((p, n), value), name, group)
+    def vsource(self, p, n, value=0.0, ac=0.0, ac_phase=0.0, name=None, group=None) -> str:
+        return self.add(el.VoltageSource((p, n), value, ac, ac_phase), name, group)
 
-    def isource(self, p, n, value=0.0, name=None, group=None) -> str:
-        return self.add(el.CurrentSource((p, n), value), name, group)
+    def isource(self, p, n, value=0.0, ac=0.0, ac_phase=0.0, name=None, group=None) -> str:
+        return self.add(el.CurrentSource((p, n), value, ac, ac_phase), name, group)
 
     def nmos(self, d, g, s, b=None, w=1e-6, l=0.13e-6, name=None, group=None,
              process=None, dvth=0.0) -> str:

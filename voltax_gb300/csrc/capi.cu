@@ -32,7 +32,10 @@ void set_error(cudaError_t e) {
 
 char* last_error_buffer() { return g_err; }
 
-size_t elem_size(int precision) { return precision == VXG_F32 ? sizeof(float) : sizeof(double); }
+size_t elem_size(int precision) {
+  return precision == VXG_F32 ? sizeof(float) : precision == VXG_C128 ? 2 * sizeof(double)
+                                                                       : sizeof(double);
+}
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -383,17 +386,36 @@ int vxg_destroy(vxg_handle* h) {
 }
 
 int vxg_workspace_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes) {
-  if (!h || !bytes || batch <= 0 || (precision != VXG_F64 && precision != VXG_F32))
+  if (!h || !bytes || batch <= 0 ||
+      (precision != VXG_F64 && precision != VXG_F32 && precision != VXG_C128))
     return VXG_ERR_INVALID;
   *bytes = layout(h->t, batch, precision).total;
   return VXG_OK;
 }
 
 int vxg_factor_size(const vxg_handle* h, int32_t batch, int32_t precision, size_t* bytes) {
-  if (!h || !bytes || batch <= 0 || (precision != VXG_F64 && precision != VXG_F32))
+  if (!h || !bytes || batch <= 0 ||
+      (precision != VXG_F64 && precision != VXG_F32 && precision != VXG_C128))
     return VXG_ERR_INVALID;
   *bytes = elem_size(precision) * (size_t)batch * h->t.work;
   return VXG_OK;
+}
+
+int vxg_ac_factor(const vxg_handle* h, int32_t n_freq, const double* G, const double* C,
+                  const double* omega, void* factors, void* workspace, void* stream) {
+  if (!h || n_freq <= 0 || !G || !C || !omega || !factors || !workspace) return VXG_ERR_INVALID;
+  const Layout L = layout(h->t, n_freq, VXG_C128);
+  return launch_factor_ac(h->t, n_freq, G, C, omega, factors, at<char>(workspace, L.scratch),
+                          (cudaStream_t)stream);
+}
+
+int vxg_ac_solve(const vxg_handle* h, int32_t n_freq, const void* factors, const double* b,
+                 int64_t b_stride, double* x, void* workspace, void* stream) {
+  if (!h || n_freq <= 0 || !factors || !b || !x || !workspace || b_stride < 0)
+    return VXG_ERR_INVALID;
+  const Layout L = layout(h->t, n_freq, VXG_C128);
+  return launch_solve_ac(h->t, n_freq, factors, b, b_stride, x, at<char>(workspace, L.scratch),
+                         (cudaStream_t)stream);
 }
 
 int vxg_eval(const vxg_handle* h, int32_t batch, const vxg_group_params* params,

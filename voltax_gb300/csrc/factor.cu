@@ -14,6 +14,7 @@
 // (deterministic, no atomics): work[t] -= sum(S[src]).
 // (voltax/sparse.py:549-572)
 
+#include "cplx.cuh"
 #include "internal.cuh"
 
 namespace vxg {
@@ -95,17 +96,18 @@ __global__ void __launch_bounds__(NT)
   // per pivot step.
   for (int c = 0; c < k; ++c) {
     if (warp == 0) {
-      T best = T(-1);
+      using M = decltype(pmag(T()));
+      M best = M(-1);
       int bi = c;
       for (int i = c + lane; i < k; i += 32) {
-        const T v = tabs(A[i * k + c]);
+        const M v = pmag(A[i * k + c]);
         if (v > best) {
           best = v;
           bi = i;
         }
       }
       for (int off = 16; off > 0; off >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, best, off);
+        const M ov = __shfl_down_sync(0xffffffffu, best, off);
         const int oi = __shfl_down_sync(0xffffffffu, bi, off);
         if (ov > best || (ov == best && oi < bi)) {
           best = ov;
@@ -213,15 +215,37 @@ size_t factor_smem_bytes(int k, size_t es) {
 }
 
 template <typename T>
+static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t s);
+
+template <typename T>
 static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scratch,
                        cudaStream_t s) {
-  const long long ws = t.work, ss = t.max_schur;
+  const long long ws = t.work;
   VXG_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(T) * (size_t)B * ws, s));
   const long long n = (long long)B * t.nnz;
   if (n)
     fill_panels_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, t.nnz, t.a_pos, data,
                                                                         work, ws);
   VXG_LAUNCHED();
+  return factor_levels<T>(t, B, work, scratch, s);
+}
+
+// Panels of A = G + j omega[b] C for every frequency b (AC small-signal).
+__global__ void fill_panels_ac_kernel(int B, long long nnz, const long long* __restrict__ a_pos,
+                                      const double* __restrict__ G,
+                                      const double* __restrict__ C,
+                                      const double* __restrict__ omega, cplx* __restrict__ work,
+                                      long long work_stride) {
+  const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gid >= (long long)B * nnz) return;
+  const int b = (int)(gid / nnz);
+  const long long e = gid - (long long)b * nnz;
+  work[(long long)b * work_stride + a_pos[e]] = cplx(G[e], omega[b] * C[e]);
+}
+
+template <typename T>
+static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t s) {
+  const long long ws = t.work, ss = t.max_schur;
   int dev = 0, max_optin = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -263,6 +287,18 @@ static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scr
     }
   }
   return VXG_OK;
+}
+
+int launch_factor_ac(const Topo& t, int B, const double* G, const double* C,
+                     const double* omega, void* factors, void* scratch, cudaStream_t s) {
+  cplx* work = (cplx*)factors;
+  VXG_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(cplx) * (size_t)B * t.work, s));
+  const long long n = (long long)B * t.nnz;
+  if (n)
+    fill_panels_ac_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, t.nnz, t.a_pos, G, C,
+                                                                      omega, work, t.work);
+  VXG_LAUNCHED();
+  return factor_levels<cplx>(t, B, work, (cplx*)scratch, s);
 }
 
 int launch_factor(const Topo& t, int B, int precision, const double* data, void* factors,

@@ -123,6 +123,10 @@ int launch_eval(const Topo& t, const GroupTable& gt, int B, const double* z, dou
 int launch_gather(const Topo& t, int B, const double* cf_buf, const double* cq_buf,
                   const double* cj_buf, const double* gmin, double gmin_scalar, double* f_out,
                   double* q_out, double* data_out, cudaStream_t s);
+int launch_factor_ac(const Topo& t, int B, const double* G, const double* C,
+                     const double* omega, void* factors, void* scratch, cudaStream_t s);
+int launch_solve_ac(const Topo& t, int B, const void* factors, const double* b,
+                    long long b_stride, double* x, void* scratch, cudaStream_t s);
 int launch_factor(const Topo& t, int B, int precision, const double* data, void* factors,
                   void* scratch, cudaStream_t s);
 int launch_solve(const Topo& t, int B, int precision, const void* factors, const double* data,

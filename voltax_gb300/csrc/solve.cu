@@ -10,13 +10,14 @@
 // Row dot products use a warp per row (lane-strided, coalesced); transposed
 // products use a thread per output column (coalesced across the warp).
 
+#include "cplx.cuh"
 #include "internal.cuh"
 
 namespace vxg {
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  for (int off = 16; off > 0; off >>= 1) v += shfl_xor(v, off);
   return v;
 }
 
@@ -229,6 +230,25 @@ static int solve_levels(const Topo& t, int B, const T* fac, T* x, T* contrib, in
     VXG_LAUNCHED();
   }
   return VXG_OK;
+}
+
+// x = A^-1 b for the complex factors of every frequency; b shared by all
+// frequencies when b_stride is 0 (interleaved re, im).
+__global__ void bcast_cplx_kernel(long long n, int S, const cplx* __restrict__ b,
+                                  long long b_stride, cplx* __restrict__ x) {
+  const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gid >= n) return;
+  const long long f = gid / S, i = gid - f * S;
+  x[gid] = b[f * b_stride + i];
+}
+
+int launch_solve_ac(const Topo& t, int B, const void* factors, const double* b,
+                    long long b_stride, double* x, void* scratch, cudaStream_t s) {
+  const long long n = (long long)B * t.S;
+  if (!n) return VXG_OK;
+  bcast_cplx_kernel<<<nblk(n, 256), 256, 0, s>>>(n, t.S, (const cplx*)b, b_stride, (cplx*)x);
+  VXG_LAUNCHED();
+  return solve_levels<cplx>(t, B, (const cplx*)factors, (cplx*)x, (cplx*)scratch, 0, s);
 }
 
 int launch_solve(const Topo& t, int B, int precision, const void* factors, const double* data,

@@ -172,6 +172,9 @@ def concatenate(elements: Sequence[Element]) -> Element:
             B = max(x.shape[0] for x in xs if x.ndim == 2)
             xs = [x if x.ndim == 2 else x.expand(B, x.shape[-1]) for x in xs]
         setattr(out, f, torch.cat(xs, dim=-1))
+    for f in ("ac", "ac_phase"):
+        if hasattr(first, f):
+            setattr(out, f, torch.cat([_t(getattr(e, f)).reshape(-1) for e in elements]))
     if hasattr(first, "value") and isinstance(first.value, Signal):
         sigs = [e.value for e in elements]
         params = []
@@ -294,12 +297,21 @@ class _Source(Element):
     terminals = ("p", "n")
     fields = ()
 
-    def _init_source(self, nodes, value):
+    def _init_source(self, nodes, value, ac=0.0, ac_phase=0.0):
         self.nodes = self._devices(nodes)
         sig = as_signal(value)
         single = _is_single(nodes)
         self.value = sig.map(lambda x: x.reshape(1) if single and x.ndim == 0
                              else self._per_device(x))
+        # small-signal stimulus (host side only: AC analysis)
+        self.ac = self._per_device(ac)
+        self.ac_phase = self._per_device(ac_phase)
+
+    def phasor(self):
+        """``ac exp(j ac_phase)`` per device (numpy complex, sources.py:30-36)."""
+        ac = np.asarray(getattr(self, "ac", np.zeros(self.size)), dtype=float)
+        ph = np.asarray(getattr(self, "ac_phase", np.zeros(self.size)), dtype=float)
+        return np.broadcast_to(ac * np.exp(1j * np.deg2rad(ph)), (self.size,))
 
     @property
     def static(self):  # waveform type decides the kernel branch
@@ -352,8 +364,8 @@ class VoltageSource(_Source):
     internal_names = ("i",)
     kind = KIND_VSOURCE
 
-    def __init__(self, nodes, value: Signal | Any = 0.0):
-        self._init_source(nodes, value)
+    def __init__(self, nodes, value: Signal | Any = 0.0, ac=0.0, ac_phase=0.0):
+        self._init_source(nodes, value, ac, ac_phase)
 
 
 class CurrentSource(_Source):
@@ -362,8 +374,8 @@ class CurrentSource(_Source):
 
     kind = KIND_ISOURCE
 
-    def __init__(self, nodes, value: Signal | Any = 0.0):
-        self._init_source(nodes, value)
+    def __init__(self, nodes, value: Signal | Any = 0.0, ac=0.0, ac_phase=0.0):
+        self._init_source(nodes, value, ac, ac_phase)
 
 
 # =============================================================================
