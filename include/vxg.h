@@ -61,7 +61,9 @@ enum {
                                      1/smooth or 0] */
   VXG_KIND_DIODE = 6,       /* Diode        [is, 1/(n vt), tt, cj]                  */
   VXG_KIND_INDUCTOR = 7,    /* Inductor     [l, rs], one internal (the current)     */
-  VXG_KIND_VCCS = 8         /* VCCS         [gm], terminals (p, n, cp, cn)          */
+  VXG_KIND_VCCS = 8,        /* VCCS         [gm], terminals (p, n, cp, cn)          */
+  VXG_KIND_BJT = 9          /* BJT          [sign, is, 1/vt, 1/bf, 1/br, 1/vaf, tf, tr,
+                                             cje, cjc], terminals (c, b, e)     */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 

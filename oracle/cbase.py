@@ -64,7 +64,7 @@ def lib():
 
 KINDS = {"Resistor": 0, "Conductance": 0, "Capacitor": 1, "VoltageSource": 2,
          "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5, "Diode": 6, "Inductor": 7,
-         "VCCS": 8}
+         "VCCS": 8, "BJT": 9}
 WAVES = {"Constant": 0, "Step": 1, "Pulse": 2}
 
 
@@ -110,6 +110,12 @@ def _rows_of(el, b):
         return [torch.exp(inst(el.log_l)).expand(n), inst(el.rs).expand(n)]
     if name == "VCCS":
         return [inst(el.gm).expand(n)]
+    if name == "BJT":
+        full = lambda x: inst(x).expand(n)  # noqa: E731
+        sign = 1.0 if el.polarity == "npn" else -1.0
+        return [torch.full((n,), sign, dtype=torch.float64), torch.exp(full(el.log_is)),
+                1.0 / full(el.vt), torch.exp(-full(el.log_bf)), torch.exp(-full(el.log_br)),
+                full(el.inv_vaf), full(el.tf), full(el.tr), full(el.cje), full(el.cjc)]
     if name == "Level1MOSFET":  # voltax/elements/mosfet.py:208-257
         p = el.process
         w, l = torch.exp(inst(el.log_w)), torch.exp(inst(el.log_l))

@@ -21,7 +21,7 @@
 #include <string.h>
 
 enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5,
-       K_DIODE = 6, K_IND = 7, K_VCCS = 8 };
+       K_DIODE = 6, K_IND = 7, K_VCCS = 8, K_BJT = 9 };
 enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
 enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
 
@@ -321,6 +321,36 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
           I[0] = u[2]; I[1] = -u[2]; I[2] = rs * u[2] - (u[0] - u[1]);
           Q[2] = l * u[2];
           J[2] = cf; J[5] = -cf; J[6] = -cf; J[7] = cf; J[8] = cf * rs + cq * l;
+          break;
+        }
+        case K_BJT: { /* rows: sign, is, 1/vt, 1/bf, 1/br, 1/vaf, tf, tr, cje, cjc */
+          const double* p = g->params;
+          const int n = g->n;
+          const double sg = p[d], is = p[n + d], ivt = p[2 * n + d], ibf = p[3 * n + d];
+          const double ibr = p[4 * n + d], ivaf = p[5 * n + d], tf = p[6 * n + d];
+          const double tr = p[7 * n + d], cje = p[8 * n + d], cjc = p[9 * n + d];
+          const double vbe = sg * (u[1] - u[2]), vbc = sg * (u[1] - u[0]);
+          const double xf = vbe * ivt, xr = vbc * ivt;
+          const double ef = exp(fmin(xf, 40.0)), er = exp(fmin(xr, 40.0));
+          const double i_f = is * ((xf > 40.0 ? ef * (1.0 + xf - 40.0) : ef) - 1.0);
+          const double i_r = is * ((xr > 40.0 ? er * (1.0 + xr - 40.0) : er) - 1.0);
+          const double early = 1.0 + (vbe - vbc) * ivaf;
+          const double ic = (i_f - i_r) * early - i_r * ibr, ib = i_f * ibf + i_r * ibr;
+          I[0] = sg * ic; I[1] = sg * ib; I[2] = sg * (-ic - ib);
+          const double q_be = tf * i_f + cje * vbe, q_bc = tr * i_r + cjc * vbc;
+          Q[0] = sg * -q_bc; Q[1] = sg * (q_be + q_bc); Q[2] = sg * -q_be;
+          const double gf = is * (xf == 40.0 ? 0.5 * ef : ef) * ivt;
+          const double gr = is * (xr == 40.0 ? 0.5 * er : er) * ivt;
+          const double dbe[3] = {0.0, 1.0, -1.0}, dbc[3] = {-1.0, 1.0, 0.0};
+          for (int kk = 0; kk < 3; ++kk) {
+            const double dic = (gf * dbe[kk] - gr * dbc[kk]) * early +
+                               (i_f - i_r) * ivaf * (dbe[kk] - dbc[kk]) - gr * ibr * dbc[kk];
+            const double dib = gf * ibf * dbe[kk] + gr * ibr * dbc[kk];
+            const double dqbe = (tf * gf + cje) * dbe[kk], dqbc = (tr * gr + cjc) * dbc[kk];
+            J[0 * 3 + kk] = cf * dic - cq * dqbc;
+            J[1 * 3 + kk] = cf * dib + cq * (dqbe + dqbc);
+            J[2 * 3 + kk] = cf * (-dic - dib) - cq * dqbe;
+          }
           break;
         }
         case K_VCCS: {

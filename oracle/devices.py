@@ -12,6 +12,7 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * Diode               voltax/elements/semiconductor.py:17-70
 * Inductor            voltax/elements/passive.py:62-87
 * VCCS                voltax/elements/controlled.py:46-60
+* BJT                 voltax/elements/semiconductor.py:73-135
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
                       ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
 * Constant/Step/Pulse voltax/signals.py:58-114
@@ -77,6 +78,12 @@ def _jmin(a, b):
     return torch.where(a < b, a, torch.where(a > b, b, 0.5 * (a + b)))
 
 
+def _explin(u, u_max=40.0):
+    """exp(u), continued linearly above u_max (semiconductor.py:17-24)."""
+    e = torch.exp(_jmin(u, torch.full_like(u, u_max)))
+    return torch.where(u > u_max, e * (1.0 + u - u_max), e)
+
+
 class GroupModel:
     """One element group of one circuit instance."""
 
@@ -86,7 +93,7 @@ class GroupModel:
         self.T = len(el.terminals)
         self.K = el.n_internal
         self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET", "Diode",
-                                         "Inductor")
+                                         "Inductor", "BJT")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -118,6 +125,13 @@ class GroupModel:
         if name == "Diode":
             i = self._diode_current(v[..., 0] - v[..., 1])
             return torch.stack([i, -i], -1), None
+        if name == "BJT":  # semiconductor.py:119-128
+            s = 1.0 if el.polarity == "npn" else -1.0
+            vbe, vbc, i_f, i_r = self._bjt_junctions(v, s)
+            early = 1.0 + (vbe - vbc) * _inst(el.inv_vaf, b)
+            ic = (i_f - i_r) * early - i_r * torch.exp(-_inst(el.log_br, b))
+            ib = i_f * torch.exp(-_inst(el.log_bf, b)) + i_r * torch.exp(-_inst(el.log_br, b))
+            return s * torch.stack([ic, ib, -ic - ib], -1), None
         if name == "Inductor":  # passive.py:62-87
             i = x[..., 0]
             rs = _inst(el.rs, b)
@@ -163,6 +177,12 @@ class GroupModel:
             q_gs, q_gd = cov * (vg - vs), cov * (vg - vd)
             overlap = torch.stack([-q_gd, q_gs + q_gd, -q_gs, torch.zeros_like(q_gs)], -1)
             return s * (intrinsic + overlap), None
+        if name == "BJT":  # semiconductor.py:130-135
+            s = 1.0 if el.polarity == "npn" else -1.0
+            vbe, vbc, i_f, i_r = self._bjt_junctions(v, s)
+            q_be = _inst(el.tf, b) * i_f + _inst(el.cje, b) * vbe
+            q_bc = _inst(el.tr, b) * i_r + _inst(el.cjc, b) * vbc
+            return s * torch.stack([-q_bc, q_be + q_bc, -q_be], -1), None
         if name == "Diode":  # q = tt i + cj v (semiconductor.py:68-70)
             vd = v[..., 0] - v[..., 1]
             q = _inst(el.tt, b) * self._diode_current(vd) + _inst(el.cj, b) * vd
@@ -191,14 +211,19 @@ class GroupModel:
         i_r = softplus((vp - (vd - vb)) / (2 * vt)) ** 2
         return i_f, i_r
 
+    def _bjt_junctions(self, v, s):
+        el, b = self.el, self.b
+        vc, vb, ve = (s * v[..., k] for k in range(3))
+        vbe, vbc = vb - ve, vb - vc
+        i_s, vt = torch.exp(_inst(el.log_is, b)), _inst(el.vt, b)
+        return vbe, vbc, i_s * (_explin(vbe / vt) - 1.0), i_s * (_explin(vbc / vt) - 1.0)
+
     def _diode_current(self, vd):
         """is (explin(vd / (n vt)) - 1), explin linear above 40
         (semiconductor.py:17-24, 62-63)."""
         el, b = self.el, self.b
         u = vd / (_inst(el.n, b) * _inst(el.vt, b))
-        e = torch.exp(_jmin(u, torch.full_like(u, 40.0)))
-        ex = torch.where(u > 40.0, e * (1.0 + u - 40.0), e)
-        return torch.exp(_inst(el.log_is, b)) * (ex - 1.0)
+        return torch.exp(_inst(el.log_is, b)) * (_explin(u) - 1.0)
 
     # Level 1 (mosfet.py:229-253). jnp.maximum / jnp.minimum give each side
     # half the derivative at a tie; _jmax / _jmin do the same under torch AD.

@@ -18,3 +18,26 @@ def mixed_circuit():
     b.vccs("d", "0", "b", "0", 2e-3, name="G1")
     b.resistor("d", "0", 1e3, name="R3")
     return b.build()
+
+
+def bjt_amplifier():
+    """A common-emitter NPN stage (emitter degeneration, Early effect,
+    junction and transit charges) with a PNP current-mirror load, driven by a
+    pulse through a coupling RC."""
+    from voltax_gb300.signals import Pulse
+    b = CircuitBuilder()
+    b.vsource("vcc", "0", 5.0, name="Vcc")
+    b.vsource("in", "0", Pulse(0.0, 0.2, delay=1e-9, rise=1e-9, fall=1e-9, width=5e-9,
+                               period=20e-9), name="Vin")
+    b.resistor("in", "x", 1e3, name="Rs")
+    b.capacitor("x", "base", 1e-9, name="Cc")
+    b.resistor("vcc", "base", 100e3, name="Rb1")
+    b.resistor("base", "0", 20e3, name="Rb2")
+    kw = dict(is_=1e-15, bf=120.0, br=2.0, vaf=60.0, tf=0.3e-9, tr=5e-9, cje=1e-12, cjc=0.5e-12)
+    b.bjt("out", "base", "emit", "npn", name="Q1", **kw)
+    b.resistor("emit", "0", 500.0, name="Re")
+    b.bjt("mir", "mir", "vcc", "pnp", name="Q2", **kw)
+    b.bjt("out", "mir", "vcc", "pnp", name="Q3", **kw)
+    b.resistor("mir", "0", 20e3, name="Rref")
+    b.capacitor("out", "0", 0.2e-12, name="CL")
+    return b.build()

@@ -47,9 +47,10 @@ CIRCUITS = {
     "ring_l1": lambda: workloads.ring_oscillator_level1(5, gamma=0.3)[0],
     "ring_l1_smooth": lambda: workloads.ring_oscillator_level1(5, smooth=0.02, gamma=0.3)[0],
 }
-from circuits import mixed_circuit  # noqa: E402
+from circuits import bjt_amplifier, mixed_circuit  # noqa: E402
 
 CIRCUITS["mixed"] = mixed_circuit
+CIRCUITS["bjt"] = bjt_amplifier
 LINEAR = ("rc_ladder", "grid")
 
 
@@ -240,6 +241,38 @@ def test_mixed_devices_transient_matches_oracle(method, engine):
     scale = max(1.0, np.abs(zr).max())
     assert np.max(np.abs(v - zr)) < 1e-9 * scale
     assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_bjt_amplifier_transient_matches_oracle(engine):
+    c = bjt_amplifier()
+    ts = np.linspace(0.0, 6e-9, 61)
+    sol = vx.transient(c, ts, ic="dc", method="trap", options=vx.Options(engine=engine))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc", method="trap")
+    assert bool(sol.converged.all()) and okr.all()
+    v = sol.z.cpu().numpy()[:, : c.n_nodes]
+    assert np.max(np.abs(v - zr[:, : c.n_nodes])) < 1e-9 * max(1.0, np.abs(zr).max())
+    assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+def test_bjt_dc_gradient_matches_finite_differences():
+    c = bjt_amplifier()
+    out = c.node("out")
+    for gname in ("BJT_npn", "BJT_pnp"):
+        el = c.elements[gname]
+        for field in ("log_is", "log_bf", "inv_vaf"):
+            e2 = el.with_nodes(el.nodes)
+            setattr(e2, field, getattr(el, field).clone().requires_grad_(True))
+            vx.dc(c.replace(gname, e2)).z[out].backward()
+            g = getattr(e2, field).grad.numpy().sum()
+            h = 1e-6
+            vals = []
+            for sgn in (1, -1):
+                e3 = el.with_nodes(el.nodes)
+                setattr(e3, field, getattr(el, field).clone() + sgn * h)
+                vals.append(float(vx.dc(c.replace(gname, e3)).z[out]))
+            np.testing.assert_allclose(g, (vals[0] - vals[1]) / (2 * h), rtol=1e-5, atol=1e-9)
 
 
 def test_mixed_devices_dc_gradient_matches_finite_differences():

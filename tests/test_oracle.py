@@ -144,7 +144,7 @@ def test_rc_ladder_dc_sweep_values():
         assert ok and np.isclose(z[c.node("out")], r / (r + 3e3))
 
 
-from circuits import mixed_circuit  # noqa: E402
+from circuits import bjt_amplifier, mixed_circuit  # noqa: E402
 
 
 def _cases():
@@ -154,6 +154,7 @@ def _cases():
         "ring": lambda: workloads.ring_oscillator(9)[0],
         "ring_l1": lambda: workloads.ring_oscillator_level1(9, gamma=0.3)[0],
         "mixed": mixed_circuit,
+        "bjt": bjt_amplifier,
     }
 
 
@@ -223,7 +224,8 @@ def test_power_grid_dc_matches_superlu():
 
 
 @pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap"),
-                                         ("ring_l1", "be"), ("mixed", "trap")])
+                                         ("ring_l1", "be"), ("mixed", "trap"),
+                                         ("bjt", "trap")])
 def test_compiled_baseline_matches_oracle(name, method):
     """oracle/cvx.c (the timed CPU baseline) equals the torch restatement."""
     from oracle import cbase

@@ -20,7 +20,7 @@ from .signals import Constant, Signal
 _PREFIX = {
     el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
     el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
-    el.Inductor: "L", el.Diode: "D", el.VCCS: "G",
+    el.Inductor: "L", el.Diode: "D", el.VCCS: "G", el.BJT: "Q",
 }
 
 
@@ -111,6 +111,9 @@ class CircuitBuilder:
 
     def diode(self, a, k, name=None, group=None, **params) -> str:
         return self.add(el.Diode((a, k), **params), name, group)
+
+    def bjt(self, c, b, e, polarity="npn", name=None, group=None, **params) -> str:
+        return self.add(el.BJT((c, b, e), polarity, **params), name, group)
 
     def vccs(self, p, n, cp, cn, gm, name=None, group=None) -> str:
         return self.add(el.VCCS((p, n, cp, cn), gm), name, group)

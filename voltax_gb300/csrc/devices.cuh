@@ -674,6 +674,49 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
       }
       break;
     }
+    case VXG_KIND_BJT: {  // voltax/elements/semiconductor.py:73-135, u = (vc, vb, ve)
+      const double sg = prm(g, 0, b, d), i_s = prm(g, 1, b, d), inv_vt = prm(g, 2, b, d);
+      const double ibf = prm(g, 3, b, d), ibr = prm(g, 4, b, d), ivaf = prm(g, 5, b, d);
+      const double tf = prm(g, 6, b, d), tr = prm(g, 7, b, d);
+      const double cje = prm(g, 8, b, d), cjc = prm(g, 9, b, d);
+      const double vc = sg * u[0], vb = sg * u[1], ve = sg * u[2];
+      const double vbe = vb - ve, vbc = vb - vc;
+      const double xf = vbe * inv_vt, xr = vbc * inv_vt;
+      const double ef = exp(fmin(xf, 40.0)), er = exp(fmin(xr, 40.0));
+      const double exf = xf > 40.0 ? ef * (1.0 + xf - 40.0) : ef;
+      const double exr = xr > 40.0 ? er * (1.0 + xr - 40.0) : er;
+      const double i_f = i_s * (exf - 1.0), i_r = i_s * (exr - 1.0);
+      const double early = 1.0 + (vbe - vbc) * ivaf;
+      const double ic = (i_f - i_r) * early - i_r * ibr;
+      const double ib = i_f * ibf + i_r * ibr;
+      if (wf) {
+        fo[d] = sg * ic;
+        fo[n + d] = sg * ib;
+        fo[2 * n + d] = sg * (-ic - ib);
+      }
+      const double q_be = tf * i_f + cje * vbe, q_bc = tr * i_r + cjc * vbc;
+      if (wq) {
+        qo[d] = sg * -q_bc;
+        qo[n + d] = sg * (q_be + q_bc);
+        qo[2 * n + d] = sg * -q_be;
+      }
+      if (wj) {
+        const double gf = i_s * (xf == 40.0 ? 0.5 * ef : ef) * inv_vt;
+        const double gr = i_s * (xr == 40.0 ? 0.5 * er : er) * inv_vt;
+        const double dbe[3] = {0.0, 1.0, -1.0}, dbc[3] = {-1.0, 1.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double dic = (gf * dbe[k] - gr * dbc[k]) * early +
+                             (i_f - i_r) * ivaf * (dbe[k] - dbc[k]) - gr * ibr * dbc[k];
+          const double dib = gf * ibf * dbe[k] + gr * ibr * dbc[k];
+          const double dqbe = (tf * gf + cje) * dbe[k], dqbc = (tr * gr + cjc) * dbc[k];
+          jo[(0 * 3 + k) * n + d] = (JT)(cf * dic + cq * -dqbc);
+          jo[(1 * 3 + k) * n + d] = (JT)(cf * dib + cq * (dqbe + dqbc));
+          jo[(2 * 3 + k) * n + d] = (JT)(cf * (-dic - dib) + cq * -dqbe);
+        }
+      }
+      break;
+    }
     case VXG_KIND_VCCS: {  // voltax/elements/controlled.py:46-60
       const double gm = prm(g, 0, b, d);
       const double i = gm * (u[2] - u[3]);

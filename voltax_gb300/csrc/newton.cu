@@ -296,6 +296,30 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
     case VXG_KIND_INDUCTOR:
       out[2] = cf * (p[1] * mk(u[2])) + cq * (p[0] * mk(u[2]));
       break;
+    case VXG_KIND_BJT: {
+      const double sg = p[0].v;
+      const Dual i_s = p[1], inv_vt = p[2], ibf = p[3], ibr = p[4], ivaf = p[5];
+      const Dual tf = p[6], tr = p[7], cje = p[8], cjc = p[9];
+      const double vbe = sg * (u[1] - u[2]), vbc = sg * (u[1] - u[0]);
+      const Dual xf = mk(vbe) * inv_vt, xr = mk(vbc) * inv_vt;
+      const Dual ef = dexp(xf.v > 40.0 ? mk(40.0) : xf), er = dexp(xr.v > 40.0 ? mk(40.0) : xr);
+      const Dual exf = xf.v > 40.0 ? ef * (1.0 + (xf - mk(40.0))) : ef;
+      const Dual exr = xr.v > 40.0 ? er * (1.0 + (xr - mk(40.0))) : er;
+      const Dual i_f = i_s * (exf - mk(1.0)), i_r = i_s * (exr - mk(1.0));
+      const Dual early = 1.0 + mk(vbe - vbc) * ivaf;
+      const Dual ic = (i_f - i_r) * early - i_r * ibr;
+      const Dual ib = i_f * ibf + i_r * ibr;
+      out[0] = cf * (sg * ic);
+      out[1] = cf * (sg * ib);
+      out[2] = cf * (sg * (-(ic + ib)));
+      if (cq != 0.0) {
+        const Dual q_be = tf * i_f + cje * mk(vbe), q_bc = tr * i_r + cjc * mk(vbc);
+        out[0] = out[0] + cq * (sg * (-q_bc));
+        out[1] = out[1] + cq * (sg * (q_be + q_bc));
+        out[2] = out[2] + cq * (sg * (-q_be));
+      }
+      break;
+    }
     case VXG_KIND_VCCS: {
       const Dual i = p[0] * mk(u[2] - u[3]);
       out[0] = cf * i;

@@ -40,6 +40,7 @@ KIND_L1 = 5
 KIND_DIODE = 6
 KIND_INDUCTOR = 7
 KIND_VCCS = 8
+KIND_BJT = 9
 
 
 def _t(x) -> torch.Tensor:
@@ -585,5 +586,53 @@ class VCCS(Element):
         return [self.gm]
 
 
+class BJT(Element):
+    """Ebers-Moll (transport form) bipolar transistor with Early effect
+    (semiconductor.py:73-135); terminals ``(c, b, e)``::
+
+        i_f = is (explin(v_be/vt) - 1),   i_r = is (explin(v_bc/vt) - 1)
+        i_c = (i_f - i_r)(1 + v_ce/vaf) - i_r/br,   i_b = i_f/bf + i_r/br
+        q_be = tf i_f + cje v_be,   q_bc = tr i_r + cjc v_bc
+
+    PNP mirrors all voltages and currents. Kernel parameter rows: sign, is,
+    1/vt, 1/bf, 1/br, 1/vaf, tf, tr, cje, cjc."""
+
+    terminals = ("c", "b", "e")
+    fields = ("log_is", "log_bf", "log_br", "inv_vaf", "tf", "tr", "cje", "cjc", "vt")
+    static = ("polarity",)
+    kind = KIND_BJT
+    has_charges = True
+
+    def __init__(self, nodes, polarity: str = "npn", is_=1e-16, bf=100.0, br=1.0,
+                 vaf=float("inf"), tf=0.0, tr=0.0, cje=0.0, cjc=0.0, vt=VT_300K):
+        if polarity not in ("npn", "pnp"):
+            raise ValueError(f"polarity must be 'npn' or 'pnp', got {polarity!r}")
+        self.nodes = self._devices(nodes)
+        self.polarity = polarity
+        self.log_is = self._log_per_device(is_)
+        self.log_bf = self._log_per_device(bf)
+        self.log_br = self._log_per_device(br)
+        self.inv_vaf = self._per_device(1.0 / _t(vaf))
+        self.tf, self.tr = self._per_device(tf), self._per_device(tr)
+        self.cje, self.cjc = self._per_device(cje), self._per_device(cjc)
+        self.vt = self._per_device(vt)
+
+    @property
+    def sign(self) -> float:
+        return 1.0 if self.polarity == "npn" else -1.0
+
+    def gpu_params(self):
+        i_s = torch.exp(self.log_is)
+        shape = i_s.shape
+
+        def full(x):
+            return _t(x).expand(shape)
+
+        return [full(self.sign), i_s, (1.0 / self.vt).expand(shape),
+                torch.exp(-self.log_bf).expand(shape), torch.exp(-self.log_br).expand(shape),
+                self.inv_vaf.expand(shape), self.tf.expand(shape), self.tr.expand(shape),
+                self.cje.expand(shape), self.cjc.expand(shape)]
+
+
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
-                 EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS)
+                 EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS, BJT)
