@@ -125,6 +125,8 @@ def parse():
     ap.add_argument("--instances", type=int, default=None)
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
+    ap.add_argument("--refine", type=int, default=1,
+                    help="FP64 refinement sweeps per solve of the FP32-factor form")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
     ap.add_argument("--epochs", type=int, default=40, help="ota_warm: training epochs")
@@ -331,7 +333,7 @@ def main():
 
     dev_circuit = to_device(circuit, dev)
     host_circuit = to_device(circuit, None, pin=True)
-    opts32 = vx.Options(precision="f32", engine=a.engine)
+    opts32 = vx.Options(precision="f32", engine=a.engine, refine=a.refine)
     opts64 = vx.Options(precision="f64", engine=a.engine)
     from voltax_gb300 import symbolic
     from voltax_gb300.analysis import _Call
@@ -450,6 +452,7 @@ def main():
         "config": {"workload": w.label(B, len(ts)), "instances": B,
                    "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,
+                   "refine": a.refine,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "plain_fp64": {"value": value64, "unit": UNIT, "speedup": value / value64},

@@ -78,11 +78,12 @@ def test_dc_sweep_with_callable_and_gradient():
     expected = sum(r / (r + 3e3) for r in (1e3, 1e4))
     x = torch.zeros((), dtype=torch.float64, requires_grad=True)
     val = out_sum(x)
-    assert np.isclose(float(val), expected)
+    assert np.isclose(val.item(), expected)
     val.backward()
     h = 1e-6
-    fd = (float(out_sum(torch.tensor(h, dtype=torch.float64))) -
-          float(out_sum(torch.tensor(-h, dtype=torch.float64)))) / (2 * h)
+    with torch.no_grad():
+        fd = (out_sum(torch.tensor(h, dtype=torch.float64)).item() -
+              out_sum(torch.tensor(-h, dtype=torch.float64)).item()) / (2 * h)
     assert np.isclose(float(x.grad), fd, rtol=1e-5)
 
 
