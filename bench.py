@@ -125,7 +125,7 @@ def parse():
     ap.add_argument("--instances", type=int, default=None)
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
-    ap.add_argument("--refine", type=int, default=1,
+    ap.add_argument("--refine", type=int, default=0,
                     help="FP64 refinement sweeps per solve of the FP32-factor form")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
