@@ -125,8 +125,9 @@ def parse():
     ap.add_argument("--instances", type=int, default=None)
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
-    ap.add_argument("--refine", type=int, default=0,
-                    help="FP64 refinement sweeps per solve of the FP32-factor form")
+    ap.add_argument("--refine", type=int, default=None,
+                    help="FP64 refinement sweeps per solve of the FP32-factor form "
+                         "(default: the library's choice per engine)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
     ap.add_argument("--epochs", type=int, default=40, help="ota_warm: training epochs")
@@ -452,7 +453,7 @@ def main():
         "config": {"workload": w.label(B, len(ts)), "instances": B,
                    "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,
-                   "refine": a.refine,
+                   "refine": _Call(dev_circuit, opts32).refine,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "plain_fp64": {"value": value64, "unit": UNIT, "speedup": value / value64},

@@ -41,7 +41,11 @@ class Options:
     iterative refinement (measured on the 4096-instance adder: the same
     iteration counts and 8.7e-13 V agreement with the plain form). `refine`
     adds inner refinement sweeps ``dz += J^-1 (b - J dz)`` per solve against
-    the FP64 Jacobian values, for systems too ill-conditioned for that. `solver` is accepted for compatibility: every solve
+    the FP64 Jacobian values; ``None`` picks 0 for the fused kernel (small
+    systems, where a sweep costs as much as a Newton iteration) and 1 for
+    the generic engine (large systems, where it saves a refactorization:
+    the 100 x 100 grid converges in 2 Newton iterations with it, 3 without).
+    Adjoint (transposed) solves always refine, since no Newton loop follows. `solver` is accepted for compatibility: every solve
     uses the supernodal GPU factorization (a circuit of at most ``2 * leaf``
     unknowns is one dense supernode).
 
@@ -61,7 +65,7 @@ class Options:
     solver: str = "auto"
     sparse_threshold: int = SPARSE_THRESHOLD
     precision: str = "f64"
-    refine: int = 0
+    refine: int | None = None
     engine: str = "auto"
     block: int = 0
     autotune: bool = True
@@ -77,11 +81,13 @@ class Options:
         if self.precision not in ("f64", "f32"):
             raise ValueError(f"precision must be 'f64' or 'f32', got {self.precision!r}")
 
-    def native(self, max_steps: int | None = None) -> L.NewtonOpts:
+    def native(self, max_steps: int | None = None, refine: int | None = None
+               ) -> L.NewtonOpts:
+        r = refine if refine is not None else (self.refine or 0)
         return L.NewtonOpts(self.max_steps if max_steps is None else max_steps, self.rtol,
                             self.atol, self.max_dv,
                             L.VXG_F32 if self.precision == "f32" else L.VXG_F64,
-                            self.refine, self.block)
+                            r, self.block)
 
 
 class Solution:
@@ -151,6 +157,7 @@ class _Call:
         if self.fused and options.engine == "auto" and options.autotune and not options.block:
             engine, self.block = autotune.choose(self)
             self.fused = engine == "fused"
+        self.refine = options.refine if options.refine is not None else (0 if self.fused else 1)
 
     def _use_fused(self) -> bool:
         if self.o.engine == "generic":
@@ -173,7 +180,7 @@ class _Call:
         z_out = torch.empty((T, self.B, self.eng.S), dtype=torch.float64, device=dev)
         conv = torch.empty((T, self.B), dtype=torch.int32, device=dev)
         iters = torch.empty((T, self.B), dtype=torch.int32, device=dev)
-        nat = o.native()
+        nat = o.native(refine=self.refine)
         nat.block = self.block
         L.check(self.eng.lib.vxg_fused_run(
             self.eng.handle, self.B, self.params, mode, T, ts_d.data_ptr(), z0.data_ptr(),
@@ -184,7 +191,7 @@ class _Call:
 
     def newton(self, mode, z, t, t_prev=0.0, z_prev=None, gmin=None, max_steps=None,
                mask=None, factors=None):
-        o = self.o.native(max_steps)
+        o = self.o.native(max_steps, refine=self.refine)
         gmin_t = None
         gmin_s = self.o.gmin
         if torch.is_tensor(gmin):
@@ -272,7 +279,8 @@ class _DCRoot(torch.autograd.Function):
         data = ctx.data if call.prec == L.VXG_F32 else None
         L.check(eng.lib.vxg_solve(eng.handle, call.B, call.prec, ctx.fac.data_ptr(),
                                   None if data is None else data.data_ptr(), gz.data_ptr(),
-                                  lam.data_ptr(), 1, call.o.refine if data is not None else 0,
+                                  lam.data_ptr(), 1, max(call.refine, 2) if data is not None
+                                  else 0,
                                   call.ws.data_ptr(), stream_ptr()), "vxg_solve")
         grads_out = []
         bufs = []
@@ -462,7 +470,7 @@ def transient(circuit, ts, ic="dc", method: str = "be",
     z_out = torch.empty((T, B, S), dtype=torch.float64, device=dev)
     conv = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
     iters = torch.empty((T, n_inst), dtype=torch.int32, device=dev)
-    o = options.native()
+    o = options.native(refine=call.refine)
     L.check(call.eng.lib.vxg_transient(
         call.eng.handle, B, call.params, mode, T, ts_np.ctypes.data_as(L.PF64), z0.data_ptr(),
         options.gmin, C.byref(o), z_out.data_ptr(), conv.data_ptr(), iters.data_ptr(),
