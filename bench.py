@@ -205,6 +205,46 @@ def _cpu_run(w, sysm, z0, ts):
     return sysm.run(ts, z0=z0, method=w.method, dc_first=z0 is None)
 
 
+def cpu_superlu(w, instances, min_seconds=5.0):
+    """A conventional CPU sparse baseline for the DC workloads: SuperLU
+    (scipy.sparse.linalg.splu) factor + solve of the Newton matrix at the
+    zero state, one thread, repeated for `min_seconds` (a DC solve of these
+    linear circuits is one such factor + solve plus a convergence check)."""
+    if w.analysis != "dc" or w.name == "ota_warm":
+        return None
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from oracle import stamp as ost
+    from voltax_gb300 import symbolic
+    try:
+        from threadpoolctl import threadpool_limits
+    except ImportError:  # not installed on every box; SuperLU itself is serial
+        threadpool_limits = None
+    c = w.circuit(instances, seed=0)
+    st = symbolic.structure(c)
+    z = np.zeros(c.size)
+    A = sp.csr_matrix((ost.jacobian(c, st, z, 0.0, 1.0, 0.0), st.indices, st.indptr),
+                      shape=(c.size, c.size)).tocsc()
+    rhs = -ost.f(c, z, 0.0)
+    per = instances if w.name == "grids" else 1
+    ctx = threadpool_limits(1) if threadpool_limits else None
+    try:
+        if ctx:
+            ctx.__enter__()
+        spla.splu(A).solve(rhs)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < min_seconds:
+            spla.splu(A).solve(rhs)
+            n += 1
+        secs = time.perf_counter() - t0
+    finally:
+        if ctx:
+            ctx.__exit__(None, None, None)
+    return {"value": n * per / secs, "unit": UNIT, "cores": 1, "kind": "superlu",
+            "sample": f"{n} SuperLU factor + solve of the {c.size}-unknown Newton matrix, "
+                      f"{secs:.1f} s (scipy.sparse.linalg.splu)"}
+
+
 def cpu_baseline(w, n_t, instances, min_seconds=10.0):
     """The compiled CPU restatement (oracle/cvx.c), one thread, whole
     instances until `min_seconds` have passed."""
@@ -311,6 +351,7 @@ def main():
     if w.name == "grids":
         main_grids(a, w, cpu)
         return
+    superlu = cpu_superlu(w, a.instances) if rank == 0 and not a.no_cpu else None
 
     import torch
     import voltax_gb300 as vx
@@ -466,6 +507,8 @@ def main():
         "cpu_baseline": cpu,
         "roofline": roofline,
     }
+    if superlu:
+        line["cpu_superlu"] = superlu
     print(json.dumps(line))
 
 
