@@ -468,3 +468,31 @@ def test_fused_wide_supernode_ota_chain_matches_generic_and_oracle():
         assert okr
         assert rel(fused.z[b, :nv].cpu().numpy(), zr[:nv]) <= 1e-9
         assert int(gen.iterations[b]) == itr
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_one_singular_instance_fails_alone(engine):
+    """A batch where instance 1 has a node cut off from every DC path
+    (its only resistor to the rest set to an infinite resistance, i.e.
+    g = 0): that instance reports converged = False; the others converge
+    to their own operating points, as voltax does per instance under vmap."""
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.resistor("in", "a", 1e3, name="R1")
+    b.resistor("a", "0", 2e3, name="R2")
+    b.resistor("a", "f", 5e3, name="R3")
+    b.capacitor("f", "0", 1e-12, name="C1")
+    c = b.build()
+    el = c.elements["Resistor"]
+    e2 = el.with_nodes(el.nodes)
+    log_r = el.log_r.expand(3, el.size).clone()
+    idx = c.devices("Resistor").index("R3")
+    log_r[1, idx] = float("inf")
+    e2.log_r = log_r
+    cb = c.replace("Resistor", e2)
+    sol = vx.dc(cb, options=vx.Options(engine=engine))
+    conv = sol.converged.cpu().numpy()
+    assert conv.tolist() == [True, False, True]
+    ref = vx.dc(c, options=vx.Options(engine=engine))
+    for k in (0, 2):
+        assert float((sol.z[k] - ref.z).abs().max()) < 1e-12
