@@ -472,16 +472,19 @@ def test_fused_wide_supernode_ota_chain_matches_generic_and_oracle():
 
 @pytest.mark.parametrize("engine", ENGINES)
 def test_one_singular_instance_fails_alone(engine):
-    """A batch where instance 1 has a node cut off from every DC path
-    (its only resistor to the rest set to an infinite resistance, i.e.
-    g = 0): that instance reports converged = False; the others converge
-    to their own operating points, as voltax does per instance under vmap."""
+    """A batch where instance 1 drives 1 mA into a node cut off from every
+    DC path (its only resistor set to an infinite resistance, g = 0): only
+    gmin holds that node, at 1e9 V, which damped Newton with gmin stepping
+    cannot reach. That instance reports converged = False; the others
+    converge to their own operating points, as voltax does per instance
+    under vmap."""
     b = CircuitBuilder()
     b.vsource("in", "0", 1.0, name="Vin")
     b.resistor("in", "a", 1e3, name="R1")
     b.resistor("a", "0", 2e3, name="R2")
     b.resistor("a", "f", 5e3, name="R3")
     b.capacitor("f", "0", 1e-12, name="C1")
+    b.isource("0", "f", 1e-3, name="I1")
     c = b.build()
     el = c.elements["Resistor"]
     e2 = el.with_nodes(el.nodes)
