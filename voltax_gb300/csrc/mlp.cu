@@ -54,6 +54,20 @@ __device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
 __device__ __forceinline__ void stage(bf16 (*s)[BK + PAD], const Operand& op, long long o0,
                                       int r0, long long O, int R) {
   const bf16 zero = __float2bfloat16_rn(0.f);
+  // 16-byte loads when the reduction dimension is contiguous, rows start on
+  // 16-byte boundaries and the slab is complete
+  const bool vec = op.sr == 1 && (op.so & 7) == 0 &&
+                   (reinterpret_cast<uintptr_t>(op.p) & 15) == 0 && r0 + BK <= R;
+  if (vec) {
+    for (int e = threadIdx.x; e < BM * BK / 8; e += NTH) {
+      const int o = e / (BK / 8), c8 = (e % (BK / 8)) * 8;
+      const long long go = o0 + o;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (go < O) v = *reinterpret_cast<const uint4*>(op.p + go * op.so + r0 + c8);
+      *reinterpret_cast<uint4*>(&s[o][c8]) = v;
+    }
+    return;
+  }
   if (op.sr == 1) {
     for (int e = threadIdx.x; e < BM * BK; e += NTH) {
       const int o = e / BK, r = e % BK;
