@@ -24,12 +24,6 @@
 
 namespace vxg {
 
-struct DevEval {
-  double I[kMaxM];
-  double Q[kMaxM];
-  double J[kMaxM * kMaxM];
-};
-
 __device__ __forceinline__ double prm(const GroupDev& g, int row, int b, int d) {
   return g.params[row * g.row_stride + (long long)b * g.batch_stride + d];
 }
