@@ -62,8 +62,13 @@ enum {
   VXG_KIND_DIODE = 6,       /* Diode        [is, 1/(n vt), tt, cj]                  */
   VXG_KIND_INDUCTOR = 7,    /* Inductor     [l, rs], one internal (the current)     */
   VXG_KIND_VCCS = 8,        /* VCCS         [gm], terminals (p, n, cp, cn)          */
-  VXG_KIND_BJT = 9          /* BJT          [sign, is, 1/vt, 1/bf, 1/br, 1/vaf, tf, tr,
+  VXG_KIND_BJT = 9,         /* BJT          [sign, is, 1/vt, 1/bf, 1/br, 1/vaf, tf, tr,
                                              cje, cjc], terminals (c, b, e)     */
+  VXG_KIND_VCVS = 10,       /* VCVS         [gain], (p, n, cp, cn) + current i      */
+  VXG_KIND_CCCS = 11,       /* CCCS         [gain], (p, n, cp, cn) + sense current  */
+  VXG_KIND_CCVS = 12,       /* CCVS         [r], (p, n, cp, cn) + i, sense current  */
+  VXG_KIND_XFMR = 13        /* Transformer  [l1, l2, k sqrt(l1 l2)], (p1, n1, p2, n2)
+                                             + winding currents i1, i2          */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 

@@ -64,7 +64,7 @@ def lib():
 
 KINDS = {"Resistor": 0, "Conductance": 0, "Capacitor": 1, "VoltageSource": 2,
          "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5, "Diode": 6, "Inductor": 7,
-         "VCCS": 8, "BJT": 9}
+         "VCCS": 8, "BJT": 9, "VCVS": 10, "CCCS": 11, "CCVS": 12, "Transformer": 13}
 WAVES = {"Constant": 0, "Step": 1, "Pulse": 2}
 
 
@@ -110,6 +110,13 @@ def _rows_of(el, b):
         return [torch.exp(inst(el.log_l)).expand(n), inst(el.rs).expand(n)]
     if name == "VCCS":
         return [inst(el.gm).expand(n)]
+    if name in ("VCVS", "CCCS"):
+        return [inst(el.gain).expand(n)]
+    if name == "CCVS":
+        return [inst(el.r).expand(n)]
+    if name == "Transformer":
+        l1, l2 = torch.exp(inst(el.log_l1)).expand(n), torch.exp(inst(el.log_l2)).expand(n)
+        return [l1, l2, inst(el.k).expand(n) * torch.sqrt(l1 * l2)]
     if name == "BJT":
         full = lambda x: inst(x).expand(n)  # noqa: E731
         sign = 1.0 if el.polarity == "npn" else -1.0

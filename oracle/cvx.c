@@ -21,7 +21,8 @@
 #include <string.h>
 
 enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5,
-       K_DIODE = 6, K_IND = 7, K_VCCS = 8, K_BJT = 9 };
+       K_DIODE = 6, K_IND = 7, K_VCCS = 8, K_BJT = 9, K_VCVS = 10, K_CCCS = 11,
+       K_CCVS = 12, K_XFMR = 13 };
 enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
 enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
 
@@ -257,8 +258,8 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
     const cvx_group* g = &s->groups[gi];
     const int m = g->T + g->K;
     for (int d = 0; d < g->n; ++d) {
-      double u[4], I[4] = {0, 0, 0, 0}, Q[4] = {0, 0, 0, 0}, J[16];
-      int row[4];
+      double u[6], I[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, J[36];
+      int row[6];
       for (int i = 0; i < g->T; ++i) {
         const int nd = g->nodes[d * g->T + i];
         u[i] = nd >= 0 ? z[nd] : 0.0;
@@ -351,6 +352,37 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
             J[1 * 3 + kk] = cf * dib + cq * (dqbe + dqbc);
             J[2 * 3 + kk] = cf * (-dic - dib) - cq * dqbe;
           }
+          break;
+        }
+        case K_VCVS: { /* (p, n, cp, cn, i) */
+          const double a = g->params[d];
+          I[0] = u[4]; I[1] = -u[4]; I[4] = (u[0] - u[1]) - a * (u[2] - u[3]);
+          J[4] = cf; J[9] = -cf; J[20] = cf; J[21] = -cf; J[22] = -cf * a; J[23] = cf * a;
+          break;
+        }
+        case K_CCCS: { /* (p, n, cp, cn, i_sense) */
+          const double a = g->params[d];
+          I[0] = a * u[4]; I[1] = -a * u[4]; I[2] = u[4]; I[3] = -u[4]; I[4] = u[2] - u[3];
+          J[4] = cf * a; J[9] = -cf * a; J[14] = cf; J[19] = -cf; J[22] = cf; J[23] = -cf;
+          break;
+        }
+        case K_CCVS: { /* (p, n, cp, cn, i, i_sense) */
+          const double r = g->params[d];
+          I[0] = u[4]; I[1] = -u[4]; I[2] = u[5]; I[3] = -u[5];
+          I[4] = (u[0] - u[1]) - r * u[5]; I[5] = u[2] - u[3];
+          J[4] = cf; J[10] = -cf; J[17] = cf; J[23] = -cf;
+          J[24] = cf; J[25] = -cf; J[29] = -cf * r; J[32] = cf; J[33] = -cf;
+          break;
+        }
+        case K_XFMR: { /* (p1, n1, p2, n2, i1, i2); rows l1, l2, m */
+          const int nn = g->n;
+          const double l1 = g->params[d], l2 = g->params[nn + d], mm = g->params[2 * nn + d];
+          I[0] = u[4]; I[1] = -u[4]; I[2] = u[5]; I[3] = -u[5];
+          I[4] = -(u[0] - u[1]); I[5] = -(u[2] - u[3]);
+          Q[4] = l1 * u[4] + mm * u[5]; Q[5] = mm * u[4] + l2 * u[5];
+          J[4] = cf; J[10] = -cf; J[17] = cf; J[23] = -cf;
+          J[24] = -cf; J[25] = cf; J[32] = -cf; J[33] = cf;
+          J[28] = cq * l1; J[29] = cq * mm; J[34] = cq * mm; J[35] = cq * l2;
           break;
         }
         case K_VCCS: {

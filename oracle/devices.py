@@ -13,6 +13,8 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * Inductor            voltax/elements/passive.py:62-87
 * VCCS                voltax/elements/controlled.py:46-60
 * BJT                 voltax/elements/semiconductor.py:73-135
+* VCVS, CCCS, CCVS    voltax/elements/controlled.py:27-98
+* Transformer         voltax/elements/passive.py:90-129
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
                       ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
 * Constant/Step/Pulse voltax/signals.py:58-114
@@ -93,7 +95,7 @@ class GroupModel:
         self.T = len(el.terminals)
         self.K = el.n_internal
         self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET", "Diode",
-                                         "Inductor", "BJT")
+                                         "Inductor", "BJT", "Transformer")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -136,6 +138,24 @@ class GroupModel:
             i = x[..., 0]
             rs = _inst(el.rs, b)
             return torch.stack([i, -i], -1), (rs * i - (v[..., 0] - v[..., 1]))[..., None]
+        if name == "VCVS":  # controlled.py:27-43
+            i = x[..., 0]
+            z = torch.zeros_like(i)
+            f = (v[..., 0] - v[..., 1]) - _inst(el.gain, b) * (v[..., 2] - v[..., 3])
+            return torch.stack([i, -i, z, z], -1), f[..., None]
+        if name == "CCCS":  # controlled.py:63-79
+            i_s = x[..., 0]
+            i = _inst(el.gain, b) * i_s
+            return torch.stack([i, -i, i_s, -i_s], -1), (v[..., 2] - v[..., 3])[..., None]
+        if name == "CCVS":  # controlled.py:82-98
+            i, i_s = x[..., 0], x[..., 1]
+            f = torch.stack([(v[..., 0] - v[..., 1]) - _inst(el.r, b) * i_s,
+                             v[..., 2] - v[..., 3]], -1)
+            return torch.stack([i, -i, i_s, -i_s], -1), f
+        if name == "Transformer":  # passive.py:120-123
+            i1, i2 = x[..., 0], x[..., 1]
+            f = -torch.stack([v[..., 0] - v[..., 1], v[..., 2] - v[..., 3]], -1)
+            return torch.stack([i1, -i1, i2, -i2], -1), f
         if name == "VCCS":  # controlled.py:46-60
             i = _inst(el.gm, b) * (v[..., 2] - v[..., 3])
             z = torch.zeros_like(i)
@@ -189,6 +209,11 @@ class GroupModel:
             return torch.stack([q, -q], -1), None
         if name == "Inductor":
             return None, (torch.exp(_inst(el.log_l, b)) * x[..., 0])[..., None]
+        if name == "Transformer":  # passive.py:125-129
+            i1, i2 = x[..., 0], x[..., 1]
+            l1, l2 = torch.exp(_inst(el.log_l1, b)), torch.exp(_inst(el.log_l2, b))
+            m = _inst(el.k, b) * torch.sqrt(l1 * l2)
+            return None, torch.stack([l1 * i1 + m * i2, m * i1 + l2 * i2], -1)
         if name == "Level1MOSFET":  # overlap charges only (mosfet.py:255-257)
             s = self._sign()
             vd, vg, vs, vb = (s * v[..., k] for k in range(4))

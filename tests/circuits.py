@@ -41,3 +41,27 @@ def bjt_amplifier():
     b.resistor("mir", "0", 20e3, name="Rref")
     b.capacitor("out", "0", 0.2e-12, name="CL")
     return b.build()
+
+
+def controlled_sources_circuit():
+    """A chain through every linear controlled source and a transformer:
+    RC input -> VCVS (x2) -> CCCS sensing through a zero-volt ammeter ->
+    CCVS sensing another branch -> series R into a transformer primary,
+    resistive secondary load."""
+    from voltax_gb300.signals import Pulse
+    b = CircuitBuilder()
+    b.vsource("in", "0", Pulse(0.0, 1.0, delay=1e-9, rise=1e-9, fall=1e-9, width=5e-9,
+                               period=20e-9), ac=1.0, name="Vin")
+    b.resistor("in", "a", 1e3, name="R1")
+    b.capacitor("a", "0", 1e-12, name="C1")
+    b.vcvs("b", "0", "a", "0", 2.0, name="E1")
+    b.cccs("c", "0", "b", "b2", 0.5, name="F1")
+    b.resistor("b2", "0", 2e3, name="R2")
+    b.resistor("c", "0", 1e3, name="R3")
+    b.ccvs("d", "0", "c", "c2", 500.0, name="H1")
+    b.resistor("c2", "0", 500.0, name="R4")
+    b.resistor("d", "d2", 100.0, name="R7")
+    b.transformer("d2", "0", "e", "0", 1e-6, 4e-6, k=0.9, name="K1")
+    b.resistor("e", "0", 50.0, name="R6")
+    b.capacitor("e", "0", 1e-12, name="C2")
+    return b.build()

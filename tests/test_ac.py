@@ -53,11 +53,14 @@ def test_phase_unwrapped_through_four_poles():
     assert np.all(np.diff(ph) < 1.0)
 
 
-@pytest.mark.parametrize("name", ["mixed", "ota"])
+@pytest.mark.parametrize("name", ["mixed", "ota", "controlled"])
 def test_ac_matches_oracle(name):
     import voltax_gb300 as vx
     from voltax_gb300 import symbolic, workloads
-    if name == "ota":
+    if name == "controlled":  # transformer and controlled sources; Vin carries ac=1
+        from circuits import controlled_sources_circuit
+        c = controlled_sources_circuit()
+    elif name == "ota":
         c = workloads.ota_chain(6)
         c = c.replace("VoltageSource", _with_ac(c.elements["VoltageSource"],
                                                  c.layout.device("Vin")[1]))

@@ -47,10 +47,11 @@ CIRCUITS = {
     "ring_l1": lambda: workloads.ring_oscillator_level1(5, gamma=0.3)[0],
     "ring_l1_smooth": lambda: workloads.ring_oscillator_level1(5, smooth=0.02, gamma=0.3)[0],
 }
-from circuits import bjt_amplifier, mixed_circuit  # noqa: E402
+from circuits import bjt_amplifier, controlled_sources_circuit, mixed_circuit  # noqa: E402
 
 CIRCUITS["mixed"] = mixed_circuit
 CIRCUITS["bjt"] = bjt_amplifier
+CIRCUITS["controlled"] = controlled_sources_circuit
 LINEAR = ("rc_ladder", "grid")
 
 
@@ -254,6 +255,42 @@ def test_bjt_amplifier_transient_matches_oracle(engine):
     v = sol.z.cpu().numpy()[:, : c.n_nodes]
     assert np.max(np.abs(v - zr[:, : c.n_nodes])) < 1e-9 * max(1.0, np.abs(zr).max())
     assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_controlled_sources_transient_matches_oracle(precision):
+    """VCVS, CCCS, CCVS and a transformer (local blocks of 5 and 6 unknowns,
+    generic engine)."""
+    c = controlled_sources_circuit()
+    ts = np.linspace(0.0, 8e-9, 81)
+    sol = vx.transient(c, ts, ic="dc", method="trap", options=vx.Options(precision=precision))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc", method="trap")
+    assert bool(sol.converged.all()) and okr.all()
+    scale = max(1.0, np.abs(zr).max())
+    assert np.max(np.abs(sol.z.cpu().numpy() - zr)) < 1e-9 * scale
+    with pytest.raises(Exception, match="not eligible"):
+        vx.dc(c, options=vx.Options(engine="fused"))
+
+
+def test_controlled_sources_dc_gradient_matches_finite_differences():
+    c = controlled_sources_circuit().set("Vin", v1=0.7)
+    out = c.node("e")
+    for gname, field in (("VCVS", "gain"), ("CCCS", "gain"), ("CCVS", "r")):
+        el = c.elements[gname]
+        e2 = el.with_nodes(el.nodes)
+        setattr(e2, field, getattr(el, field).clone().requires_grad_(True))
+        sol = vx.dc(c.replace(gname, e2))
+        (sol.z[c.node("d")] + sol.z[out]).backward()
+        g = getattr(e2, field).grad.numpy().sum()
+        h = 1e-6 * max(1.0, float(getattr(el, field).abs().max()))
+        vals = []
+        for sgn in (1, -1):
+            e3 = el.with_nodes(el.nodes)
+            setattr(e3, field, getattr(el, field).clone() + sgn * h)
+            s3 = vx.dc(c.replace(gname, e3))
+            vals.append(float(s3.z[c.node("d")] + s3.z[out]))
+        np.testing.assert_allclose(g, (vals[0] - vals[1]) / (2 * h), rtol=1e-6, atol=1e-12)
 
 
 def test_bjt_dc_gradient_matches_finite_differences():

@@ -144,7 +144,7 @@ def test_rc_ladder_dc_sweep_values():
         assert ok and np.isclose(z[c.node("out")], r / (r + 3e3))
 
 
-from circuits import bjt_amplifier, mixed_circuit  # noqa: E402
+from circuits import bjt_amplifier, controlled_sources_circuit, mixed_circuit  # noqa: E402
 
 
 def _cases():
@@ -155,6 +155,7 @@ def _cases():
         "ring_l1": lambda: workloads.ring_oscillator_level1(9, gamma=0.3)[0],
         "mixed": mixed_circuit,
         "bjt": bjt_amplifier,
+        "controlled": controlled_sources_circuit,
     }
 
 
@@ -225,7 +226,7 @@ def test_power_grid_dc_matches_superlu():
 
 @pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap"),
                                          ("ring_l1", "be"), ("mixed", "trap"),
-                                         ("bjt", "trap")])
+                                         ("bjt", "trap"), ("controlled", "be")])
 def test_compiled_baseline_matches_oracle(name, method):
     """oracle/cvx.c (the timed CPU baseline) equals the torch restatement."""
     from oracle import cbase

@@ -20,7 +20,8 @@ from .signals import Constant, Signal
 _PREFIX = {
     el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
     el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
-    el.Inductor: "L", el.Diode: "D", el.VCCS: "G", el.BJT: "Q",
+    el.Inductor: "L", el.Diode: "D", el.VCCS: "G", el.BJT: "Q", el.VCVS: "E", el.CCCS: "F",
+    el.CCVS: "H", el.Transformer: "K",
 }
 
 
@@ -114,6 +115,18 @@ class CircuitBuilder:
 
     def bjt(self, c, b, e, polarity="npn", name=None, group=None, **params) -> str:
         return self.add(el.BJT((c, b, e), polarity, **params), name, group)
+
+    def transformer(self, p1, n1, p2, n2, l1, l2, k=1.0, name=None, group=None) -> str:
+        return self.add(el.Transformer((p1, n1, p2, n2), l1, l2, k), name, group)
+
+    def vcvs(self, p, n, cp, cn, gain, name=None, group=None) -> str:
+        return self.add(el.VCVS((p, n, cp, cn), gain), name, group)
+
+    def cccs(self, p, n, sp, sn, gain, name=None, group=None) -> str:
+        return self.add(el.CCCS((p, n, sp, sn), gain), name, group)
+
+    def ccvs(self, p, n, sp, sn, r, name=None, group=None) -> str:
+        return self.add(el.CCVS((p, n, sp, sn), r), name, group)
 
     def vccs(self, p, n, cp, cn, gm, name=None, group=None) -> str:
         return self.add(el.VCCS((p, n, cp, cn), gm), name, group)

@@ -254,7 +254,7 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
       d->n_seg <= 0 || d->n_levels < 0)
     return VXG_ERR_INVALID;
   for (int i = 0; i < d->n_groups; ++i)
-    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_BJT ||
+    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_XFMR ||
         d->groups[i].n_params < 0 || d->groups[i].n_params > VXG_MAX_PARAM_ROWS ||
         d->groups[i].T < 0 || d->groups[i].K < 0 || d->groups[i].T + d->groups[i].K > kMaxM)
       return VXG_ERR_INVALID;
@@ -267,6 +267,9 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
   t.nv = d->n_nodes;
   t.nnz = d->nnz;
   t.n_groups = d->n_groups;
+  t.max_m = 0;
+  for (int i = 0; i < d->n_groups; ++i)
+    t.max_m = std::max(t.max_m, d->groups[i].T + d->groups[i].K);
   t.n_res_slots = d->n_res_slots;
   t.n_jac_slots = d->n_jac_slots;
   t.n_seg = d->n_seg;

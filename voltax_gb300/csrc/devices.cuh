@@ -521,6 +521,85 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
       }
       break;
     }
+    case VXG_KIND_VCVS:   // voltax/elements/controlled.py:27-43, u = (p, n, cp, cn, i)
+    case VXG_KIND_CCCS:   // controlled.py:63-79, u = (p, n, cp, cn, i_sense)
+    case VXG_KIND_CCVS:   // controlled.py:82-98, u = (p, n, cp, cn, i, i_sense)
+    case VXG_KIND_XFMR: {  // passive.py:90-129, u = (p1, n1, p2, n2, i1, i2)
+      const int m = g.m;
+      double I[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0};
+      double J[36];  // cf dI/du + cq dQ/du, linear devices
+#pragma unroll
+      for (int e = 0; e < 36; ++e) J[e] = 0.0;
+      const double p0 = prm(g, 0, b, d);
+      if (g.kind == VXG_KIND_VCVS) {
+        I[0] = u[4];
+        I[1] = -u[4];
+        I[4] = (u[0] - u[1]) - p0 * (u[2] - u[3]);
+        J[0 * 5 + 4] = cf;
+        J[1 * 5 + 4] = -cf;
+        J[4 * 5 + 0] = cf;
+        J[4 * 5 + 1] = -cf;
+        J[4 * 5 + 2] = -cf * p0;
+        J[4 * 5 + 3] = cf * p0;
+      } else if (g.kind == VXG_KIND_CCCS) {
+        I[0] = p0 * u[4];
+        I[1] = -p0 * u[4];
+        I[2] = u[4];
+        I[3] = -u[4];
+        I[4] = u[2] - u[3];
+        J[0 * 5 + 4] = cf * p0;
+        J[1 * 5 + 4] = -cf * p0;
+        J[2 * 5 + 4] = cf;
+        J[3 * 5 + 4] = -cf;
+        J[4 * 5 + 2] = cf;
+        J[4 * 5 + 3] = -cf;
+      } else if (g.kind == VXG_KIND_CCVS) {
+        I[0] = u[4];
+        I[1] = -u[4];
+        I[2] = u[5];
+        I[3] = -u[5];
+        I[4] = (u[0] - u[1]) - p0 * u[5];
+        I[5] = u[2] - u[3];
+        J[0 * 6 + 4] = cf;
+        J[1 * 6 + 4] = -cf;
+        J[2 * 6 + 5] = cf;
+        J[3 * 6 + 5] = -cf;
+        J[4 * 6 + 0] = cf;
+        J[4 * 6 + 1] = -cf;
+        J[4 * 6 + 5] = -cf * p0;
+        J[5 * 6 + 2] = cf;
+        J[5 * 6 + 3] = -cf;
+      } else {  // transformer: rows [l1, l2, m]
+        const double l2 = prm(g, 1, b, d), mm = prm(g, 2, b, d);
+        I[0] = u[4];
+        I[1] = -u[4];
+        I[2] = u[5];
+        I[3] = -u[5];
+        I[4] = -(u[0] - u[1]);
+        I[5] = -(u[2] - u[3]);
+        Q[4] = p0 * u[4] + mm * u[5];
+        Q[5] = mm * u[4] + l2 * u[5];
+        J[0 * 6 + 4] = cf;
+        J[1 * 6 + 4] = -cf;
+        J[2 * 6 + 5] = cf;
+        J[3 * 6 + 5] = -cf;
+        J[4 * 6 + 0] = -cf;
+        J[4 * 6 + 1] = cf;
+        J[5 * 6 + 2] = -cf;
+        J[5 * 6 + 3] = cf;
+        J[4 * 6 + 4] = cq * p0;
+        J[4 * 6 + 5] = cq * mm;
+        J[5 * 6 + 4] = cq * mm;
+        J[5 * 6 + 5] = cq * l2;
+      }
+      for (int i = 0; i < m; ++i) {
+        if (wf) fo[i * n + d] = I[i];
+        if (wq) qo[i * n + d] = Q[i];
+      }
+      if (wj)
+        for (int e = 0; e < m * m; ++e) jo[e * n + d] = (JT)J[e];
+      break;
+    }
     case VXG_KIND_VCCS: {  // voltax/elements/controlled.py:46-60
       const double gm = prm(g, 0, b, d);
       const double i = gm * (u[2] - u[3]);

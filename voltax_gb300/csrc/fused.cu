@@ -10,7 +10,8 @@ namespace vxg {
 // tables (the largest, read once per level) stay in global memory.
 static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
                           int* first_global = nullptr, int* staged_out = nullptr) {
-  if (t.kmax > kCtaK || t.n_seg != 1 || !t.d_blob) return VXG_ERR_TOO_LARGE;
+  if (t.kmax > kCtaK || t.n_seg != 1 || !t.d_blob || t.max_m > kFusedMaxM)
+    return VXG_ERR_TOO_LARGE;
   const int max_scr = (int)std::max(t.max_schur, t.max_bord);
   int dev = 0, max_optin = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));

@@ -564,9 +564,9 @@ struct Instance {
       const GroupDev& g = gt.g[gi];
       const int d = flat - (int)g.dev_base;
       const u16* nd = nodes + A.bo.node_off[gi] + d * g.T;
-      double u[kMaxM];
+      double u[kFusedMaxM];
 #pragma unroll
-      for (int i = 0; i < kMaxM; ++i) {
+      for (int i = 0; i < kFusedMaxM; ++i) {
         if (i < g.T) {
           const u16 node = nd[i];
           u[i] = node != 0xFFFF ? zz[node] : 0.0;

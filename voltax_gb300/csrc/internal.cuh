@@ -8,7 +8,8 @@
 
 namespace vxg {
 
-constexpr int kMaxM = 4;  // largest local block (EKV: 4 terminals)
+constexpr int kMaxM = 6;       // largest local block (transformer, CCVS: 4 + 2)
+constexpr int kFusedMaxM = 4;  // largest local block the fused kernel evaluates
 
 // One group as the kernels see it (passed by value in a GroupTable).
 struct GroupDev {
@@ -77,6 +78,7 @@ struct Topo {
   long long *bt_ptr, *bt_src;
   long long max_schur, max_bord;  // largest per-level scratch
   int kmax, rmax;
+  int max_m;  // largest local block (terminals + internals) over the groups
   // pinned host word for loop control
   int* h_flag;
   int* d_flag;

@@ -320,6 +320,20 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
       }
       break;
     }
+    case VXG_KIND_VCVS:
+      out[4] = cf * (mk(u[0] - u[1]) - p[0] * mk(u[2] - u[3]));
+      break;
+    case VXG_KIND_CCCS:
+      out[0] = cf * (p[0] * mk(u[4]));
+      out[1] = cf * (-(p[0] * mk(u[4])));
+      break;
+    case VXG_KIND_CCVS:
+      out[4] = cf * (mk(u[0] - u[1]) - p[0] * mk(u[5]));
+      break;
+    case VXG_KIND_XFMR:
+      out[4] = cq * (p[0] * mk(u[4]) + p[2] * mk(u[5]));
+      out[5] = cq * (p[2] * mk(u[4]) + p[1] * mk(u[5]));
+      break;
     case VXG_KIND_VCCS: {
       const Dual i = p[0] * mk(u[2] - u[3]);
       out[0] = cf * i;

@@ -41,6 +41,10 @@ KIND_DIODE = 6
 KIND_INDUCTOR = 7
 KIND_VCCS = 8
 KIND_BJT = 9
+KIND_VCVS = 10
+KIND_CCCS = 11
+KIND_CCVS = 12
+KIND_XFMR = 13
 
 
 def _t(x) -> torch.Tensor:
@@ -634,5 +638,82 @@ class BJT(Element):
                 self.cje.expand(shape), self.cjc.expand(shape)]
 
 
+class _Linear4(Element):
+    """Four-terminal linear controlled source: ``(p, n)`` output port,
+    ``(cp, cn)`` control / sense port (controlled.py:1-98)."""
+
+    terminals = ("p", "n", "cp", "cn")
+
+    def gpu_params(self):
+        return [getattr(self, self.fields[0])]
+
+
+class VCVS(_Linear4):
+    """Voltage-controlled voltage source (E): ``v_out = gain v_ctrl``; internal
+    unknown: the output current (controlled.py:27-43). Kernel row: gain."""
+
+    n_internal = 1
+    internal_names = ("i",)
+    fields = ("gain",)
+    kind = KIND_VCVS
+
+    def __init__(self, nodes, gain):
+        self.nodes = self._devices(nodes)
+        self.gain = self._per_device(gain)
+
+
+class CCCS(_Linear4):
+    """Current-controlled current source (F): ``i_out = gain i_sense``, the
+    sense current through a zero-volt ammeter ``cp -> cn``
+    (controlled.py:63-79). Kernel row: gain."""
+
+    n_internal = 1
+    internal_names = ("i_sense",)
+    fields = ("gain",)
+    kind = KIND_CCCS
+
+    def __init__(self, nodes, gain):
+        self.nodes = self._devices(nodes)
+        self.gain = self._per_device(gain)
+
+
+class CCVS(_Linear4):
+    """Current-controlled voltage source (H): ``v_out = r i_sense``
+    (controlled.py:82-98). Kernel row: r."""
+
+    n_internal = 2
+    internal_names = ("i", "i_sense")
+    fields = ("r",)
+    kind = KIND_CCVS
+
+    def __init__(self, nodes, r):
+        self.nodes = self._devices(nodes)
+        self.r = self._per_device(r)
+
+
+class Transformer(Element):
+    """Two coupled inductors, mutual inductance ``k sqrt(l1 l2)``; terminals
+    ``(p1, n1, p2, n2)``, internal unknowns the winding currents
+    (passive.py:90-129). Kernel rows: l1, l2, k sqrt(l1 l2)."""
+
+    terminals = ("p1", "n1", "p2", "n2")
+    n_internal = 2
+    internal_names = ("i1", "i2")
+    fields = ("log_l1", "log_l2", "k")
+    kind = KIND_XFMR
+    has_charges = True
+
+    def __init__(self, nodes, l1, l2, k=1.0):
+        self.nodes = self._devices(nodes)
+        self.log_l1 = self._log_per_device(l1)
+        self.log_l2 = self._log_per_device(l2)
+        self.k = self._per_device(k)
+
+    def gpu_params(self):
+        l1, l2 = torch.exp(self.log_l1), torch.exp(self.log_l2)
+        return [l1, l2, self.k * torch.sqrt(l1 * l2)]
+
+
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
-                 EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS, BJT)
+                 EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS, BJT, VCVS, CCCS, CCVS,
+                 Transformer)
