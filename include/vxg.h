@@ -67,8 +67,13 @@ enum {
   VXG_KIND_VCVS = 10,       /* VCVS         [gain], (p, n, cp, cn) + current i      */
   VXG_KIND_CCCS = 11,       /* CCCS         [gain], (p, n, cp, cn) + sense current  */
   VXG_KIND_CCVS = 12,       /* CCVS         [r], (p, n, cp, cn) + i, sense current  */
-  VXG_KIND_XFMR = 13        /* Transformer  [l1, l2, k sqrt(l1 l2)], (p1, n1, p2, n2)
+  VXG_KIND_XFMR = 13,       /* Transformer  [l1, l2, k sqrt(l1 l2)], (p1, n1, p2, n2)
                                              + winding currents i1, i2          */
+  VXG_KIND_IDEAL_OPAMP = 14,/* IdealOpAmp   [unused], (inp, inn, out) + output current */
+  VXG_KIND_OPAMP = 15,      /* OpAmp        [a0, 1/rout, tau, mid, half, 1/half],
+                                             (inp, inn, out) + state x          */
+  VXG_KIND_SWITCH = 16      /* Switch       [log roff, log(roff/ron), vth, 1/vwidth],
+                                             (p, n, cp, cn)                     */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 

@@ -64,7 +64,8 @@ def lib():
 
 KINDS = {"Resistor": 0, "Conductance": 0, "Capacitor": 1, "VoltageSource": 2,
          "CurrentSource": 3, "EKVMOSFET": 4, "Level1MOSFET": 5, "Diode": 6, "Inductor": 7,
-         "VCCS": 8, "BJT": 9, "VCVS": 10, "CCCS": 11, "CCVS": 12, "Transformer": 13}
+         "VCCS": 8, "BJT": 9, "VCVS": 10, "CCCS": 11, "CCVS": 12, "Transformer": 13,
+         "IdealOpAmp": 14, "OpAmp": 15, "Switch": 16}
 WAVES = {"Constant": 0, "Step": 1, "Pulse": 2}
 
 
@@ -110,6 +111,19 @@ def _rows_of(el, b):
         return [torch.exp(inst(el.log_l)).expand(n), inst(el.rs).expand(n)]
     if name == "VCCS":
         return [inst(el.gm).expand(n)]
+    if name == "IdealOpAmp":
+        return [torch.zeros(n, dtype=torch.float64)]
+    if name == "OpAmp":
+        import math
+        full = lambda x: inst(x).expand(n)  # noqa: E731
+        a0 = torch.exp(full(el.log_a0))
+        half = 0.5 * (full(el.vmax) - full(el.vmin))
+        return [a0, torch.exp(-full(el.log_rout)), a0 / (2 * math.pi * torch.exp(full(el.log_gbw))),
+                0.5 * (full(el.vmax) + full(el.vmin)), half, 1.0 / half]
+    if name == "Switch":
+        full = lambda x: inst(x).expand(n)  # noqa: E731
+        return [full(el.log_roff), full(el.log_roff) - full(el.log_ron), full(el.vth),
+                1.0 / full(el.vwidth)]
     if name in ("VCVS", "CCCS"):
         return [inst(el.gain).expand(n)]
     if name == "CCVS":

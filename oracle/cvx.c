@@ -22,7 +22,7 @@
 
 enum { K_COND = 0, K_CAP = 1, K_VSRC = 2, K_ISRC = 3, K_EKV = 4, K_L1 = 5,
        K_DIODE = 6, K_IND = 7, K_VCCS = 8, K_BJT = 9, K_VCVS = 10, K_CCCS = 11,
-       K_CCVS = 12, K_XFMR = 13 };
+       K_CCVS = 12, K_XFMR = 13, K_IOPAMP = 14, K_OPAMP = 15, K_SWITCH = 16 };
 enum { W_CONST = 0, W_STEP = 1, W_PULSE = 2 };
 enum { M_DC = 0, M_BE = 1, M_TRAP = 2 };
 
@@ -383,6 +383,34 @@ static void stamp(const cvx_sys* s, const double* z, double t, double cf, double
           J[4] = cf; J[10] = -cf; J[17] = cf; J[23] = -cf;
           J[24] = -cf; J[25] = cf; J[32] = -cf; J[33] = cf;
           J[28] = cq * l1; J[29] = cq * mm; J[34] = cq * mm; J[35] = cq * l2;
+          break;
+        }
+        case K_IOPAMP: /* (inp, inn, out, i_out) */
+          I[2] = -u[3]; I[3] = u[0] - u[1];
+          J[11] = -cf; J[12] = cf; J[13] = -cf;
+          break;
+        case K_OPAMP: { /* rows a0, 1/rout, tau, mid, half, 1/half; (inp, inn, out, x) */
+          const double* p = g->params;
+          const int nn = g->n;
+          const double a0 = p[d], gr = p[nn + d], tau = p[2 * nn + d], mid = p[3 * nn + d];
+          const double half = p[4 * nn + d];
+          const double th = tanh((a0 * (u[0] - u[1]) - mid) / half);
+          I[2] = (u[2] - u[3]) * gr; I[3] = u[3] - (mid + half * th);
+          Q[3] = tau * u[3];
+          const double ds = a0 * (1.0 - th * th);
+          J[10] = cf * gr; J[11] = -cf * gr; J[12] = -cf * ds; J[13] = cf * ds; J[15] = cf + cq * tau;
+          break;
+        }
+        case K_SWITCH: { /* rows log roff, log(roff/ron), vth, 1/vwidth; (p, n, cp, cn) */
+          const double* p = g->params;
+          const int nn = g->n;
+          const double lroff = p[d], lrat = p[nn + d], vth = p[2 * nn + d], iw = p[3 * nn + d];
+          double sp, on;
+          softplus2((u[2] - u[3] - vth) * iw, &sp, &on);
+          const double gg = exp(-lroff + on * lrat), vpn = u[0] - u[1];
+          I[0] = gg * vpn; I[1] = -I[0];
+          const double a = cf * gg, c = cf * gg * lrat * on * (1.0 - on) * iw * vpn;
+          J[0] = a; J[1] = -a; J[2] = c; J[3] = -c; J[4] = -a; J[5] = a; J[6] = -c; J[7] = c;
           break;
         }
         case K_VCCS: {

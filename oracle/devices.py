@@ -15,6 +15,8 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * BJT                 voltax/elements/semiconductor.py:73-135
 * VCVS, CCCS, CCVS    voltax/elements/controlled.py:27-98
 * Transformer         voltax/elements/passive.py:90-129
+* IdealOpAmp, OpAmp   voltax/elements/opamp.py:13-103
+* Switch              voltax/elements/switch.py:14-50
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
                       ``logaddexp(x, 0)`` as in ``jax.nn.softplus``)
 * Constant/Step/Pulse voltax/signals.py:58-114
@@ -25,6 +27,8 @@ unknown, as voltax/sparse.py:200-249 does with ``jax.jvp``.
 """
 
 from __future__ import annotations
+
+import math
 
 import numpy as np
 import torch
@@ -95,7 +99,7 @@ class GroupModel:
         self.T = len(el.terminals)
         self.K = el.n_internal
         self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET", "Diode",
-                                         "Inductor", "BJT", "Transformer")
+                                         "Inductor", "BJT", "Transformer", "OpAmp")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -138,6 +142,28 @@ class GroupModel:
             i = x[..., 0]
             rs = _inst(el.rs, b)
             return torch.stack([i, -i], -1), (rs * i - (v[..., 0] - v[..., 1]))[..., None]
+        if name == "IdealOpAmp":  # opamp.py:28-32
+            i = x[..., 0]
+            z = torch.zeros_like(i)
+            return torch.stack([z, z, -i], -1), (v[..., 0] - v[..., 1])[..., None]
+        if name == "OpAmp":  # opamp.py:93-100
+            st = x[..., 0]
+            rout = torch.exp(_inst(el.log_rout, b))
+            a0 = torch.exp(_inst(el.log_a0, b))
+            vmin, vmax = _inst(el.vmin, b), _inst(el.vmax, b)
+            mid, half = 0.5 * (vmax + vmin), 0.5 * (vmax - vmin)
+            u_ = a0 * (v[..., 0] - v[..., 1])
+            clip = mid + half * torch.tanh((u_ - mid) / half)
+            i_out = (v[..., 2] - st) / rout
+            z = torch.zeros_like(i_out)
+            return torch.stack([z, z, i_out], -1), (st - clip)[..., None]
+        if name == "Switch":  # switch.py:39-50
+            on = torch.sigmoid((v[..., 2] - v[..., 3] - _inst(el.vth, b)) / _inst(el.vwidth, b))
+            lroff, lron = _inst(el.log_roff, b), _inst(el.log_ron, b)
+            g = torch.exp(-lroff + on * (lroff - lron))
+            i = g * (v[..., 0] - v[..., 1])
+            z = torch.zeros_like(i)
+            return torch.stack([i, -i, z, z], -1), None
         if name == "VCVS":  # controlled.py:27-43
             i = x[..., 0]
             z = torch.zeros_like(i)
@@ -209,6 +235,9 @@ class GroupModel:
             return torch.stack([q, -q], -1), None
         if name == "Inductor":
             return None, (torch.exp(_inst(el.log_l, b)) * x[..., 0])[..., None]
+        if name == "OpAmp":  # opamp.py:102-103: tau x on the state row
+            tau = torch.exp(_inst(el.log_a0, b)) / (2 * math.pi * torch.exp(_inst(el.log_gbw, b)))
+            return None, (tau * x[..., 0])[..., None]
         if name == "Transformer":  # passive.py:125-129
             i1, i2 = x[..., 0], x[..., 1]
             l1, l2 = torch.exp(_inst(el.log_l1, b)), torch.exp(_inst(el.log_l2, b))

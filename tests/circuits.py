@@ -65,3 +65,23 @@ def controlled_sources_circuit():
     b.resistor("e", "0", 50.0, name="R6")
     b.capacitor("e", "0", 1e-12, name="C2")
     return b.build()
+
+
+def opamp_switch_circuit():
+    """An ideal-op-amp inverting amplifier feeding a single-pole op-amp
+    integrator-follower, and a smoothed switch that a pulse opens and closes
+    between the output and an RC load."""
+    from voltax_gb300.signals import Pulse
+    b = CircuitBuilder()
+    b.vsource("in", "0", Pulse(-0.2, 0.3, delay=0.2e-6, rise=0.1e-6, fall=0.1e-6,
+                               width=1e-6, period=3e-6), name="Vin")
+    b.resistor("in", "m", 1e3, name="R1")
+    b.resistor("m", "a", 4e3, name="R2")
+    b.ideal_opamp("0", "m", "a", name="U1")
+    b.opamp("a", "o", "o", name="U2", a0=1e4, gbw=5e6, rout=10.0, vmin=-1.5, vmax=1.5)
+    b.vsource("ctl", "0", Pulse(0.0, 1.0, delay=0.5e-6, rise=50e-9, fall=50e-9, width=0.8e-6,
+                                period=3e-6), name="Vctl")
+    b.switch("o", "s", "ctl", "0", name="S1", ron=10.0, roff=1e7, vth=0.5, vwidth=0.05)
+    b.resistor("s", "0", 1e3, name="R3")
+    b.capacitor("s", "0", 1e-10, name="C1")
+    return b.build()

@@ -47,11 +47,13 @@ CIRCUITS = {
     "ring_l1": lambda: workloads.ring_oscillator_level1(5, gamma=0.3)[0],
     "ring_l1_smooth": lambda: workloads.ring_oscillator_level1(5, smooth=0.02, gamma=0.3)[0],
 }
-from circuits import bjt_amplifier, controlled_sources_circuit, mixed_circuit  # noqa: E402
+from circuits import (bjt_amplifier, controlled_sources_circuit, mixed_circuit,  # noqa: E402
+                      opamp_switch_circuit)
 
 CIRCUITS["mixed"] = mixed_circuit
 CIRCUITS["bjt"] = bjt_amplifier
 CIRCUITS["controlled"] = controlled_sources_circuit
+CIRCUITS["opamp_switch"] = opamp_switch_circuit
 LINEAR = ("rc_ladder", "grid")
 
 
@@ -271,6 +273,22 @@ def test_controlled_sources_transient_matches_oracle(precision):
     assert np.max(np.abs(sol.z.cpu().numpy() - zr)) < 1e-9 * scale
     with pytest.raises(Exception, match="not eligible"):
         vx.dc(c, options=vx.Options(engine="fused"))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_opamp_switch_transient_matches_oracle(engine):
+    """Ideal and single-pole op-amps and a smoothed switch."""
+    c = opamp_switch_circuit()
+    ts = np.linspace(0.0, 2e-6, 101)
+    sol = vx.transient(c, ts, ic="dc", method="be", options=vx.Options(engine=engine))
+    st = symbolic.structure(c)
+    zr, okr, itr = oa.transient(oa.System(c, st, st.plan), ts, ic="dc", method="be")
+    assert bool(sol.converged.all()) and okr.all()
+    v = sol.z.cpu().numpy()[:, : c.n_nodes]
+    assert np.max(np.abs(v - zr[:, : c.n_nodes])) < 1e-9 * max(1.0, np.abs(zr).max())
+    assert np.array_equal(sol.iterations.cpu().numpy()[1:], itr[1:])
+    # the inverting stage: a = -4 in at DC (ideal op-amp, 1k / 4k)
+    assert abs(float(sol.z[0, c.node("a")]) - (-4 * -0.2)) < 1e-9
 
 
 def test_controlled_sources_dc_gradient_matches_finite_differences():

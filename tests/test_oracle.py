@@ -144,7 +144,8 @@ def test_rc_ladder_dc_sweep_values():
         assert ok and np.isclose(z[c.node("out")], r / (r + 3e3))
 
 
-from circuits import bjt_amplifier, controlled_sources_circuit, mixed_circuit  # noqa: E402
+from circuits import (bjt_amplifier, controlled_sources_circuit, mixed_circuit,  # noqa: E402
+                      opamp_switch_circuit)
 
 
 def _cases():
@@ -156,6 +157,7 @@ def _cases():
         "mixed": mixed_circuit,
         "bjt": bjt_amplifier,
         "controlled": controlled_sources_circuit,
+        "opamp_switch": opamp_switch_circuit,
     }
 
 
@@ -226,7 +228,8 @@ def test_power_grid_dc_matches_superlu():
 
 @pytest.mark.parametrize("name,method", [("grid", "be"), ("adder", "be"), ("ring", "trap"),
                                          ("ring_l1", "be"), ("mixed", "trap"),
-                                         ("bjt", "trap"), ("controlled", "be")])
+                                         ("bjt", "trap"), ("controlled", "be"),
+                                         ("opamp_switch", "be")])
 def test_compiled_baseline_matches_oracle(name, method):
     """oracle/cvx.c (the timed CPU baseline) equals the torch restatement."""
     from oracle import cbase

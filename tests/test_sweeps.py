@@ -118,3 +118,24 @@ def test_dc_sweep_follows_branches_and_shows_hysteresis():
     for k in (5, mid, 40):
         s = vx.dc(c.set("Vin", value=float(vin[k])), guess=up.z[k])
         assert float((s.z - up.z[k]).abs().max()) < 1e-9
+
+
+@pytest.mark.gpu
+def test_dc_sweep_schmitt_trigger_hysteresis():
+    """voltax tests/test_analysis.py:252-273, verbatim circuit: inverting
+    Schmitt trigger with thresholds at +-vmax R2/(R1+R2) = +-0.5 V."""
+    b = CircuitBuilder()
+    b.vsource("in", "0", 0.0, name="Vin")
+    b.opamp("p", "in", "out", a0=1e3, vmin=-1.0, vmax=1.0)
+    b.resistor("out", "p", 10e3)
+    b.resistor("p", "0", 10e3)
+    c = b.build()
+    vin = np.linspace(-1, 1, 81)
+    up = vx.dc_sweep(c, vin, "Vin")
+    down = vx.dc_sweep(c, vin[::-1], "Vin", guess=up.z[-1])
+    assert bool(up.converged.all()) and bool(down.converged.all())
+    out_up, out_dn = up.v("out").cpu().numpy(), down.v("out").cpu().numpy()
+    assert out_up[40] > 0.9 and out_dn[40] < -0.9  # two stable states at 0 V
+    rise_thr = _crossing(vin, out_up, 0.0)
+    fall_thr = -_crossing(-vin[::-1], out_dn, 0.0)
+    assert 0.4 < rise_thr < 0.55 and -0.55 < fall_thr < -0.4

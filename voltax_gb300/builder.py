@@ -21,7 +21,7 @@ _PREFIX = {
     el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
     el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
     el.Inductor: "L", el.Diode: "D", el.VCCS: "G", el.BJT: "Q", el.VCVS: "E", el.CCCS: "F",
-    el.CCVS: "H", el.Transformer: "K",
+    el.CCVS: "H", el.Transformer: "K", el.IdealOpAmp: "U", el.OpAmp: "U", el.Switch: "S",
 }
 
 
@@ -127,6 +127,15 @@ class CircuitBuilder:
 
     def ccvs(self, p, n, sp, sn, r, name=None, group=None) -> str:
         return self.add(el.CCVS((p, n, sp, sn), r), name, group)
+
+    def opamp(self, inp, inn, out, name=None, group=None, **params) -> str:
+        return self.add(el.OpAmp((inp, inn, out), **params), name, group)
+
+    def ideal_opamp(self, inp, inn, out, name=None, group=None) -> str:
+        return self.add(el.IdealOpAmp((inp, inn, out)), name, group)
+
+    def switch(self, p, n, cp, cn, name=None, group=None, **params) -> str:
+        return self.add(el.Switch((p, n, cp, cn), **params), name, group)
 
     def vccs(self, p, n, cp, cn, gm, name=None, group=None) -> str:
         return self.add(el.VCCS((p, n, cp, cn), gm), name, group)

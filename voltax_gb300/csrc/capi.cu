@@ -254,7 +254,7 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
       d->n_seg <= 0 || d->n_levels < 0)
     return VXG_ERR_INVALID;
   for (int i = 0; i < d->n_groups; ++i)
-    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_XFMR ||
+    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_SWITCH ||
         d->groups[i].n_params < 0 || d->groups[i].n_params > VXG_MAX_PARAM_ROWS ||
         d->groups[i].T < 0 || d->groups[i].K < 0 || d->groups[i].T + d->groups[i].K > kMaxM)
       return VXG_ERR_INVALID;

@@ -600,6 +600,88 @@ __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const 
         for (int e = 0; e < m * m; ++e) jo[e * n + d] = (JT)J[e];
       break;
     }
+    case VXG_KIND_IDEAL_OPAMP: {  // voltax/elements/opamp.py:13-32, u = (inp, inn, out, i)
+      if (wf) {
+        fo[d] = 0.0;
+        fo[n + d] = 0.0;
+        fo[2 * n + d] = -u[3];
+        fo[3 * n + d] = u[0] - u[1];
+      }
+      if (wq) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) qo[e * n + d] = 0.0;
+      }
+      if (wj) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) jo[e * n + d] = JT(0);
+        jo[(2 * 4 + 3) * n + d] = (JT)(-cf);
+        jo[(3 * 4 + 0) * n + d] = (JT)cf;
+        jo[(3 * 4 + 1) * n + d] = (JT)(-cf);
+      }
+      break;
+    }
+    case VXG_KIND_OPAMP: {  // voltax/elements/opamp.py:35-103, u = (inp, inn, out, x)
+      const double a0 = prm(g, 0, b, d), grout = prm(g, 1, b, d), tau = prm(g, 2, b, d);
+      const double mid = prm(g, 3, b, d), half = prm(g, 4, b, d), ihalf = prm(g, 5, b, d);
+      const double th = tanh((a0 * (u[0] - u[1]) - mid) * ihalf);
+      if (wf) {
+        fo[d] = 0.0;
+        fo[n + d] = 0.0;
+        fo[2 * n + d] = (u[2] - u[3]) * grout;
+        fo[3 * n + d] = u[3] - (mid + half * th);
+      }
+      if (wq) {
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+        qo[2 * n + d] = 0.0;
+        qo[3 * n + d] = tau * u[3];
+      }
+      if (wj) {
+        const double ds = a0 * (1.0 - th * th);  // d clip(a0 vd) / d vd
+#pragma unroll
+        for (int e = 0; e < 16; ++e) jo[e * n + d] = JT(0);
+        jo[(2 * 4 + 2) * n + d] = (JT)(cf * grout);
+        jo[(2 * 4 + 3) * n + d] = (JT)(-cf * grout);
+        jo[(3 * 4 + 0) * n + d] = (JT)(-cf * ds);
+        jo[(3 * 4 + 1) * n + d] = (JT)(cf * ds);
+        jo[(3 * 4 + 3) * n + d] = (JT)(cf + cq * tau);
+      }
+      break;
+    }
+    case VXG_KIND_SWITCH: {  // voltax/elements/switch.py:14-50, u = (p, n, cp, cn)
+      const double lroff = prm(g, 0, b, d), lratio = prm(g, 1, b, d);
+      const double vth = prm(g, 2, b, d), iw = prm(g, 3, b, d);
+      double sp, on;
+      softplus_and_sigmoid((u[2] - u[3] - vth) * iw, &sp, &on);
+      const double gg = exp(-lroff + on * lratio);
+      const double vpn = u[0] - u[1];
+      const double i = gg * vpn;
+      if (wf) {
+        fo[d] = i;
+        fo[n + d] = -i;
+        fo[2 * n + d] = 0.0;
+        fo[3 * n + d] = 0.0;
+      }
+      if (wq) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) qo[e * n + d] = 0.0;
+      }
+      if (wj) {
+        const double dgc = gg * lratio * on * (1.0 - on) * iw * vpn;  // d i / d v_ctrl
+#pragma unroll
+        for (int e = 0; e < 16; ++e) jo[e * n + d] = JT(0);
+        const double a = cf * gg, c = cf * dgc;
+        jo[0 * n + d] = (JT)a;
+        jo[1 * n + d] = (JT)(-a);
+        jo[2 * n + d] = (JT)c;
+        jo[3 * n + d] = (JT)(-c);
+        jo[4 * n + d] = (JT)(-a);
+        jo[5 * n + d] = (JT)a;
+        jo[6 * n + d] = (JT)(-c);
+        jo[7 * n + d] = (JT)c;
+      }
+      break;
+    }
     case VXG_KIND_VCCS: {  // voltax/elements/controlled.py:46-60
       const double gm = prm(g, 0, b, d);
       const double i = gm * (u[2] - u[3]);

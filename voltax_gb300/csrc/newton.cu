@@ -320,6 +320,26 @@ __device__ void dual_outputs(const GroupDev& g, const Dual* p, const double* u, 
       }
       break;
     }
+    case VXG_KIND_OPAMP: {
+      const Dual a0 = p[0], grout = p[1], tau = p[2], mid = p[3], half = p[4];
+      const Dual arg = (a0 * mk(u[0] - u[1]) - mid) / half;
+      const double th = tanh(arg.v);
+      const Dual clip = mid + half * Dual{th, (1.0 - th * th) * arg.d};
+      out[2] = cf * (mk(u[2] - u[3]) * grout);
+      out[3] = cf * (mk(u[3]) - clip) + cq * (tau * mk(u[3]));
+      break;
+    }
+    case VXG_KIND_SWITCH: {
+      const Dual on_arg = (mk(u[2] - u[3]) - p[2]) * p[3];
+      double sp, sg;
+      softplus_and_sigmoid(on_arg.v, &sp, &sg);
+      const Dual on = {sg, sg * (1.0 - sg) * on_arg.d};
+      const Dual gg = dexp(on * p[1] - p[0]);
+      const Dual i = gg * mk(u[0] - u[1]);
+      out[0] = cf * i;
+      out[1] = cf * (-i);
+      break;
+    }
     case VXG_KIND_VCVS:
       out[4] = cf * (mk(u[0] - u[1]) - p[0] * mk(u[2] - u[3]));
       break;

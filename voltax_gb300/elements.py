@@ -21,6 +21,8 @@ from __future__ import annotations
 
 from typing import Any, Sequence
 
+import math
+
 import numpy as np
 import torch
 
@@ -45,6 +47,9 @@ KIND_VCVS = 10
 KIND_CCCS = 11
 KIND_CCVS = 12
 KIND_XFMR = 13
+KIND_IDEAL_OPAMP = 14
+KIND_OPAMP = 15
+KIND_SWITCH = 16
 
 
 def _t(x) -> torch.Tensor:
@@ -714,6 +719,77 @@ class Transformer(Element):
         return [l1, l2, self.k * torch.sqrt(l1 * l2)]
 
 
+class IdealOpAmp(Element):
+    """Ideal op-amp (nullor), terminals ``(inp, inn, out)``: the output
+    sources the current ``i_out`` (from ground into ``out``) that enforces
+    ``v_inp = v_inn`` (opamp.py:13-32). One unused kernel parameter row."""
+
+    terminals = ("inp", "inn", "out")
+    n_internal = 1
+    internal_names = ("i_out",)
+    fields = ()
+    kind = KIND_IDEAL_OPAMP
+
+    def __init__(self, nodes):
+        self.nodes = self._devices(nodes)
+
+    def gpu_params(self):
+        return [torch.zeros(self.size, dtype=torch.float64)]  # no parameters: one unused row
+
+
+class OpAmp(Element):
+    """Single-pole op-amp macromodel with soft output rails (opamp.py:35-103):
+    ``tau dx/dt + x = clip(a0 (v_inp - v_inn))``, ``clip(u) = mid + half
+    tanh((u - mid)/half)``, the output driving ``out`` through ``rout``;
+    ``tau = a0 / (2 pi gbw)``. Kernel rows: a0, 1/rout, tau, mid, half,
+    1/half."""
+
+    terminals = ("inp", "inn", "out")
+    n_internal = 1
+    internal_names = ("x",)
+    fields = ("log_a0", "log_gbw", "log_rout", "vmin", "vmax")
+    kind = KIND_OPAMP
+    has_charges = True
+
+    def __init__(self, nodes, a0=1e5, gbw=1e6, rout=1.0, vmin=-15.0, vmax=15.0):
+        self.nodes = self._devices(nodes)
+        self.log_a0 = self._log_per_device(a0)
+        self.log_gbw = self._log_per_device(gbw)
+        self.log_rout = self._log_per_device(rout)
+        self.vmin = self._per_device(vmin)
+        self.vmax = self._per_device(vmax)
+
+    def gpu_params(self):
+        a0 = torch.exp(self.log_a0)
+        shape = a0.shape
+        half = (0.5 * (self.vmax - self.vmin)).expand(shape)
+        return [a0, torch.exp(-self.log_rout).expand(shape),
+                (a0 / (2 * math.pi * torch.exp(self.log_gbw))).expand(shape),
+                (0.5 * (self.vmax + self.vmin)).expand(shape), half, 1.0 / half]
+
+
+class Switch(Element):
+    """Voltage-controlled switch, smoothed (switch.py:14-50): terminals
+    ``(p, n, cp, cn)``, ``log g = -log roff + sigmoid((v_c - vth)/vwidth)
+    log(roff/ron)``. Kernel rows: log roff, log(roff/ron), vth, 1/vwidth."""
+
+    terminals = ("p", "n", "cp", "cn")
+    fields = ("log_ron", "log_roff", "vth", "vwidth")
+    kind = KIND_SWITCH
+
+    def __init__(self, nodes, ron=1.0, roff=1e9, vth=0.5, vwidth=0.05):
+        self.nodes = self._devices(nodes)
+        self.log_ron = self._log_per_device(ron)
+        self.log_roff = self._log_per_device(roff)
+        self.vth = self._per_device(vth)
+        self.vwidth = self._per_device(vwidth)
+
+    def gpu_params(self):
+        shape = torch.broadcast_shapes(self.log_ron.shape, self.log_roff.shape)
+        return [self.log_roff.expand(shape), (self.log_roff - self.log_ron).expand(shape),
+                self.vth.expand(shape), (1.0 / self.vwidth).expand(shape)]
+
+
 ELEMENT_TYPES = (Resistor, Conductance, Capacitor, VoltageSource, CurrentSource,
                  EKVMOSFET, Level1MOSFET, Inductor, Diode, VCCS, BJT, VCVS, CCCS, CCVS,
-                 Transformer)
+                 Transformer, IdealOpAmp, OpAmp, Switch)
