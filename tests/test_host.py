@@ -1,0 +1,86 @@
+"""Host-side logic that needs no GPU: segment declarations, AC stimulus,
+option validation and the device-model host tables."""
+
+import numpy as np
+import pytest
+import torch
+
+import voltax_gb300 as vx
+from voltax_gb300 import workloads
+from voltax_gb300.builder import CircuitBuilder
+
+
+def test_power_grid_batch_segments():
+    c = workloads.power_grid_batch([4, 6, 5], seed=2)
+    seg = c.unknown_segments()
+    counts = np.bincount(seg)
+    # nodes plus the pad currents of each grid
+    assert counts.tolist() == [16 + len(workloads.grid_pads(4)), 36 + len(workloads.grid_pads(6)),
+                               25 + len(workloads.grid_pads(5))]
+    # each grid's segment is closed: no element joins two segments
+    for name, el in c.elements.items():
+        nodes = el.node_array()
+        for row in nodes:
+            s = {int(seg[v]) for v in row if v >= 0}
+            assert len(s) <= 1, name
+
+
+def test_with_segments_rejects_joined_segments():
+    b = CircuitBuilder()
+    b.vsource("a", "0", 1.0)
+    b.resistor("a", "b", 1e3)
+    b.resistor("b", "0", 1e3)
+    c = b.build()
+    with pytest.raises(ValueError, match="joins two segments"):
+        c.with_segments([0, 1])
+    with pytest.raises(ValueError, match="entries"):
+        c.with_segments([0])
+
+
+def test_ac_stimulus_matches_oracle_restatement():
+    from oracle.analysis import _ac_stimulus
+    b = CircuitBuilder()
+    b.vsource("in", "0", 0.0, ac=1.0, ac_phase=30.0, name="Vin")
+    b.vsource("x", "0", 1.0, name="Vdc")
+    b.resistor("in", "a", 1e3)
+    b.resistor("x", "a", 1e3)
+    b.isource("a", "0", 0.0, ac=2.0, ac_phase=-45.0, name="I1")
+    b.isource("0", "x", 0.0, ac=0.5, name="I2")
+    c = b.build()
+    np.testing.assert_allclose(c.ac_stimulus(), _ac_stimulus(c), rtol=0, atol=0)
+
+
+def test_options_validation():
+    with pytest.raises(ValueError):
+        vx.Options(engine="turbo")
+    with pytest.raises(ValueError):
+        vx.Options(block=64)
+    with pytest.raises(ValueError):
+        vx.Options(precision="f16")
+    assert vx.Options(refine=None).native(refine=1).refine == 1
+
+
+@pytest.mark.parametrize("make", [
+    lambda: vx.Diode((0, 1), is_=1e-14, n=1.5, cj=1e-12, tt=1e-9),
+    lambda: vx.BJT((0, 1, 2), "pnp", vaf=50.0),
+    lambda: vx.OpAmp((0, 1, 2), a0=1e4, gbw=1e7),
+    lambda: vx.Switch((0, 1, 2, 3), ron=2.0, roff=1e8),
+    lambda: vx.Transformer((0, 1, 2, 3), 1e-6, 4e-6, k=0.5),
+    lambda: vx.Level1MOSFET((0, 1, 2, 3), smooth=0.0),
+])
+def test_parameter_rows_are_finite_and_differentiable(make):
+    el = make()
+    rows = el.gpu_params()
+    assert 1 <= len(rows) <= 13
+    for r in rows:
+        r = torch.as_tensor(r)
+        assert r.shape[-1] == el.size and bool(torch.isfinite(r).all())
+    # every per-device field reaches at least one row through autograd
+    for f in el.fields:
+        x = getattr(el, f).detach().clone().requires_grad_(True)
+        e2 = el.with_nodes(el.nodes)
+        setattr(e2, f, x)
+        total = sum(torch.as_tensor(r).sum() for r in e2.gpu_params())
+        if total.requires_grad:
+            total.backward()
+            assert x.grad is not None
