@@ -451,9 +451,8 @@ def main():
     achieved = bytes_per_iter * total_iters / step_s / 1e9
     # DRAM traffic of one fused launch: the packed parameter rows read once per
     # instance, the states written per time point, converged + iterations. An
-    # ncu capture of 512 instances x 21 points read 5.87 MB = the packed rows
-    # (profiles/fused_kernel_adder_mc512_v4.md); its 6.4 MB of states stayed
-    # in L2, at this size they do not.
+    # ncu capture of 512 instances x 21 points read 5.8 MB = the packed rows;
+    # its 6.4 MB of states stayed in L2, at this size they do not.
     traffic = None
     if engine_used == "fused":
         packed = sum(t.numel() * 8 for t in _Call(dev_circuit, opts32).keep)
