@@ -9,7 +9,7 @@ refactorization under a reused symbolic plan, and level-scheduled
 
 from . import library, signals, sparse, workloads  # noqa: F401
 from .analysis import (ACSolution, Options, Solution, ac, dc, dc_sweep,  # noqa: F401
-                       time_grid, transient)
+                       linearize, time_grid, transient)
 from .builder import CircuitBuilder  # noqa: F401
 from .circuit import Circuit, Layout  # noqa: F401
 from .elements import (VT_300K, Capacitor, Conductance, CurrentSource,  # noqa: F401

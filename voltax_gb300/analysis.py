@@ -549,6 +549,17 @@ def time_grid(circuit, t_stop: float, dt_max: float, dt_min: float | None = None
 # =============================================================================
 
 
+def linearize(circuit, z, t: float = 0.0):
+    """Small-signal matrices ``G = df/dz`` and ``C = dq/dz`` at state `z` as
+    dense ``(S, S)`` tensors (voltax/analysis.py:483-491); the stamped sparse
+    values come from `sparse.jacobian`."""
+    from . import sparse
+    st = structure(circuit)
+    G = sparse.jacobian(circuit, z, t, 1.0, 0.0, structure=st)
+    C = sparse.jacobian(circuit, z, t, 0.0, 1.0, structure=st)
+    return sparse.to_dense(st, G), sparse.to_dense(st, C)
+
+
 class ACSolution:
     """Result of `ac` (voltax/analysis.py:142-178): complex phasors
     ``z`` of shape ``(F, S)`` at the frequencies ``freqs`` (Hz)."""

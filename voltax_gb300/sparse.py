@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -142,6 +143,19 @@ def solve(plan, factors: Factors, b, transpose: bool = False, refine: int = 2):
                               refine if factors.precision == L.VXG_F32 else 0,
                               ws.data_ptr(), stream_ptr()), "vxg_solve")
     return x[0] if single and B == 1 else x
+
+
+def to_dense(st: Structure, data) -> torch.Tensor:
+    """Dense ``(..., S, S)`` matrix of CSR values on `st`'s pattern
+    (voltax/sparse.py:135-140)."""
+    data = torch.as_tensor(data)
+    rows = torch.as_tensor(np.repeat(np.arange(st.size), np.diff(st.indptr)),
+                           device=data.device)
+    cols = torch.as_tensor(np.asarray(st.indices), device=data.device)
+    out = torch.zeros((*data.shape[:-1], st.size, st.size), dtype=data.dtype,
+                      device=data.device)
+    out[..., rows, cols] = data
+    return out
 
 
 def matvec(st: Structure, data, x):
