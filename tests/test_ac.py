@@ -84,3 +84,20 @@ def _with_ac(el, idx):
     ac[idx] = 1.0
     e.ac, e.ac_phase = ac, torch.full((el.size,), 30.0, dtype=torch.float64)
     return e
+
+
+def test_linearize_matches_oracle_jacobians():
+    import voltax_gb300 as vx
+    from oracle import stamp as ost
+    from voltax_gb300 import symbolic
+    from circuits import mixed_circuit
+    c = mixed_circuit()
+    st = symbolic.structure(c)
+    z = np.random.default_rng(3).uniform(-0.3, 0.8, c.size)
+    G, C = vx.linearize(c, torch.as_tensor(z), 0.0)
+    rows = np.repeat(np.arange(st.size), np.diff(st.indptr))
+    for M, (cf, cq) in ((G, (1.0, 0.0)), (C, (0.0, 1.0))):
+        ref = np.zeros((st.size, st.size))
+        ref[rows, st.indices] = ost.jacobian(c, st, z, 0.0, cf, cq)
+        np.testing.assert_allclose(M.cpu().numpy(), ref, rtol=1e-12,
+                                   atol=1e-15 * max(1.0, np.abs(ref).max()))
