@@ -112,10 +112,10 @@ typedef struct {
   /* stamping: canonical-order gathers of device contributions */
   int64_t n_res_slots;    /* sum over groups of n*(T+K) */
   const int64_t* res_ptr; /* S+1 */
-  const int64_t* res_src; /* slot ids, ascending within each row */
+  const int64_t* res_src; /* storage slot ids per row, in summation order */
   int64_t n_jac_slots;    /* sum over groups of n*(T+K)^2 */
   const int64_t* jac_ptr; /* nnz+1 */
-  const int64_t* jac_src; /* slot ids, ascending within each entry */
+  const int64_t* jac_src; /* storage slot ids per entry, in summation order */
   /* independent sub-circuits (segments) inside the topology */
   int32_t n_seg;
   const int32_t* seg_ptr;  /* n_seg+1 offsets into seg_idx */

@@ -3,10 +3,14 @@
 `Engine` owns one ``vxg_handle`` (a topology + symbolic plan resident on the
 GPU) and the index tables that define the deterministic stamping order:
 
-* residual slots: group-major, device-major, local unknown order; each row
-  lists its slots in ascending order (voltax/circuit.py:209-226);
-* Jacobian slots: group-major, device-major, row-major local blocks; each
-  CSR entry lists its slots in ascending order (voltax/sparse.py:233-248).
+* residual slots: each row sums its contributions in canonical order --
+  group-major, device-major, local unknown order (voltax/circuit.py:209-226);
+* Jacobian slots: each CSR entry sums its contributions in canonical order --
+  group-major, device-major, row-major local blocks (voltax/sparse.py:233-248).
+
+The gathers hold storage slot ids: within a group the device contributions
+are stored SoA (residual slot (i, d) at i*n + d, Jacobian slot (i, j, d) at
+(i*m + j)*n + d), so the ids of one row are not ascending.
 
 Engines are cached per topology (the analogue of voltax's cached
 `structure` / `plan`, voltax/sparse.py:114-117, 150-161).
