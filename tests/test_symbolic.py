@@ -3,7 +3,8 @@
 Golden fixtures come from the reference's own ``voltax/sparse.py`` run on the
 same topologies (``tests/golden/make_fixtures.py``): CSR pattern and stamp
 positions, pivot groups, supernodes, borders, bucket classes and plan
-statistics. Also checks the GPU panel layout's invariants.
+statistics. Both planners are pinned: the C++ one (the default) and the
+numpy restatement. Also checks the GPU panel layout's invariants.
 """
 
 import hashlib
@@ -40,15 +41,18 @@ SMALL = [n for n, r in INDEX.items() if r["size"] <= 200]
 LARGE = ["grid30", "grid50"]
 
 
-def _check(name, circuit, leaves):
+def _check(name, circuit, leaves, native):
     rec = INDEX[name]
     st = symbolic.structure(circuit)
     assert (st.size, st.n_nodes, st.nnz) == (rec["size"], rec["n_nodes"], rec["nnz"])
     assert digest(st.indptr, st.indices, *[p for _, p, _ in st.stamps]) == rec["structure"]
     assert digest(symbolic.pivot_groups(st)) == rec["pivot_groups"]
+    if native:
+        gid = symbolic.native_fields(st, symbolic.LEAF_SIZE)["gid"]
+        assert digest(gid) == rec["pivot_groups"]
     for leaf in leaves:
         want = rec["plans"][str(leaf)]
-        plan = symbolic.make_plan(st, leaf)
+        plan = symbolic.make_plan(st, leaf, native=native)
         assert [len(c) for c in plan.buckets] == want["buckets"]
         sets = [plan.supernodes[i] for c in plan.buckets for i in c]
         bords = [plan.borders[i] for c in plan.buckets for i in c]
@@ -76,10 +80,11 @@ def _check_layout(st, plan):
             assert np.all(plan.level[owner] > li)
 
 
+@pytest.mark.parametrize("native", [True, False], ids=["cpp", "numpy"])
 @pytest.mark.parametrize("name", SMALL)
-def test_small_topologies_match_reference(name):
+def test_small_topologies_match_reference(name, native):
     circuit, leaves = fixture_circuits([name])[name]
-    _check(name, circuit, leaves)
+    _check(name, circuit, leaves, native)
     arrays = np.load(GOLDEN / f"{name}.npz")
     st = symbolic.structure(circuit)
     assert np.array_equal(st.indptr, arrays["indptr"])
@@ -87,10 +92,11 @@ def test_small_topologies_match_reference(name):
     assert np.array_equal(symbolic.pivot_groups(st), arrays["pivot_groups"])
 
 
+@pytest.mark.parametrize("native", [True, False], ids=["cpp", "numpy"])
 @pytest.mark.parametrize("name", LARGE)
-def test_power_grids_match_reference(name):
+def test_power_grids_match_reference(name, native):
     circuit, leaves = fixture_circuits([name])[name]
-    _check(name, circuit, leaves)
+    _check(name, circuit, leaves, native)
 
 
 def test_voltage_sources_pair_with_their_node():

@@ -1,7 +1,9 @@
-"""Build ``libvxg.so`` (the CUDA kernels + C ABI) in-tree for sm_103a.
+"""Build ``libvxg.so`` (the CUDA kernels + C ABI) in-tree for sm_103a, and
+``libvxg_symbolic.so`` (the host symbolic analysis, plain C++).
 
 Plain nvcc, one translation unit per source compiled in parallel, then one
-link; no torch, no cmake. Output: ``voltax_gb300/_lib/libvxg.so``.
+link; the host planner is one g++ call. No torch, no cmake. Outputs:
+``voltax_gb300/_lib/libvxg.so`` and ``voltax_gb300/_lib/libvxg_symbolic.so``.
 """
 
 from __future__ import annotations
@@ -46,7 +48,28 @@ def _compile(name: str, extra) -> Path:
     return obj
 
 
+def build_symbolic(verbose: bool = False) -> Path:
+    """The host planner library (no CUDA): rebuilt when its sources change."""
+    OUT.mkdir(exist_ok=True)
+    lib = OUT / "libvxg_symbolic.so"
+    src = SRC / "symbolic.cpp"
+    deps = [src, INCLUDE / "vxg_symbolic.h"]
+    if lib.exists() and lib.stat().st_mtime > max(d.stat().st_mtime for d in deps):
+        return lib
+    tmp = OUT / f".libvxg_symbolic.{os.getpid()}.so"
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-shared", "-fPIC",
+           f"-I{INCLUDE}", str(src), "-o", str(tmp)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"g++ failed on symbolic.cpp:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, lib)  # atomic: a concurrent loader never sees a partial file
+    if verbose:
+        print(lib)
+    return lib
+
+
 def build(verbose: bool = False, extra=()) -> Path:
+    build_symbolic(verbose)
     OUT.mkdir(exist_ok=True)
     lib = OUT / "libvxg.so"
     sources = [s for s in SOURCES if (SRC / s).exists()]

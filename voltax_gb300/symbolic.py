@@ -14,6 +14,11 @@ per-bucket batches, every supernode owns an unpadded, contiguous panel
 and each elimination level is one launch whose CTAs take supernodes of
 different sizes. The index maps the kernels need (pattern -> panel,
 deterministic Schur-update and border-update gathers) are built here.
+
+Two planners give identical plans: the C++ one (`csrc/symbolic.cpp`, the
+default; ~50x faster on large grids) and the numpy restatement
+(`make_plan_numpy`), which is pinned to the reference's own output. The
+bipartite matching of the pivot grouping runs in scipy for both.
 """
 
 from __future__ import annotations
@@ -31,6 +36,8 @@ LEAF_SIZE = int(os.environ.get("VOLTAX_SPARSE_LEAF", 16))
 """Largest nested-dissection leaf kept as one dense supernode (sparse.py:63)."""
 SPLIT_SAVING = 1e6
 """Padded flops a level must save to be split in two buckets (sparse.py:64)."""
+NATIVE = os.environ.get("VOLTAX_SYMBOLIC", "native") != "numpy"
+"""Plan with the C++ planner (`libvxg_symbolic.so`) unless VOLTAX_SYMBOLIC=numpy."""
 
 
 # =============================================================================
@@ -140,26 +147,12 @@ def build_structure(S: int, nv: int, offsets: dict, groups, leaf: int = LEAF_SIZ
 # =============================================================================
 
 
-def pivot_groups(st: Structure) -> np.ndarray:
-    """Group id of every unknown (voltax/sparse.py:257-305): unknowns whose
-    diagonal may vanish are glued to a terminal node of their device; two-
-    terminal devices with one internal pick a partner by bipartite matching."""
-    S = st.size
-    parent = np.arange(S)
-
-    def find(a):
-        root = a
-        while parent[root] != root:
-            root = parent[root]
-        while parent[a] != root:  # path compression
-            parent[a], a = root, parent[a]
-        return root
-
-    def union(a, b):
-        ra, rb = find(a), find(b)
-        if ra != rb:
-            parent[rb] = ra
-
+def union_pairs(st: Structure) -> tuple[np.ndarray, np.ndarray]:
+    """The ordered ``union(a, b)`` calls of voltax's pivot grouping
+    (voltax/sparse.py:257-305): unknowns whose diagonal may vanish are glued
+    to a terminal node of their device; two-terminal devices with one
+    internal pick a partner by bipartite matching (matched pairs first, in
+    device order), every other device glues all its unknowns."""
     pair_x, pair_cands, full = [], [], []
     for _, allv, T, local in st.devices:
         k = allv.shape[1] - T
@@ -176,6 +169,8 @@ def pivot_groups(st: Structure) -> np.ndarray:
                 pair_cands.append(terms)
             else:
                 full.append(terms + internals)
+    ua: list[int] = []
+    ub: list[int] = []
     if pair_x:
         r = np.repeat(np.arange(len(pair_x)), [len(c) for c in pair_cands])
         c = np.concatenate(pair_cands)
@@ -183,12 +178,34 @@ def pivot_groups(st: Structure) -> np.ndarray:
         match = csg.maximum_bipartite_matching(g, perm_type="column")
         for i, (x, cands) in enumerate(zip(pair_x, pair_cands)):
             if match[i] >= 0:
-                union(int(match[i]), x)
+                ua.append(int(match[i]))
+                ub.append(x)
             else:
                 full.append(cands + [x])
     for members in full:
-        for v in members[1:]:
-            union(members[0], v)
+        ua += [members[0]] * (len(members) - 1)
+        ub += members[1:]
+    return np.asarray(ua, np.int64), np.asarray(ub, np.int64)
+
+
+def pivot_groups(st: Structure) -> np.ndarray:
+    """Group id of every unknown (voltax/sparse.py:257-305): union-find over
+    `union_pairs`, groups numbered by their root."""
+    S = st.size
+    parent = np.arange(S)
+
+    def find(a):
+        root = a
+        while parent[root] != root:
+            root = parent[root]
+        while parent[a] != root:  # path compression
+            parent[a], a = root, parent[a]
+        return root
+
+    for a, b in zip(*union_pairs(st)):
+        ra, rb = find(int(a)), find(int(b))
+        if ra != rb:
+            parent[rb] = ra
     roots = np.array([find(a) for a in range(S)])
     return np.unique(roots, return_inverse=True)[1]
 
@@ -339,9 +356,36 @@ def _gather_csr(targets: np.ndarray):
     return uniq.astype(np.int64), ptr, order.astype(np.int64)
 
 
-def make_plan(st: Structure, leaf: int | None = None) -> Plan:
+def _stats(k, r, level, classes, G) -> dict:
+    """voltax's ``plan.stats`` (voltax/sparse.py:528-535)."""
+    padded = 0.0
+    ref_work = 0
+    for sel in classes:
+        m, kp, rp = len(sel), int(k[sel].max()), int(r[sel].max())
+        padded += m * (2.0 * kp**3 + 2.0 * kp * kp * rp + 2.0 * kp * rp * rp)
+        ref_work += m * (kp * kp + 2 * kp * rp)
+    flops = float(np.sum(2.0 * k**3 + 2.0 * k * k * r + 2.0 * k * r * r))
+    return dict(supernodes=len(k), levels=int(level.max()) + 1, buckets=len(classes),
+                factor_entries=int(np.sum(k * k + 2 * k * r)), work=ref_work,
+                flops=flops, padded_flops=padded, largest_supernode=int(k.max()),
+                pivot_groups=G)
+
+
+def make_plan(st: Structure, leaf: int | None = None, native: bool | None = None) -> Plan:
     """Symbolic factorization (voltax/sparse.py:412-535) plus the GPU panel
-    layout and per-level gather tables."""
+    layout and per-level gather tables.
+
+    ``native`` (default: on unless ``VOLTAX_SYMBOLIC=numpy``) runs the C++
+    planner (`voltax_gb300/csrc/symbolic.cpp`); otherwise the numpy
+    restatement below. Both give identical plans."""
+    leaf = LEAF_SIZE if leaf is None else leaf
+    if native is None:
+        native = NATIVE
+    return _make_plan_native(st, leaf) if native else make_plan_numpy(st, leaf)
+
+
+def make_plan_numpy(st: Structure, leaf: int | None = None) -> Plan:
+    """The numpy restatement of the symbolic factorization."""
     leaf = LEAF_SIZE if leaf is None else leaf
     S = st.size
     gid = pivot_groups(st)
@@ -400,17 +444,7 @@ def make_plan(st: Structure, leaf: int | None = None) -> Plan:
         if cost(sel) - cost(sel[:cut]) - cost(sel[cut:]) < SPLIT_SAVING:
             cut = 0
         classes += [part for part in (sel[:cut], sel[cut:]) if len(part)]
-    padded = 0.0
-    ref_work = 0
-    for sel in classes:
-        m, kp, rp = len(sel), int(k[sel].max()), int(r[sel].max())
-        padded += m * (2.0 * kp**3 + 2.0 * kp * kp * rp + 2.0 * kp * rp * rp)
-        ref_work += m * (kp * kp + 2 * kp * rp)
-    flops = float(np.sum(2.0 * k**3 + 2.0 * k * k * r + 2.0 * k * r * r))
-    stats = dict(supernodes=nsn, levels=int(level.max()) + 1, buckets=len(classes),
-                 factor_entries=int(np.sum(k * k + 2 * k * r)), work=ref_work,
-                 flops=flops, padded_flops=padded, largest_supernode=int(k.max()),
-                 pivot_groups=G)
+    stats = _stats(k, r, level, classes, G)
 
     # ---- GPU layout: unpadded panels in supernode order
     sizes = k * k + 2 * k * r
@@ -485,3 +519,87 @@ def make_plan(st: Structure, leaf: int | None = None) -> Plan:
 
     return Plan(S, sns, parents, borders, level, classes, stats, k, r, panel, work,
                 a_pos, levels, sn_of, pos_in, st)
+
+
+# =============================================================================
+# The C++ planner
+# =============================================================================
+
+_FIELDS = ("gid", "sn_ptr", "sn_idx", "parent", "bd_ptr", "bd_idx", "level", "cls_ptr",
+           "cls_idx", "k", "r", "panel", "sn_of", "pos_in", "a_pos", "lv_ptr", "lv_sn",
+           "lv_schur_off", "lv_bord_off", "lv_schur_len", "lv_bord_len", "lv_st_ptr",
+           "st_tgt", "st_ptr", "st_src", "lv_bt_ptr", "bt_tgt", "bt_ptr", "bt_src")
+"""Field ids of vxs_plan_copy, in the order of include/vxg_symbolic.h."""
+
+
+@functools.lru_cache(maxsize=1)
+def _symlib():
+    import ctypes as C
+
+    from . import build
+    lib = C.CDLL(str(build.build_symbolic()))
+    P, I64 = C.c_void_p, C.c_int64
+    lib.vxs_plan_create.argtypes = [I64, P, P, I64, P, P, I64, C.POINTER(C.c_void_p)]
+    lib.vxs_plan_create.restype = C.c_int
+    lib.vxs_plan_len.argtypes = [P, C.c_int32]
+    lib.vxs_plan_len.restype = I64
+    lib.vxs_plan_copy.argtypes = [P, C.c_int32, P]
+    lib.vxs_plan_copy.restype = C.c_int
+    lib.vxs_plan_destroy.argtypes = [P]
+    lib.vxs_plan_destroy.restype = None
+    lib.vxs_last_error.argtypes = []
+    lib.vxs_last_error.restype = C.c_char_p
+    return lib
+
+
+def native_fields(st: Structure, leaf: int) -> dict[str, np.ndarray]:
+    """Every field of the C++ plan of `st`, as int64 arrays."""
+    import ctypes as C
+
+    lib = _symlib()
+    indptr = np.ascontiguousarray(st.indptr, np.int64)
+    indices = np.ascontiguousarray(st.indices, np.int64)
+    ua, ub = union_pairs(st)
+    h = C.c_void_p()
+    rc = lib.vxs_plan_create(st.size, indptr.ctypes.data, indices.ctypes.data, len(ua),
+                             ua.ctypes.data, ub.ctypes.data, leaf, C.byref(h))
+    if rc != 0:
+        msg = lib.vxs_last_error().decode()
+        raise (AssertionError if rc == 2 else ValueError)(msg)
+    try:
+        out = {}
+        for fid, name in enumerate(_FIELDS):
+            a = np.empty(lib.vxs_plan_len(h, fid), np.int64)
+            if lib.vxs_plan_copy(h, fid, a.ctypes.data) != 0:
+                raise ValueError(lib.vxs_last_error().decode())
+            out[name] = a
+        return out
+    finally:
+        lib.vxs_plan_destroy(h)
+
+
+def _split(ptr: np.ndarray, idx: np.ndarray) -> list[np.ndarray]:
+    return np.split(idx, ptr[1:-1]) if len(ptr) > 1 else []
+
+
+def _make_plan_native(st: Structure, leaf: int) -> Plan:
+    f = native_fields(st, leaf)
+    k, r, level = f["k"], f["r"], f["level"]
+    classes = _split(f["cls_ptr"], f["cls_idx"])
+    G = int(f["gid"].max()) + 1 if st.size else 0
+    levels = []
+    for lv in range(len(f["lv_ptr"]) - 1):
+        a, b = f["lv_ptr"][lv], f["lv_ptr"][lv + 1]
+        ta, tb = f["lv_st_ptr"][lv], f["lv_st_ptr"][lv + 1]
+        sptr = f["st_ptr"][ta:tb + 1]
+        ba, bb = f["lv_bt_ptr"][lv], f["lv_bt_ptr"][lv + 1]
+        bptr = f["bt_ptr"][ba:bb + 1]
+        levels.append(LevelTable(
+            f["lv_sn"][a:b], f["lv_schur_off"][a:b], int(f["lv_schur_len"][lv]),
+            f["st_tgt"][ta:tb], sptr - sptr[0], f["st_src"][sptr[0]:sptr[-1]],
+            f["lv_bord_off"][a:b], int(f["lv_bord_len"][lv]),
+            f["bt_tgt"][ba:bb], bptr - bptr[0], f["bt_src"][bptr[0]:bptr[-1]]))
+    return Plan(st.size, _split(f["sn_ptr"], f["sn_idx"]), f["parent"],
+                _split(f["bd_ptr"], f["bd_idx"]), level, classes,
+                _stats(k, r, level, classes, G), k, r, f["panel"],
+                int(np.sum(k * k + 2 * k * r)), f["a_pos"], levels, f["sn_of"], f["pos_in"], st)
