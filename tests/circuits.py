@@ -85,3 +85,31 @@ def opamp_switch_circuit():
     b.resistor("s", "0", 1e3, name="R3")
     b.capacitor("s", "0", 1e-10, name="C1")
     return b.build()
+
+
+def grid_via_builder(n, seed=0, prefix="", b=None, sigma=0.3, sink_max=1e-3, vpad=1.0):
+    """A power grid added to a `CircuitBuilder` device by device: the
+    construction `workloads.power_grid` reproduces from arrays."""
+    import numpy as np
+
+    from voltax_gb300.workloads import grid_pads
+    own = b is None
+    b = CircuitBuilder() if own else b
+    rng = np.random.default_rng(seed)
+    node = lambda i, j: f"{prefix}n{i}_{j}"  # noqa: E731
+    edges = []
+    for i in range(n):
+        for j in range(n):
+            if j + 1 < n:
+                edges.append((node(i, j), node(i, j + 1)))
+            if i + 1 < n:
+                edges.append((node(i, j), node(i + 1, j)))
+    g = np.exp(rng.normal(0.0, sigma, len(edges)))
+    for k, (a, c) in enumerate(edges):
+        b.resistor(a, c, 1.0 / g[k], name=f"{prefix}R{k}")
+    sinks = rng.uniform(0.0, sink_max, n * n)
+    for p in range(n * n):
+        b.isource(node(p // n, p % n), "0", sinks[p], name=f"{prefix}I{p}")
+    for k, (i, j) in enumerate(grid_pads(n)):
+        b.vsource(node(i, j), "0", vpad, name=f"{prefix}Vpad{k}")
+    return b.build() if own else b

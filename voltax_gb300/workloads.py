@@ -44,31 +44,77 @@ def grid_pads(n: int, every: int = 25) -> list[tuple[int, int]]:
     return sorted(sites)
 
 
-def _grid_into(b: CircuitBuilder, n: int, rng, sigma: float, sink_max: float, vpad: float,
-               prefix: str = "") -> None:
-    node = lambda i, j: f"{prefix}n{i}_{j}"  # noqa: E731
-    edges = []
-    for i in range(n):
-        for j in range(n):
-            if j + 1 < n:
-                edges.append((node(i, j), node(i, j + 1)))
-            if i + 1 < n:
-                edges.append((node(i, j), node(i + 1, j)))
-    g = np.exp(rng.normal(0.0, sigma, len(edges)))
-    for k, (a, c) in enumerate(edges):
-        b.resistor(a, c, 1.0 / g[k], name=f"{prefix}R{k}")
+def _grid_arrays(n: int, rng, sigma: float, sink_max: float):
+    """One grid in the order a per-device `CircuitBuilder` walk visits it:
+    segments (i, j)-(i, j+1) then (i, j)-(i+1, j) for i, j row-major, a sink
+    at every node, then the pads. Returns the nodes as row-major ids in
+    first-seen order, the segment ends and pads as indices into that order,
+    and the conductances and sinks."""
+    ids = np.arange(n * n).reshape(n, n)
+    right = np.stack([ids[:, :-1], ids[:, 1:]], -1)                # (n, n-1, 2)
+    down = np.stack([ids[:-1, :], ids[1:, :]], -1)                 # (n-1, n, 2)
+    ends = np.full((n, n, 2, 2), -1, np.int64)  # per site: [right, down] x (a, c)
+    ends[:, :-1, 0] = right
+    ends[:-1, :, 1] = down
+    ends = ends.reshape(-1, 2)
+    ends = ends[ends[:, 0] >= 0]
+    pads = np.array([i * n + j for i, j in grid_pads(n)], np.int64)
+    walk = np.concatenate([ends.ravel(), ids.ravel(), pads])
+    first = np.unique(walk, return_index=True)[1]
+    order = np.argsort(first, kind="stable")          # row-major ids, first seen first
+    rank = np.empty(n * n, np.int64)
+    rank[order] = np.arange(n * n)
+    g = np.exp(rng.normal(0.0, sigma, len(ends)))
     sinks = rng.uniform(0.0, sink_max, n * n)
-    for p in range(n * n):
-        b.isource(node(p // n, p % n), "0", sinks[p], name=f"{prefix}I{p}")
-    for k, (i, j) in enumerate(grid_pads(n)):
-        b.vsource(node(i, j), "0", vpad, name=f"{prefix}Vpad{k}")
+    return order, rank[ends], rank[ids.ravel()], rank[pads], g, sinks
+
+
+def _grids(sides, seeds, sigma: float, sink_max: float, vpad: float, prefixes):
+    """Grids as one circuit, built from arrays: the node numbering, device
+    names, groups and parameters of adding every segment, sink and pad to a
+    `CircuitBuilder` one by one (grid by grid), without the per-device
+    objects."""
+    from .circuit import Circuit
+    from .elements import CurrentSource, Resistor, VoltageSource
+
+    names, seg = [], []
+    r_nodes, i_nodes, v_nodes = [], [], []
+    r_val, i_val = [], []
+    r_names, i_names, v_names = [], [], []
+    off = 0
+    for k, (n, seed, pre) in enumerate(zip(sides, seeds, prefixes)):
+        order, ends, sink_at, pad_at, g, sinks = _grid_arrays(
+            int(n), np.random.default_rng(seed), sigma, sink_max)
+        names += [f"{pre}n{q // n}_{q % n}" for q in order]
+        seg += [k] * len(order)
+        r_nodes.append(ends + off)
+        r_val.append(1.0 / g)
+        i_nodes.append(sink_at + off)
+        i_val.append(sinks)
+        v_nodes.append(pad_at + off)
+        r_names += [f"{pre}R{q}" for q in range(len(ends))]
+        i_names += [f"{pre}I{q}" for q in range(len(sinks))]
+        v_names += [f"{pre}Vpad{q}" for q in range(len(pad_at))]
+        off += len(order)
+    cat = np.concatenate
+    gnd = lambda a: np.stack([a, np.full_like(a, -1)], 1)  # noqa: E731
+    pads = cat(v_nodes)
+    groups, devices = {}, {}
+    for gname, make, members in (
+            ("Resistor", lambda: Resistor(cat(r_nodes).tolist(), cat(r_val)), r_names),
+            ("CurrentSource", lambda: CurrentSource(gnd(cat(i_nodes)).tolist(), cat(i_val)),
+             i_names),
+            ("VoltageSource", lambda: VoltageSource(gnd(pads).tolist(),
+                                                    np.full(len(pads), float(vpad))), v_names)):
+        if members:
+            groups[gname] = make()
+            devices.update((name, (gname, i)) for i, name in enumerate(members))
+    return Circuit(groups, tuple(names), devices), seg
 
 
 def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
                sink_max: float = 1e-3, vpad: float = 1.0):
-    b = CircuitBuilder()
-    _grid_into(b, n, np.random.default_rng(seed), sigma, sink_max, vpad)
-    return b.build()
+    return _grids([n], [seed], sigma, sink_max, vpad, [""])[0]
 
 
 def power_grid_batch(sides, seed: int = 0, sigma: float = 0.3, sink_max: float = 1e-3,
@@ -76,12 +122,9 @@ def power_grid_batch(sides, seed: int = 0, sigma: float = 0.3, sink_max: float =
     """An uneven batch of grids as one circuit of independent segments:
     grid k (nodes ``g{k}_n{i}_{j}``) is `power_grid` ``(sides[k],
     seed + k)``, and segment k is its nodes and pad currents."""
-    b = CircuitBuilder()
-    for k, n in enumerate(sides):
-        _grid_into(b, int(n), np.random.default_rng(seed + k), sigma, sink_max, vpad,
-                   prefix=f"g{k}_")
-    c = b.build()
-    seg = [int(name[1:name.index("_")]) for name in c.layout.node_names]
+    sides = [int(n) for n in sides]
+    c, seg = _grids(sides, [seed + k for k in range(len(sides))], sigma, sink_max, vpad,
+                    [f"g{k}_" for k in range(len(sides))])
     return c.with_segments(seg)
 
 
