@@ -554,3 +554,32 @@ def test_one_singular_instance_fails_alone(engine):
     ref = vx.dc(c, options=vx.Options(engine=engine))
     for k in (0, 2):
         assert float((sol.z[k] - ref.z).abs().max()) < 1e-12
+
+
+@pytest.mark.parametrize("side,precision", [(200, "f64"), (300, "f64"), (300, "f32")])
+def test_wide_supernodes_factor_and_solve(side, precision):
+    """Supernodes wider than a CTA's shared memory (grid 200: k = 164, grid
+    300: k = 246) factor in place in their panels; solves equal SuperLU."""
+    import scipy.sparse.linalg as sla
+    c = workloads.power_grid(side, seed=1)
+    st = symbolic.structure(c)
+    plan = st.plan
+    assert plan.k.max() > (141 if precision == "f64" else 211)
+    z = np.random.default_rng(0).uniform(-0.5, 1.5, c.size)
+    G = ost.add_gmin(ost.jacobian(c, st, z, 0.0), st, c.n_nodes, 1e-12)
+    rhs = np.random.default_rng(1).standard_normal(c.size)
+    lu = sla.splu(st.to_scipy(G).tocsc())
+    fac = sparse.factor(plan, torch.as_tensor(G), precision)
+    for tr in (False, True):
+        x = sparse.solve(plan, fac, torch.as_tensor(rhs), tr, refine=4).cpu().numpy()
+        ref = lu.solve(rhs, trans="T" if tr else "N")
+        np.testing.assert_allclose(x, ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+
+
+def test_wide_supernodes_dc_matches_oracle():
+    c = workloads.power_grid(300, seed=2)
+    sol = vx.dc(c, options=vx.Options(engine="generic"))
+    z_ref, ok_ref, it_ref = _oracle_dc(c)
+    assert bool(sol.converged) == ok_ref
+    assert rel(sol.z.cpu().numpy(), z_ref) < 1e-9
+    assert int(sol.iterations) == it_ref

@@ -13,6 +13,16 @@
 // one thread per target slot sums its sources in ascending order
 // (deterministic, no atomics): work[t] -= sum(S[src]).
 // (voltax/sparse.py:549-572)
+//
+// Wide supernodes of the real factorizations (F11 larger than a CTA's shared
+// memory: k above ~141 in FP64, ~211 in FP32; up to ~437 / ~870) run the
+// same kernel with F11 left in place in its panel (`Wide`): the Gauss-Jordan
+// steps read and write global memory, which the CTA's own barriers order
+// exactly as they order shared memory, and only the pivot row and column and
+// the 32-wide tiles are staged on chip. Every arithmetic operation and its
+// order are unchanged.
+
+#include <type_traits>
 
 #include "cplx.cuh"
 #include "internal.cuh"
@@ -62,7 +72,7 @@ __device__ __forceinline__ void tile_product(int nr, int nc, int k, const T* X, 
   }
 }
 
-template <typename T, int NT>
+template <typename T, int NT, bool Wide>
 __global__ void __launch_bounds__(NT)
     factor_level_kernel(const int* __restrict__ lv_sn, const long long* __restrict__ schur_off,
                         const int* __restrict__ sn_k, const int* __restrict__ sn_r,
@@ -80,14 +90,16 @@ __global__ void __launch_bounds__(NT)
   T* Sout = scratch + (long long)b * scratch_stride + schur_off[blockIdx.x];
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* A = reinterpret_cast<T*>(smem_raw);  // k*k
-  T* col = A + k * k;                     // k: pivot column
+  T* const base = reinterpret_cast<T*>(smem_raw);
+  T* A = Wide ? F11 : base;               // k*k (on chip unless wide)
+  T* col = Wide ? base : base + k * k;    // k: pivot column
   T* rowb = col + k;                      // k: scaled pivot row
   T* tA = rowb + k;                       // kTile*k
   T* tB = tA + kTile * k;                 // k*kTile
   int* perm = reinterpret_cast<int*>(tB + k * kTile);
 
-  for (int i = threadIdx.x; i < k * k; i += NT) A[i] = F11[i];
+  if (!Wide)
+    for (int i = threadIdx.x; i < k * k; i += NT) A[i] = F11[i];
   __syncthreads();
 
   // ---- Gauss-Jordan inverse with partial pivoting (row swaps recorded).
@@ -154,7 +166,8 @@ __global__ void __launch_bounds__(NT)
       }
     }
   __syncthreads();
-  for (int i = threadIdx.x; i < k * k; i += NT) F11[i] = A[i];
+  if (!Wide)
+    for (int i = threadIdx.x; i < k * k; i += NT) F11[i] = A[i];
   if (r == 0) return;
 
   // ---- Ub = W F12 (in place, column tiles)
@@ -210,8 +223,20 @@ __global__ void schur_apply_kernel(int B, long long ntgt, const long long* __res
   work[(long long)b * work_stride + tgt[t]] -= acc;
 }
 
-size_t factor_smem_bytes(int k, size_t es) {
-  return (size_t)(k * k + 2 * k + 2 * kTile * k) * es + (size_t)k * sizeof(int) + 16;
+size_t factor_smem_bytes(int k, size_t es, bool wide = false) {
+  const size_t a = wide ? 0 : (size_t)k * k;
+  return (a + 2 * (size_t)k + 2 * (size_t)kTile * k) * es + (size_t)k * sizeof(int) + 16;
+}
+
+template <typename T, int NT, bool Wide>
+static int launch_level(dim3 grid, size_t smem, const Topo& t, long long lo, T* work,
+                        long long ws, T* scratch, long long ss, cudaStream_t s) {
+  auto kern = factor_level_kernel<T, NT, Wide>;
+  VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<grid, NT, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r, t.sn_panel, work,
+                              ws, scratch, ss);
+  VXG_LAUNCHED();
+  return VXG_OK;
 }
 
 template <typename T>
@@ -253,31 +278,25 @@ static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t
     const long long lo = t.h_lv_ptr[L], hi = t.h_lv_ptr[L + 1];
     if (hi == lo) continue;
     const int kmax = t.h_lv_kmax[L];
-    const size_t smem = factor_smem_bytes(kmax, sizeof(T));
-    if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
     dim3 grid((unsigned)(hi - lo), (unsigned)B);
-    if (kmax > 80) {
-      auto kern = factor_level_kernel<T, 512>;
-      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-      kern<<<grid, 512, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
-                                   t.sn_panel, work, ws, scratch, ss);
-      VXG_LAUNCHED();
+    size_t smem = factor_smem_bytes(kmax, sizeof(T));
+    int st;
+    if (smem > (size_t)max_optin) {  // F11 stays in the panel (real factors only)
+      if constexpr (std::is_same<T, cplx>::value) {
+        return VXG_ERR_TOO_LARGE;
+      } else {
+        smem = factor_smem_bytes(kmax, sizeof(T), true);
+        if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+        st = launch_level<T, 512, true>(grid, smem, t, lo, work, ws, scratch, ss, s);
+      }
+    } else if (kmax > 80) {
+      st = launch_level<T, 512, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
     } else if (kmax > 48) {
-      auto kern = factor_level_kernel<T, 256>;
-      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-      kern<<<grid, 256, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
-                                   t.sn_panel, work, ws, scratch, ss);
-      VXG_LAUNCHED();
+      st = launch_level<T, 256, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
     } else {
-      auto kern = factor_level_kernel<T, 128>;
-      VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-      kern<<<grid, 128, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r,
-                                   t.sn_panel, work, ws, scratch, ss);
-      VXG_LAUNCHED();
+      st = launch_level<T, 128, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
     }
+    if (st != VXG_OK) return st;
     const long long tlo = t.h_lv_st_ptr[L], thi = t.h_lv_st_ptr[L + 1];
     const long long nt = (long long)B * (thi - tlo);
     if (nt) {
