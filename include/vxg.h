@@ -177,7 +177,10 @@ const char* vxg_last_error(void);
 
 /* Upload a topology + plan. Replaces voltax's host-side Structure/Plan
  * caching (voltax/sparse.py:150-193, 412-535); the symbolic analysis itself
- * runs on the host before this call. */
+ * runs on the host before this call. Every index array is checked against
+ * the buffer it addresses (and each group's terminals, internals and
+ * parameter rows against its kind) before anything is copied:
+ * VXG_ERR_INVALID names the first violated field in vxg_last_error(). */
 int vxg_create(const vxg_topology_desc* desc, vxg_handle** out);
 int vxg_destroy(vxg_handle* h);
 

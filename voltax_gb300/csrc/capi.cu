@@ -32,6 +32,10 @@ void set_error(cudaError_t e) {
 
 char* last_error_buffer() { return g_err; }
 
+void set_error_text(const char* what) {
+  std::snprintf(g_err, sizeof(g_err), "invalid topology descriptor: %s", what);
+}
+
 size_t elem_size(int precision) {
   return precision == VXG_F32 ? sizeof(float) : precision == VXG_C128 ? 2 * sizeof(double)
                                                                        : sizeof(double);
@@ -241,6 +245,146 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
   return ok;
 }
 
+// Terminals, internals and parameter rows the device kernels use for each
+// kind (rows of sources: by waveform).
+struct KindShape {
+  int T, K, rows;
+};
+constexpr KindShape kShapes[VXG_KIND_SWITCH + 1] = {
+    {2, 0, 1},  {2, 0, 1},  {2, 1, -1}, {2, 0, -1}, {4, 0, 13}, {4, 0, 12},
+    {2, 0, 4},  {2, 1, 2},  {4, 0, 1},  {3, 0, 10}, {4, 1, 1},  {4, 1, 1},
+    {4, 2, 1},  {4, 2, 3},  {3, 1, 0},  {3, 1, 6},  {4, 0, 4}};
+constexpr int kWaveRows[3] = {1, 4, 7};  // constant, step, pulse
+
+// Every index the kernels dereference lies inside its buffer: checked once
+// on the host, so that a malformed descriptor is an error status, never an
+// out-of-bounds access on the device. Returns the first violation, or null.
+const char* validate(const vxg_topology_desc* d) {
+  const long long S = d->size, nnz = d->nnz;
+  if (S <= 0 || d->n_nodes < 0 || d->n_nodes > S || nnz < S) return "size, n_nodes or nnz";
+  if (d->n_groups < 0 || d->n_groups > VXG_MAX_GROUPS || (d->n_groups && !d->groups))
+    return "n_groups";
+  if (d->n_seg <= 0 || d->n_sn <= 0 || d->n_levels <= 0 || d->work <= 0)
+    return "n_seg, n_sn, n_levels or work";
+  const void* req[] = {d->indptr, d->indices, d->rows, d->tptr, d->tent, d->diag, d->res_ptr,
+                       d->jac_ptr, d->seg_ptr, d->seg_of, d->sn_k, d->sn_r, d->sn_panel,
+                       d->sn_piv_ptr, d->sn_piv, d->sn_bord_ptr, d->a_pos, d->lv_ptr, d->lv_sn,
+                       d->lv_schur_off, d->lv_bord_off, d->lv_schur_len, d->lv_bord_len,
+                       d->lv_st_ptr, d->st_ptr, d->lv_bt_ptr, d->bt_ptr};
+  for (const void* p : req)
+    if (!p) return "a required array is NULL";
+  auto is_ptr = [](const int64_t* p, long long n, long long total) {  // CSR offsets
+    if (p[0] != 0 || p[n] != total) return false;
+    for (long long i = 0; i < n; ++i)
+      if (p[i + 1] < p[i]) return false;
+    return true;
+  };
+  // pattern
+  if (!is_ptr(d->indptr, S, nnz) || !is_ptr(d->tptr, S, nnz)) return "indptr or tptr";
+  for (long long i = 0; i < S; ++i)
+    for (long long e = d->indptr[i]; e < d->indptr[i + 1]; ++e)
+      if (d->rows[e] != i || d->indices[e] < 0 || d->indices[e] >= S) return "indices or rows";
+  for (long long e = 0; e < nnz; ++e)
+    if (d->tent[e] < 0 || d->tent[e] >= nnz) return "tent";
+  for (long long i = 0; i < S; ++i) {
+    const long long e = d->diag[i];
+    if (e < 0 || e >= nnz || d->rows[e] != i || d->indices[e] != i) return "diag";
+  }
+  // groups and stamping gathers
+  long long res = 0, jac = 0;
+  for (int i = 0; i < d->n_groups; ++i) {
+    const vxg_group_desc& g = d->groups[i];
+    if (g.kind < VXG_KIND_CONDUCTANCE || g.kind > VXG_KIND_SWITCH || g.n < 0)
+      return "group kind or size";
+    const KindShape sh = kShapes[g.kind];
+    int rows = sh.rows;
+    if (rows < 0) {
+      if (g.wave < VXG_WAVE_CONSTANT || g.wave > VXG_WAVE_PULSE) return "source waveform";
+      rows = kWaveRows[g.wave];
+    }
+    if (g.T != sh.T || g.K != sh.K) return "group terminals or internals for its kind";
+    if (g.n_params < rows || g.n_params > VXG_MAX_PARAM_ROWS) return "group parameter rows";
+    if (g.n && g.T && !g.nodes) return "group nodes";
+    for (long long q = 0; q < (long long)g.n * g.T; ++q)
+      if (g.nodes[q] < -1 || g.nodes[q] >= d->n_nodes) return "group node index";
+    if (g.K && (g.int_offset < d->n_nodes || g.int_offset + (long long)g.n * g.K > S))
+      return "group internal offset";
+    const long long m = g.T + g.K;
+    res += g.n * m;
+    jac += g.n * m * m;
+  }
+  if (res != d->n_res_slots || jac != d->n_jac_slots) return "n_res_slots or n_jac_slots";
+  if (!is_ptr(d->res_ptr, S, d->res_ptr[S]) || !is_ptr(d->jac_ptr, nnz, d->jac_ptr[nnz]))
+    return "res_ptr or jac_ptr";
+  if ((d->res_ptr[S] && !d->res_src) || (d->jac_ptr[nnz] && !d->jac_src)) return "res_src or jac_src";
+  for (long long q = 0; q < d->res_ptr[S]; ++q)
+    if (d->res_src[q] < 0 || d->res_src[q] >= res) return "res_src";
+  for (long long q = 0; q < d->jac_ptr[nnz]; ++q)
+    if (d->jac_src[q] < 0 || d->jac_src[q] >= jac) return "jac_src";
+  // segments
+  {
+    const int32_t* sp = d->seg_ptr;
+    if (sp[0] != 0 || sp[d->n_seg] != S) return "seg_ptr";
+    for (int s = 0; s < d->n_seg; ++s) {
+      if (sp[s + 1] < sp[s]) return "seg_ptr";
+      for (long long q = sp[s]; q < sp[s + 1]; ++q) {
+        const long long u = d->seg_idx ? d->seg_idx[q] : q;
+        if (u < 0 || u >= S || d->seg_of[u] != s) return "seg_idx or seg_of";
+      }
+    }
+  }
+  // supernodes and panels
+  const long long nsn = d->n_sn;
+  long long piv = 0, bord = 0;
+  for (long long j = 0; j < nsn; ++j) {
+    const long long k = d->sn_k[j], r = d->sn_r[j];
+    if (k < 1 || r < 0 || d->sn_piv_ptr[j] != piv || d->sn_bord_ptr[j] != bord)
+      return "sn_k, sn_r or their offsets";
+    piv += k;
+    bord += r;
+    if (d->sn_panel[j] < 0 || d->sn_panel[j] + k * k + 2 * k * r > d->work) return "sn_panel";
+  }
+  if (piv != S || d->sn_piv_ptr[nsn] != S || d->sn_bord_ptr[nsn] != bord) return "sn_piv_ptr";
+  if (bord && !d->sn_bord) return "sn_bord";
+  for (long long q = 0; q < S; ++q)
+    if (d->sn_piv[q] < 0 || d->sn_piv[q] >= S) return "sn_piv";
+  for (long long q = 0; q < bord; ++q)
+    if (d->sn_bord[q] < 0 || d->sn_bord[q] >= S) return "sn_bord";
+  for (long long e = 0; e < nnz; ++e)
+    if (d->a_pos[e] < 0 || d->a_pos[e] >= d->work) return "a_pos";
+  // levels and their gathers
+  const long long nl = d->n_levels;
+  if (!is_ptr(d->lv_ptr, nl, nsn)) return "lv_ptr";
+  const long long nst = d->lv_st_ptr[nl], nbt = d->lv_bt_ptr[nl];
+  if (!is_ptr(d->lv_st_ptr, nl, nst) || !is_ptr(d->lv_bt_ptr, nl, nbt)) return "lv_st_ptr or lv_bt_ptr";
+  if (!is_ptr(d->st_ptr, nst, d->st_ptr[nst]) || !is_ptr(d->bt_ptr, nbt, d->bt_ptr[nbt]))
+    return "st_ptr or bt_ptr";
+  if ((nst && (!d->st_tgt || !d->st_src)) || (nbt && (!d->bt_tgt || !d->bt_src)))
+    return "st_tgt, st_src, bt_tgt or bt_src";
+  for (long long L = 0; L < nl; ++L) {
+    const long long slen = d->lv_schur_len[L], blen = d->lv_bord_len[L];
+    if (slen < 0 || blen < 0) return "lv_schur_len or lv_bord_len";
+    for (long long q = d->lv_ptr[L]; q < d->lv_ptr[L + 1]; ++q) {
+      const long long j = d->lv_sn[q];
+      if (j < 0 || j >= nsn) return "lv_sn";
+      const long long r = d->sn_r[j];
+      if (d->lv_schur_off[q] < 0 || d->lv_schur_off[q] + r * r > slen) return "lv_schur_off";
+      if (d->lv_bord_off[q] < 0 || d->lv_bord_off[q] + r > blen) return "lv_bord_off";
+    }
+    for (long long t = d->lv_st_ptr[L]; t < d->lv_st_ptr[L + 1]; ++t) {
+      if (d->st_tgt[t] < 0 || d->st_tgt[t] >= d->work) return "st_tgt";
+      for (long long p = d->st_ptr[t]; p < d->st_ptr[t + 1]; ++p)
+        if (d->st_src[p] < 0 || d->st_src[p] >= slen) return "st_src";
+    }
+    for (long long t = d->lv_bt_ptr[L]; t < d->lv_bt_ptr[L + 1]; ++t) {
+      if (d->bt_tgt[t] < 0 || d->bt_tgt[t] >= S) return "bt_tgt";
+      for (long long p = d->bt_ptr[t]; p < d->bt_ptr[t + 1]; ++p)
+        if (d->bt_src[p] < 0 || d->bt_src[p] >= blen) return "bt_src";
+    }
+  }
+  return nullptr;
+}
+
 }  // namespace vxg
 
 using namespace vxg;
@@ -250,14 +394,11 @@ extern "C" {
 const char* vxg_last_error(void) { return g_err; }
 
 int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
-  if (!d || !out || d->size <= 0 || d->n_groups < 0 || d->n_groups > VXG_MAX_GROUPS ||
-      d->n_seg <= 0 || d->n_levels < 0)
+  if (!d || !out) return VXG_ERR_INVALID;
+  if (const char* why = validate(d)) {
+    set_error_text(why);
     return VXG_ERR_INVALID;
-  for (int i = 0; i < d->n_groups; ++i)
-    if (d->groups[i].kind < VXG_KIND_CONDUCTANCE || d->groups[i].kind > VXG_KIND_SWITCH ||
-        d->groups[i].n_params < 0 || d->groups[i].n_params > VXG_MAX_PARAM_ROWS ||
-        d->groups[i].T < 0 || d->groups[i].K < 0 || d->groups[i].T + d->groups[i].K > kMaxM)
-      return VXG_ERR_INVALID;
+  }
   *out = nullptr;
   vxg_handle* h = new (std::nothrow) vxg_handle;
   if (!h) return VXG_ERR_ALLOC;
