@@ -131,7 +131,16 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
     ap.add_argument("--epochs", type=int, default=40, help="ota_warm: training epochs")
+    ap.add_argument("--grid-sides", type=int, nargs=2, default=None, metavar=("LO", "HI"),
+                    help="grids: mesh sides drawn from U{LO..HI} (default 50 120; the "
+                         "full uneven-grid configuration is --instances 512 --grid-sides 50 300)")
     a = ap.parse_args()
+    if a.grid_sides is not None:
+        global GRID_SIDES
+        lo, hi = a.grid_sides
+        if not 2 <= lo <= hi:
+            ap.error("--grid-sides needs 2 <= LO <= HI")
+        GRID_SIDES = (lo, hi)
     w = WORKLOADS[a.workload]
     if a.instances is None:
         a.instances = w.default_instances
@@ -657,6 +666,7 @@ def main_grids(a, w, cpu):
     t0 = time.perf_counter()
     circuit = w.circuit(a.instances, seed=0)
     st = symbolic.structure(circuit)
+    st.plan  # the C++ planner (otherwise built lazily by the first analysis)
     plan_s = time.perf_counter() - t0
     n_grids = a.instances
     c_dev = to_device(circuit, dev)

@@ -83,6 +83,10 @@ int64_t vxs_plan_len(const vxs_plan* p, int32_t field);
 /* Copies a field into dst (vxs_plan_len elements). */
 int vxs_plan_copy(const vxs_plan* p, int32_t field, int64_t* dst);
 
+/* Copies a field into dst and frees the plan's copy of it (its length is 0
+ * afterwards): the caller never holds two copies of the large gathers. */
+int vxs_plan_take(vxs_plan* p, int32_t field, int64_t* dst);
+
 void vxs_plan_destroy(vxs_plan* p);
 
 /* Text of the calling thread's last error. */

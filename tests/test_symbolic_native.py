@@ -12,7 +12,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from voltax_gb300 import build, symbolic, workloads
+from voltax_gb300 import build, runtime, symbolic, workloads
 
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(Path(__file__).parent))
@@ -120,3 +120,40 @@ def test_default_planner_is_native(monkeypatch):
                         lambda *a: calls.append(1) or real(*a))
     symbolic.make_plan(st)
     assert calls == [1]
+
+
+@pytest.mark.parametrize("name", ["grid37", "grid_batch", "mirror_adder", "ota_chain", "mixed"])
+def test_device_tables_from_native_plan_equal_restatement(name):
+    """The upload tables taken straight from the C++ plan's flat arrays equal
+    those assembled from the numpy plan's per-level tables."""
+    c = CASES[name]()
+    st = symbolic.structure(c)
+    a = runtime.Tables(c, st, symbolic.make_plan(st, native=True))
+    b = runtime.Tables(c, st, symbolic.make_plan_numpy(st))
+    keys = [k for k, v in vars(b).items() if isinstance(v, np.ndarray)]
+    assert "st_src" in keys and "bt_ptr" in keys and "sn_piv" in keys
+    for k in keys:
+        x, y = getattr(a, k), getattr(b, k)
+        assert x.dtype == y.dtype and np.array_equal(x, y), k
+    assert a.work == b.work and a.n_seg == b.n_seg
+
+
+def test_take_moves_fields_out_of_the_plan():
+    import ctypes as C
+    lib = symbolic._symlib()
+    st = symbolic.structure(workloads.power_grid(5))
+    indptr = np.ascontiguousarray(st.indptr, np.int64)
+    indices = np.ascontiguousarray(st.indices, np.int64)
+    ua, ub = symbolic.union_pairs(st)
+    h = C.c_void_p()
+    assert lib.vxs_plan_create(st.size, indptr.ctypes.data, indices.ctypes.data, len(ua),
+                               ua.ctypes.data, ub.ctypes.data, 16, C.byref(h)) == 0
+    try:
+        n = lib.vxs_plan_len(h, 14)
+        assert n == st.nnz
+        a = np.empty(n, np.int64)
+        assert lib.vxs_plan_take(h, 14, a.ctypes.data) == 0
+        assert lib.vxs_plan_len(h, 14) == 0
+        assert a.min() >= 0
+    finally:
+        lib.vxs_plan_destroy(h)

@@ -57,7 +57,7 @@ def build_symbolic(verbose: bool = False) -> Path:
     if lib.exists() and lib.stat().st_mtime > max(d.stat().st_mtime for d in deps):
         return lib
     tmp = OUT / f".libvxg_symbolic.{os.getpid()}.so"
-    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-shared", "-fPIC",
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-shared", "-fPIC", "-pthread",
            f"-I{INCLUDE}", str(src), "-o", str(tmp)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

@@ -13,11 +13,16 @@
 #include "vxg_symbolic.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -310,6 +315,137 @@ double bucket_cost(i64 len, i64 K, i64 R) {
 
 constexpr double kSplitSaving = 1e6;
 
+struct GatherScratch {
+  Vec tq;                             // target of each source, in source order
+  std::vector<uint64_t> pa, pb;       // packed (target << 32 | source)
+  Vec key_a, key_b, src_a, src_b;     // unpacked, when a value needs 32+ bits
+};
+
+// Unique targets of `w.tq` ascending (`tgt`), the end of each target's
+// sources (`end`, CSR ends from 0) and the sources in that order, ascending
+// within a target (`src`): a stable LSD radix sort of the sources by target
+// (11-bit digits; sequential passes, no random access over the panel).
+void gather(GatherScratch& w, i64 n_targets, Vec& tgt, Vec& end, Vec& src) {
+  const i64 n = (i64)w.tq.size();
+  tgt.clear();
+  end.clear();
+  src.clear();
+  if (n == 0) return;
+  constexpr int kBits = 11;
+  constexpr i64 kRadix = i64(1) << kBits;
+  std::vector<i64> count(kRadix);
+  auto digit_passes = [&](auto&& key_of, auto&& move) {
+    for (int shift = 0; shift == 0 || ((n_targets - 1) >> shift) > 0; shift += kBits) {
+      std::fill(count.begin(), count.end(), 0);
+      for (i64 i = 0; i < n; ++i) count[(key_of(i) >> shift) & (kRadix - 1)]++;
+      i64 run = 0;
+      for (i64 d = 0; d < kRadix; ++d) {
+        const i64 c = count[d];
+        count[d] = run;
+        run += c;
+      }
+      for (i64 i = 0; i < n; ++i) move(i, count[(key_of(i) >> shift) & (kRadix - 1)]++);
+      move(-1, 0);  // swap the buffers
+    }
+  };
+  auto emit = [&](auto&& key_at, auto&& src_at) {
+    tgt.reserve(n);
+    end.reserve(n);
+    src.resize(n);
+    for (i64 i = 0; i < n; ++i) {
+      const i64 k = key_at(i);
+      if (i > 0 && k != key_at(i - 1)) end.push_back(i);
+      if (i == 0 || k != key_at(i - 1)) tgt.push_back(k);
+      src[i] = src_at(i);
+    }
+    end.push_back(n);
+    tgt.shrink_to_fit();
+    end.shrink_to_fit();
+  };
+  if (n_targets <= (i64(1) << 32) && n <= (i64(1) << 32)) {
+    w.pa.resize(n);
+    w.pb.resize(n);
+    for (i64 s = 0; s < n; ++s) w.pa[s] = ((uint64_t)w.tq[s] << 32) | (uint64_t)s;
+    digit_passes([&](i64 i) { return (i64)(w.pa[i] >> 32); },
+                 [&](i64 i, i64 at) {
+                   if (i < 0) w.pa.swap(w.pb);
+                   else w.pb[at] = w.pa[i];
+                 });
+    emit([&](i64 i) { return (i64)(w.pa[i] >> 32); },
+         [&](i64 i) { return (i64)(w.pa[i] & 0xffffffffu); });
+  } else {
+    w.key_a = w.tq;
+    w.src_a.resize(n);
+    for (i64 s = 0; s < n; ++s) w.src_a[s] = s;
+    w.key_b.resize(n);
+    w.src_b.resize(n);
+    digit_passes([&](i64 i) { return w.key_a[i]; },
+                 [&](i64 i, i64 at) {
+                   if (i < 0) {
+                     w.key_a.swap(w.key_b);
+                     w.src_a.swap(w.src_b);
+                   } else {
+                     w.key_b[at] = w.key_a[i];
+                     w.src_b[at] = w.src_a[i];
+                   }
+                 });
+    emit([&](i64 i) { return w.key_a[i]; }, [&](i64 i) { return w.src_a[i]; });
+  }
+}
+
+// One elimination level's launch tables (ends are local CSR ends).
+struct LevelOut {
+  Vec sn, schur_off, bord_off, st_tgt, st_end, st_src, bt_tgt, bt_end, bt_src;
+  i64 schur_len = 0, bord_len = 0;
+};
+
+// Runs fn(level, scratch) for every level on up to VXS_THREADS threads
+// (default: the hardware's, at most 8); the first error is rethrown here.
+template <typename Fn>
+void run_levels(i64 nlev, Fn&& fn) {
+  i64 want = (i64)std::thread::hardware_concurrency();
+  if (want <= 0) want = 1;
+  want = std::min<i64>(want, 8);
+  if (const char* env = std::getenv("VXS_THREADS")) {
+    const long v = std::strtol(env, nullptr, 10);
+    if (v > 0) want = v;
+  }
+  const i64 nthreads = std::max<i64>(1, std::min(want, nlev));
+  std::atomic<i64> next{0};
+  std::atomic<bool> failed{false};
+  std::mutex mu;
+  int code = VXS_OK;
+  std::string msg;
+  auto worker = [&] {
+    GatherScratch w;
+    for (;;) {
+      const i64 lv = next.fetch_add(1);
+      if (lv >= nlev || failed.load()) return;
+      try {
+        fn(lv, w);
+      } catch (const Error& e) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!failed.exchange(true)) code = e.code, msg = e.msg;
+      } catch (const std::bad_alloc&) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!failed.exchange(true)) code = VXS_ERR_NOMEM, msg = "out of host memory";
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (i64 t = 1; t < nthreads; ++t) {
+    try {
+      pool.emplace_back(worker);
+    } catch (const std::system_error&) {
+      break;  // fewer threads: the calling thread takes the remaining levels
+    }
+  }
+  worker();
+  for (std::thread& t : pool) t.join();
+  if (failed.load()) fail(code, msg);
+}
+
+
 void build(Plan& P, i64 S, const i64* indptr, const i64* indices, i64 n_unions,
            const i64* ua, const i64* ub, i64 leaf) {
   if (S < 0 || leaf < 1) fail(VXS_ERR_INVALID, "S must be >= 0 and leaf >= 1");
@@ -495,7 +631,36 @@ void build(Plan& P, i64 S, const i64* indptr, const i64* indices, i64 n_unions,
   a_pos.resize(nnz);
   for (i64 e = 0; e < nnz; ++e) a_pos[e] = position(rows[e], indices[e]);
 
-  // ---- per-level launch tables with deterministic gathers
+  // ---- per-level launch tables with deterministic gathers. Levels are
+  // independent (every input is read-only here): a small pool of threads
+  // builds them, and they are concatenated in level order.
+  const i64 work_len = nsn ? panel[nsn - 1] + K[nsn - 1] * K[nsn - 1] + 2 * K[nsn - 1] * R[nsn - 1] : 0;
+  std::vector<LevelOut> outs(nlev);
+  auto build_level = [&](i64 lv, GatherScratch& w, LevelOut& o) {
+    o.sn.assign(by_level.idx.begin() + by_level.begin(lv), by_level.idx.begin() + by_level.end(lv));
+    std::stable_sort(o.sn.begin(), o.sn.end(),
+                     [&](i64 a, i64 b) { return key3(K[a], R[a]) > key3(K[b], R[b]); });
+    i64 soff = 0, boff = 0;
+    w.tq.clear();
+    for (i64 j : o.sn) {
+      o.schur_off.push_back(soff);
+      o.bord_off.push_back(boff);
+      const i64 r = R[j];
+      const i64* b = bd_idx.data() + bd_ptr[j];
+      for (i64 x = 0; x < r; ++x)  // row-major r x r block: source soff + x*r + y
+        for (i64 y = 0; y < r; ++y) w.tq.push_back(position(b[x], b[y]));
+      soff += r * r;
+      boff += r;
+    }
+    o.schur_len = soff;
+    o.bord_len = boff;
+    gather(w, work_len, o.st_tgt, o.st_end, o.st_src);
+    w.tq.clear();
+    for (i64 j : o.sn) w.tq.insert(w.tq.end(), bd_idx.begin() + bd_ptr[j], bd_idx.begin() + bd_ptr[j + 1]);
+    gather(w, S, o.bt_tgt, o.bt_end, o.bt_src);
+  };
+  run_levels(nlev, [&](i64 lv, GatherScratch& w) { build_level(lv, w, outs[lv]); });
+
   Vec& lv_ptr = P.f[VXS_LV_PTR];
   Vec& lv_sn = P.f[VXS_LV_SN];
   Vec& lv_schur_off = P.f[VXS_LV_SCHUR_OFF];
@@ -510,76 +675,45 @@ void build(Plan& P, i64 S, const i64* indptr, const i64* indices, i64 n_unions,
   Vec& bt_tgt = P.f[VXS_BT_TGT];
   Vec& bt_ptr = P.f[VXS_BT_PTR];
   Vec& bt_src = P.f[VXS_BT_SRC];
+  i64 n_st = 0, n_ss = 0, n_bt = 0, n_bs = 0;
+  for (const LevelOut& o : outs) {
+    n_st += (i64)o.st_tgt.size();
+    n_ss += (i64)o.st_src.size();
+    n_bt += (i64)o.bt_tgt.size();
+    n_bs += (i64)o.bt_src.size();
+  }
+  lv_sn.reserve(nsn);
+  st_tgt.reserve(n_st);
+  st_ptr.reserve(n_st + 1);
+  st_src.reserve(n_ss);
+  bt_tgt.reserve(n_bt);
+  bt_ptr.reserve(n_bt + 1);
+  bt_src.reserve(n_bs);
   lv_ptr.assign(1, 0);
   lv_st_ptr.assign(1, 0);
   lv_bt_ptr.assign(1, 0);
   st_ptr.assign(1, 0);
   bt_ptr.assign(1, 0);
-  // Gather of one level: `tq[s]` is the target of source s (sources are
-  // numbered in generation order). Unique targets ascending, each with its
-  // sources ascending: a stable LSD radix sort of the sources by target
-  // (11-bit digits; sequential passes, no random access over the panel).
-  Vec tq, key_a, key_b, src_a, src_b;
-  auto gather = [&](i64 n_targets, Vec& tgt, Vec& ptr, Vec& src) {
-    const i64 n = (i64)tq.size();
-    if (n == 0) return;
-    key_a = tq;
-    src_a.resize(n);
-    for (i64 s = 0; s < n; ++s) src_a[s] = s;
-    key_b.resize(n);
-    src_b.resize(n);
-    constexpr int kBits = 11;
-    constexpr i64 kRadix = i64(1) << kBits;
-    i64 count[kRadix];
-    for (int shift = 0; shift == 0 || ((n_targets - 1) >> shift) > 0; shift += kBits) {
-      std::fill(count, count + kRadix, 0);
-      for (i64 i = 0; i < n; ++i) count[(key_a[i] >> shift) & (kRadix - 1)]++;
-      i64 run = 0;
-      for (i64 d = 0; d < kRadix; ++d) {
-        i64 c = count[d];
-        count[d] = run;
-        run += c;
-      }
-      for (i64 i = 0; i < n; ++i) {
-        i64 at = count[(key_a[i] >> shift) & (kRadix - 1)]++;
-        key_b[at] = key_a[i];
-        src_b[at] = src_a[i];
-      }
-      key_a.swap(key_b);
-      src_a.swap(src_b);
-    }
-    for (i64 i = 0; i < n; ++i) {
-      if (i > 0 && key_a[i] != key_a[i - 1]) ptr.push_back((i64)src.size() + i);
-      if (i == 0 || key_a[i] != key_a[i - 1]) tgt.push_back(key_a[i]);
-    }
-    src.insert(src.end(), src_a.begin(), src_a.end());
-    ptr.push_back((i64)src.size());
+  auto append = [](Vec& dst, Vec& src) {
+    dst.insert(dst.end(), src.begin(), src.end());
+    Vec().swap(src);
   };
-  const i64 work_len = nsn ? panel[nsn - 1] + K[nsn - 1] * K[nsn - 1] + 2 * K[nsn - 1] * R[nsn - 1] : 0;
-  for (i64 lv = 0; lv < nlev; ++lv) {
-    Vec ids(by_level.idx.begin() + by_level.begin(lv), by_level.idx.begin() + by_level.end(lv));
-    std::stable_sort(ids.begin(), ids.end(),
-                     [&](i64 a, i64 b) { return key3(K[a], R[a]) > key3(K[b], R[b]); });
-    i64 soff = 0, boff = 0;
-    tq.clear();
-    for (i64 j : ids) {
-      lv_sn.push_back(j);
-      lv_schur_off.push_back(soff);
-      lv_bord_off.push_back(boff);
-      i64 r = R[j];
-      const i64* b = bd_idx.data() + bd_ptr[j];
-      for (i64 x = 0; x < r; ++x)  // row-major r x r block: source soff + x*r + y
-        for (i64 y = 0; y < r; ++y) tq.push_back(position(b[x], b[y]));
-      soff += r * r;
-      boff += r;
-    }
-    gather(work_len, st_tgt, st_ptr, st_src);
-    tq.clear();
-    for (i64 j : ids) tq.insert(tq.end(), bd_idx.begin() + bd_ptr[j], bd_idx.begin() + bd_ptr[j + 1]);
-    gather(S, bt_tgt, bt_ptr, bt_src);
+  for (LevelOut& o : outs) {  // level order; each level freed once copied
+    append(lv_sn, o.sn);
+    append(lv_schur_off, o.schur_off);
+    append(lv_bord_off, o.bord_off);
+    const i64 sbase = (i64)st_src.size(), bbase = (i64)bt_src.size();
+    for (i64 e : o.st_end) st_ptr.push_back(sbase + e);
+    for (i64 e : o.bt_end) bt_ptr.push_back(bbase + e);
+    Vec().swap(o.st_end);
+    Vec().swap(o.bt_end);
+    append(st_tgt, o.st_tgt);
+    append(st_src, o.st_src);
+    append(bt_tgt, o.bt_tgt);
+    append(bt_src, o.bt_src);
     lv_ptr.push_back((i64)lv_sn.size());
-    lv_schur_len.push_back(soff);
-    lv_bord_len.push_back(boff);
+    lv_schur_len.push_back(o.schur_len);
+    lv_bord_len.push_back(o.bord_len);
     lv_st_ptr.push_back((i64)st_tgt.size());
     lv_bt_ptr.push_back((i64)bt_tgt.size());
   }
@@ -641,6 +775,12 @@ int vxs_plan_copy(const vxs_plan* p, int32_t field, int64_t* dst) {
     std::memcpy(dst, v.data(), v.size() * sizeof(int64_t));
   }
   return VXS_OK;
+}
+
+int vxs_plan_take(vxs_plan* p, int32_t field, int64_t* dst) {
+  const int rc = vxs_plan_copy(p, field, dst);
+  if (rc == VXS_OK) Vec().swap(p->p.f[field]);
+  return rc;
 }
 
 void vxs_plan_destroy(vxs_plan* p) { delete p; }

@@ -113,10 +113,22 @@ class Tables:
         self.sn_r = i32(plan.r)
         self.sn_panel = i64(plan.panel)
         self.sn_piv_ptr = i64(np.concatenate([[0], np.cumsum(plan.k)]))
-        self.sn_piv = i32(np.concatenate(plan.supernodes))
         self.sn_bord_ptr = i64(np.concatenate([[0], np.cumsum(plan.r)]))
-        self.sn_bord = i32(np.concatenate(plan.borders) if len(plan.borders) else [])
         self.a_pos = i64(plan.a_pos)
+        self.work = int(plan.work)
+        if plan.flat is not None:  # the C++ planner's arrays already have this layout
+            f = plan.flat
+            self.sn_piv, self.sn_bord = i32(f["sn_idx"]), i32(f["bd_idx"])
+            self.lv_ptr, self.lv_sn = i64(f["lv_ptr"]), i32(f["lv_sn"])
+            self.lv_schur_off, self.lv_bord_off = i64(f["lv_schur_off"]), i64(f["lv_bord_off"])
+            self.lv_schur_len, self.lv_bord_len = i64(f["lv_schur_len"]), i64(f["lv_bord_len"])
+            self.lv_st_ptr, self.st_tgt = i64(f["lv_st_ptr"]), i64(f["st_tgt"])
+            self.st_ptr, self.st_src = i64(f["st_ptr"]), i64(f["st_src"])
+            self.lv_bt_ptr, self.bt_tgt = i64(f["lv_bt_ptr"]), i32(f["bt_tgt"])
+            self.bt_ptr, self.bt_src = i64(f["bt_ptr"]), i64(f["bt_src"])
+            return
+        self.sn_piv = i32(np.concatenate(plan.supernodes))
+        self.sn_bord = i32(np.concatenate(plan.borders) if len(plan.borders) else [])
         lv = plan.levels
         self.lv_ptr = i64(np.concatenate([[0], np.cumsum([len(x.sns) for x in lv])]))
         self.lv_sn = i32(np.concatenate([x.sns for x in lv]))
@@ -136,7 +148,6 @@ class Tables:
         bsrc_off = np.concatenate([[0], np.cumsum([len(x.bord_src) for x in lv])])
         self.bt_ptr = i64(np.concatenate([x.bord_ptr[:-1] + o for x, o in zip(lv, bsrc_off)]
                                          + [[bsrc_off[-1]]]))
-        self.work = int(plan.work)
 
     @staticmethod
     def _pull(targets: np.ndarray, slot_ids: np.ndarray, n_out: int):

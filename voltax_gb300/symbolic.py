@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import functools
 import os
+from collections.abc import Sequence
 from dataclasses import dataclass, field
 from functools import cached_property
 
@@ -127,7 +128,9 @@ def build_structure(S: int, nv: int, offsets: dict, groups, leaf: int = LEAF_SIZ
         c = np.broadcast_to(blocks[:, None, :], r.shape)
         keep = (r >= 0) & (c >= 0)
         keys.append(r[keep] * S + c[keep])
-    uniq = np.unique(np.concatenate(keys))
+    uniq = np.concatenate(keys)
+    uniq.sort()  # sorted distinct keys (a sort beats np.unique's hashing here)
+    uniq = uniq[np.concatenate(([True], uniq[1:] != uniq[:-1]))]
     row_of = uniq // S
     indptr = np.zeros(S + 1, np.int64)
     np.cumsum(np.bincount(row_of, minlength=S), out=indptr[1:])
@@ -318,6 +321,9 @@ class Plan:
     sn_of: np.ndarray | None = None
     pos_in: np.ndarray | None = None
     structure: object = None
+    flat: dict | None = None
+    """The C++ planner's arrays (all levels concatenated, global CSR
+    offsets: the layout `vxg_create` takes), or None for the numpy plan."""
 
 
 @dataclass(frozen=True, eq=False)
@@ -545,6 +551,8 @@ def _symlib():
     lib.vxs_plan_len.restype = I64
     lib.vxs_plan_copy.argtypes = [P, C.c_int32, P]
     lib.vxs_plan_copy.restype = C.c_int
+    lib.vxs_plan_take.argtypes = [P, C.c_int32, P]
+    lib.vxs_plan_take.restype = C.c_int
     lib.vxs_plan_destroy.argtypes = [P]
     lib.vxs_plan_destroy.restype = None
     lib.vxs_last_error.argtypes = []
@@ -553,7 +561,8 @@ def _symlib():
 
 
 def native_fields(st: Structure, leaf: int) -> dict[str, np.ndarray]:
-    """Every field of the C++ plan of `st`, as int64 arrays."""
+    """Every field of the C++ plan of `st`, as int64 arrays (each moved out
+    of the library's memory as it is copied)."""
     import ctypes as C
 
     lib = _symlib()
@@ -570,7 +579,7 @@ def native_fields(st: Structure, leaf: int) -> dict[str, np.ndarray]:
         out = {}
         for fid, name in enumerate(_FIELDS):
             a = np.empty(lib.vxs_plan_len(h, fid), np.int64)
-            if lib.vxs_plan_copy(h, fid, a.ctypes.data) != 0:
+            if lib.vxs_plan_take(h, fid, a.ctypes.data) != 0:
                 raise ValueError(lib.vxs_last_error().decode())
             out[name] = a
         return out
@@ -582,24 +591,43 @@ def _split(ptr: np.ndarray, idx: np.ndarray) -> list[np.ndarray]:
     return np.split(idx, ptr[1:-1]) if len(ptr) > 1 else []
 
 
-def _make_plan_native(st: Structure, leaf: int) -> Plan:
-    f = native_fields(st, leaf)
-    k, r, level = f["k"], f["r"], f["level"]
-    classes = _split(f["cls_ptr"], f["cls_idx"])
-    G = int(f["gid"].max()) + 1 if st.size else 0
-    levels = []
-    for lv in range(len(f["lv_ptr"]) - 1):
+class _Levels(Sequence):
+    """The per-level `LevelTable` views of a C++ plan, made on access (the
+    flat arrays are what the library uploads)."""
+
+    def __init__(self, f: dict):
+        self._f = f
+
+    def __len__(self) -> int:
+        return len(self._f["lv_ptr"]) - 1
+
+    def __getitem__(self, lv):
+        if isinstance(lv, slice):
+            return [self[i] for i in range(*lv.indices(len(self)))]
+        if lv < 0:
+            lv += len(self)
+        if not 0 <= lv < len(self):
+            raise IndexError(lv)
+        f = self._f
         a, b = f["lv_ptr"][lv], f["lv_ptr"][lv + 1]
         ta, tb = f["lv_st_ptr"][lv], f["lv_st_ptr"][lv + 1]
         sptr = f["st_ptr"][ta:tb + 1]
         ba, bb = f["lv_bt_ptr"][lv], f["lv_bt_ptr"][lv + 1]
         bptr = f["bt_ptr"][ba:bb + 1]
-        levels.append(LevelTable(
+        return LevelTable(
             f["lv_sn"][a:b], f["lv_schur_off"][a:b], int(f["lv_schur_len"][lv]),
             f["st_tgt"][ta:tb], sptr - sptr[0], f["st_src"][sptr[0]:sptr[-1]],
             f["lv_bord_off"][a:b], int(f["lv_bord_len"][lv]),
-            f["bt_tgt"][ba:bb], bptr - bptr[0], f["bt_src"][bptr[0]:bptr[-1]]))
+            f["bt_tgt"][ba:bb], bptr - bptr[0], f["bt_src"][bptr[0]:bptr[-1]])
+
+
+def _make_plan_native(st: Structure, leaf: int) -> Plan:
+    f = native_fields(st, leaf)
+    k, r, level = f["k"], f["r"], f["level"]
+    classes = _split(f["cls_ptr"], f["cls_idx"])
+    G = int(f["gid"].max()) + 1 if st.size else 0
     return Plan(st.size, _split(f["sn_ptr"], f["sn_idx"]), f["parent"],
                 _split(f["bd_ptr"], f["bd_idx"]), level, classes,
                 _stats(k, r, level, classes, G), k, r, f["panel"],
-                int(np.sum(k * k + 2 * k * r)), f["a_pos"], levels, f["sn_of"], f["pos_in"], st)
+                int(np.sum(k * k + 2 * k * r)), f["a_pos"], _Levels(f), f["sn_of"],
+                f["pos_in"], st, f)
