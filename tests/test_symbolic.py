@@ -119,3 +119,23 @@ def test_structure_is_cached_per_topology():
     a = workloads.power_grid(8, seed=1)
     b = workloads.power_grid(8, seed=2)
     assert symbolic.structure(a) is symbolic.structure(b)
+
+
+def test_pattern_covers_device_blocks_only():
+    """voltax tests/test_sparse.py:192-198: the pattern is the union of the
+    device blocks plus the diagonal, nothing else."""
+    from voltax_gb300.builder import CircuitBuilder
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.resistor("in", "a", 1e3, name="R1")
+    b.resistor("a", "out", 2e3, name="R2")
+    b.resistor("out", "0", 1e4, name="Rload")
+    b.capacitor("a", "0", 1e-9, name="C1")
+    b.capacitor("out", "0", 0.5e-9, name="C2")
+    c = b.build()
+    st = symbolic.structure(c)
+    P = st.to_scipy(np.ones(st.nnz)).toarray()
+    a, out, vin = c.layout.node("a"), c.layout.node("out"), c.layout.internal("Vin")
+    assert P[a, out] and P[out, a] and P[vin, c.layout.node("in")]
+    assert not P[c.layout.node("in"), out]  # no device connects in and out
+    assert np.all(np.diag(P))
