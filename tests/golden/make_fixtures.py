@@ -132,7 +132,7 @@ def main():
     index = {}
     for name, factory, leaves in circuits():
         circuit = factory()
-        key = circuit.topology_key()
+        key = circuit.topology_key().value  # (layout, groups): the reference's key shape
         st = ref._structure(key)
         rec = dict(size=int(st.size), n_nodes=int(st.n_nodes), nnz=int(st.nnz),
                    structure=digest(st.indptr, st.indices,

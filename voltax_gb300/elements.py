@@ -101,7 +101,8 @@ class Element:
     def with_nodes(self, nodes) -> "Element":
         new = object.__new__(type(self))
         new.__dict__.update(self.__dict__)
-        new.nodes = tuple(tuple(d) for d in nodes)
+        # the same node table keeps its identity (a circuit then keeps its topology key)
+        new.nodes = self.nodes if nodes is self.nodes else tuple(tuple(d) for d in nodes)
         return new
 
     @staticmethod

@@ -278,8 +278,7 @@ def engine_for(st: Structure, circuit=None, plan: Plan | None = None) -> Engine:
     """The cached `Engine` of a structure and plan (default ``st.plan``),
     with the device tables of `circuit` when stamping is needed."""
     plan = st.plan if plan is None else plan
-    segs = None if circuit is None else circuit.node_segment
-    key = (id(st), id(plan), _kinds(circuit), None if segs is None else hash(segs))
+    key = (id(st), id(plan), _kinds(circuit), None if circuit is None else circuit.segment_hash())
     eng = _ENGINES.get(key)
     if eng is None or eng.st is not st or eng.plan is not plan:
         if circuit is None:  # linear algebra only: reuse any engine of this plan

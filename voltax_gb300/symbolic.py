@@ -105,8 +105,8 @@ def structure(circuit, leaf: int | None = None) -> Structure:
 
 
 @functools.lru_cache(maxsize=512)
-def _structure(key: tuple, leaf: int) -> Structure:
-    layout, groups = key
+def _structure(key, leaf: int) -> Structure:
+    layout, groups = key.value
     return build_structure(layout.size, layout.n_nodes,
                            {g: (n, k, off) for g, n, k, off in layout.groups},
                            groups, leaf)
