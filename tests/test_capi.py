@@ -41,3 +41,30 @@ def test_no_cpu_fallback_without_gpu(lib):
     from voltax_gb300 import _lib, workloads
     with pytest.raises(_lib.VxgError, match="CUDA GPU"):
         vx.dc(workloads.power_grid(4))
+
+
+def _zero(argtype):
+    import ctypes as C
+    if argtype in (C.c_double, C.c_float):
+        return 0.0
+    if isinstance(argtype, type) and issubclass(argtype, (C.c_int32, C.c_int64, C.c_uint64,
+                                                          C.c_size_t)):
+        return 0
+    return None  # every pointer, handle and struct pointer
+
+
+def test_every_entry_point_rejects_null_arguments(lib):
+    """The boundary's error behaviour: each entry point checks its handle,
+    sizes and buffers before anything reaches CUDA, so null / zero
+    arguments return VXG_ERR_INVALID (no crash, no device call)."""
+    from voltax_gb300 import _lib
+    skip = {"vxg_last_error", "vxg_launch_count"}  # no status to return
+    checked = 0
+    for name, (argtypes, restype) in _lib.SIGNATURES.items():
+        if name in skip:
+            continue
+        fn = getattr(lib, name)
+        rc = fn(*[_zero(t) for t in argtypes])
+        assert rc == _lib.VXG_ERR_INVALID, (name, rc)
+        checked += 1
+    assert checked == len(declared_functions()) - len(skip)
