@@ -163,6 +163,9 @@ constexpr long long kLongSum = 32;
 
 // Build the 16-bit table blob of the fused kernel; false if a value does not fit.
 static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& out, Blob& b) {
+  // indptr[S] = nnz is one of the blob's values: a pattern this large can
+  // never fit, so skip walking (and allocating for) every table
+  if (d->nnz >= 0xFFFF) return false;
   bool ok = true;
   auto push = [&](int sec, const auto* src, long long n, bool nodes = false) {
     b.off[sec] = (int)out.size();
