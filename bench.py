@@ -323,7 +323,7 @@ def run_reference(a):
     sample = (f"{cores} threads x {per_thread} whole instances "
               f"({len(ts) * per_system} solves each) per step; compiled C restatement "
               "oracle/cvx.c")
-    if per_system < a.instances:
+    if w.name == "grids" and per_system < a.instances:
         sample += f"; each instance is the first {per_system} of the {a.instances} grids"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,

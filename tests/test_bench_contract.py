@@ -1,0 +1,39 @@
+"""bench.py's reference arm (the compiled C restatement on the host cores)
+prints one JSON line with the contract's keys; it needs no GPU."""
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def run_reference(*args):
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "1", *args],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    return json.loads(lines[0])
+
+
+@pytest.mark.parametrize("args", [(), ("--workload", "grids", "--instances", "40")],
+                         ids=["adder_mc", "grids"])
+def test_reference_arm_prints_the_contract_line(args):
+    line = run_reference(*args)
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"],
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    base = line["cpu_baseline"]
+    assert base["value"] == line["value"] and base["kind"] == "port" and base["cores"] >= 1
+    if args:
+        assert "first 32 of the 40 grids" in base["sample"]
+    else:
+        assert "grids" not in base["sample"]
