@@ -37,3 +37,22 @@ def test_reference_arm_prints_the_contract_line(args):
         assert "first 32 of the 40 grids" in base["sample"]
     else:
         assert "grids" not in base["sample"]
+
+
+@pytest.mark.parametrize("name,instances", [("adder_mc", 8), ("grid100", 1), ("grids", 40)])
+def test_cpu_legs_report_a_bounded_sample(name, instances):
+    sys.path.insert(0, str(ROOT))
+    import bench
+    w = bench.WORKLOADS[name]
+    n_t = 5 if w.analysis == "transient" else 1
+    base = bench.cpu_baseline(w, n_t, instances, min_seconds=0.2)
+    assert base["kind"] == "port" and base["cores"] == 1 and base["value"] > 0
+    assert ("first 32 of the 40 grids" in base["sample"]) == (name == "grids")
+    lu = bench.cpu_superlu(w, instances, min_seconds=0.2)
+    if w.analysis == "dc":
+        assert lu["kind"] == "superlu" and lu["value"] > 0
+        grids = min(instances, bench.CPU_GRIDS) if name == "grids" else 1
+        unknowns = int(lu["sample"].split("of the ")[1].split("-unknown")[0])
+        assert (unknowns > 200_000) == (grids > 1)
+    else:
+        assert lu is None
