@@ -56,3 +56,17 @@ def test_cpu_legs_report_a_bounded_sample(name, instances):
         assert (unknowns > 200_000) == (grids > 1)
     else:
         assert lu is None
+
+
+def test_clock_summary_reads_throttle_reasons():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    clk = bench.Clocks()
+    assert clk.summary()["reasons"] == ["unsampled"]
+    row = "0, {sm}, 2070, 900.0, 0x0, Not Active, {hw}, Not Active, {pc}"
+    for sm, hw, pc in [(1965, "Not Active", "Active"), (2070, "Not Active", "Not Active"),
+                       (1980, "Active", "Not Active")]:
+        clk.rows.append([x.strip() for x in row.format(sm=sm, hw=hw, pc=pc).split(",")])
+    s = clk.summary()
+    assert s["sm_mhz"] == 1980 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
+    assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
