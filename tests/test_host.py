@@ -84,3 +84,32 @@ def test_parameter_rows_are_finite_and_differentiable(make):
         if total.requires_grad:
             total.backward()
             assert x.grad is not None
+
+
+def test_ac_solution_accessors():
+    """voltax/analysis.py:142-172 on synthetic phasors: node and device
+    lookups, 20 log10 |v| and the unwrapped phase in degrees."""
+    import voltax_gb300 as vx
+    from voltax_gb300.analysis import ACSolution
+    b = CircuitBuilder()
+    b.vsource("in", "0", 0.0, ac=1.0, name="Vin")
+    b.resistor("in", "out", 1e3, name="R1")
+    b.capacitor("out", "0", 1e-9, name="C1")
+    c = b.build()
+    F = 64
+    f = np.logspace(1, 8, F)
+    ang = np.linspace(0.0, -3.5 * np.pi, F)  # wraps past -pi twice
+    mag = np.logspace(0, -3, F)
+    z = np.zeros((F, c.size), complex)
+    out = c.layout.node("out")
+    z[:, out] = mag * np.exp(1j * ang)
+    z[:, c.layout.internal("Vin")] = 2.0 - 1.0j
+    s = ACSolution(torch.as_tensor(f), torch.as_tensor(z), None, c.layout)
+    np.testing.assert_allclose(s.db("out").numpy(), 20 * np.log10(mag), rtol=1e-12)
+    np.testing.assert_allclose(s.phase("out").numpy(), np.rad2deg(ang), atol=1e-9)
+    wrapped = np.rad2deg(np.angle(np.exp(1j * ang)))
+    np.testing.assert_allclose(s.phase("out", unwrap=False).numpy(), wrapped, atol=1e-9)
+    assert torch.equal(s.v("0"), torch.zeros(F, dtype=torch.complex128))
+    assert s.v().shape == (F, c.n_nodes)
+    assert torch.all(s.i("Vin") == torch.tensor(2.0 - 1.0j))
+    assert isinstance(vx.ac, type(vx.dc))
