@@ -113,3 +113,31 @@ def test_ac_solution_accessors():
     assert s.v().shape == (F, c.n_nodes)
     assert torch.all(s.i("Vin") == torch.tensor(2.0 - 1.0j))
     assert isinstance(vx.ac, type(vx.dc))
+
+
+def test_solution_accessors_and_check():
+    """voltax/analysis.py:92-139: lookups by node / device name, and check()
+    raising voltax's RuntimeError (with the first failing time) on
+    non-convergence or non-finite states."""
+    from voltax_gb300.analysis import Solution
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.resistor("in", "out", 1e3, name="R1")
+    b.resistor("out", "0", 1e3, name="R2")
+    c = b.build()
+    T = 4
+    z = torch.arange(T * c.size, dtype=torch.float64).reshape(T, c.size)
+    ok = torch.ones(T, dtype=torch.int32)
+    s = Solution(torch.linspace(0, 3e-9, T, dtype=torch.float64), z, ok, c.layout)
+    assert s.check() is s
+    assert torch.equal(s["out"], z[:, c.layout.node("out")])
+    assert torch.equal(s["Vin.i"], z[:, c.layout.internal("Vin", "i")])
+    assert torch.equal(s.v("gnd"), torch.zeros(T, dtype=torch.float64))
+    bad = ok.clone()
+    bad[2] = 0
+    with pytest.raises(RuntimeError, match=r"did not converge at t=2e-09"):
+        Solution(s.t, z, bad, c.layout).check()
+    z2 = z.clone()
+    z2[1, 0] = float("nan")
+    with pytest.raises(RuntimeError, match="did not converge"):
+        Solution(s.t, z2, ok, c.layout).check()
