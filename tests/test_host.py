@@ -141,3 +141,22 @@ def test_solution_accessors_and_check():
     z2[1, 0] = float("nan")
     with pytest.raises(RuntimeError, match="did not converge"):
         Solution(s.t, z2, ok, c.layout).check()
+
+
+def test_layout_state_names_and_group_internals():
+    """voltax/circuit.py:92-107: labels of every state entry and the internal
+    indices of a group."""
+    b = CircuitBuilder()
+    b.vsource("in", "0", 1.0, name="Vin")
+    b.inductor("in", "mid", 1e-6, name="L1")
+    b.inductor("mid", "out", 2e-6, name="L2")
+    b.resistor("out", "0", 50.0, name="R1")
+    c = b.build()
+    names = c.layout.state_names()
+    assert len(names) == c.size
+    assert names[:c.n_nodes] == [f"v({n})" for n in c.layout.node_names]
+    for dev in ("Vin", "L1", "L2"):
+        assert names[c.layout.internal(dev)] == f"i({dev})"
+    idx = c.layout.group_internals("Inductor")
+    assert idx.shape == (2, 1)
+    assert [int(i) for i in idx[:, 0]] == [c.layout.internal("L1"), c.layout.internal("L2")]
