@@ -157,3 +157,15 @@ def test_take_moves_fields_out_of_the_plan():
         assert a.min() >= 0
     finally:
         lib.vxs_plan_destroy(h)
+
+
+def test_plan_is_identical_for_any_thread_count(monkeypatch):
+    st = symbolic.structure(workloads.power_grid_batch([15, 22, 9, 30]), 8)
+    runs = []
+    for threads in ("1", "3", "16"):
+        monkeypatch.setenv("VXS_THREADS", threads)
+        runs.append(symbolic.native_fields(st, 8))
+    for other in runs[1:]:
+        assert runs[0].keys() == other.keys()
+        for k in runs[0]:
+            assert np.array_equal(runs[0][k], other[k]), k
