@@ -102,14 +102,14 @@ class Element:
         new = object.__new__(type(self))
         new.__dict__.update(self.__dict__)
         # the same node table keeps its identity (a circuit then keeps its topology key)
-        new.nodes = self.nodes if nodes is self.nodes else tuple(tuple(d) for d in nodes)
+        new.nodes = self.nodes if nodes is self.nodes else tuple(map(tuple, nodes))
         return new
 
     @staticmethod
     def _devices(nodes) -> tuple[tuple[Any, ...], ...]:
         if _is_single(nodes):
             return (tuple(nodes),)
-        return tuple(tuple(d) for d in nodes)
+        return tuple(map(tuple, nodes))
 
     def _per_device(self, value) -> torch.Tensor:
         value = _t(value)
