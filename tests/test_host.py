@@ -160,3 +160,36 @@ def test_layout_state_names_and_group_internals():
     idx = c.layout.group_internals("Inductor")
     assert idx.shape == (2, 1)
     assert [int(i) for i in idx[:, 0]] == [c.layout.internal("L1"), c.layout.internal("L2")]
+
+
+def test_time_grid_properties():
+    """voltax/analysis.py:575-620 on the host: every waveform corner is a
+    grid point, each interval holds at least `ramp_points` steps, steps never
+    exceed `dt_max`, and steps grow by at most `growth` after a corner."""
+    import voltax_gb300 as vx
+    from voltax_gb300.signals import Pulse, Step
+    b = CircuitBuilder()
+    b.vsource("in", "0", Pulse(0.0, 1.0, delay=1e-9, rise=1e-10, fall=2e-10, width=2e-9,
+                               period=5e-9), name="V1")
+    b.isource("x", "0", Step(0.0, 1e-3, delay=2.5e-9, rise=5e-11), name="I1")
+    b.resistor("in", "x", 1e3, name="R1")
+    b.capacitor("x", "0", 1e-12, name="C1")
+    c = b.build()
+    t_stop, dt_max, ramp, growth = 12e-9, 0.5e-9, 10, 1.2
+    grid = vx.time_grid(c, t_stop, dt_max=dt_max, ramp_points=ramp, growth=growth)
+    corners = np.unique(np.concatenate(
+        [[0.0, t_stop], c.elements["VoltageSource_Pulse"].value.breakpoints(t_stop),
+         c.elements["CurrentSource_Step"].value.breakpoints(t_stop)]))
+    assert grid[0] == 0.0 and grid[-1] == t_stop and np.all(np.diff(grid) > 0)
+    for t in corners:
+        assert np.min(np.abs(grid - t)) <= 1e-9 * 1e-12
+    steps = np.diff(grid)
+    assert steps.max() <= dt_max * (1 + 1e-12)
+    for a, z in zip(corners[:-1], corners[1:]):
+        inside = (grid > a) & (grid <= z)
+        assert inside.sum() >= ramp
+        s = np.diff(np.concatenate([[a], grid[inside]]))
+        assert np.all(s[1:-1] <= s[:-2] * growth * (1 + 1e-12))
+    # a pulse corner every period: 1, 1.1, 3.1, 3.3 ns and again 5 ns later
+    for t in (1e-9, 1.1e-9, 3.1e-9, 3.3e-9, 6e-9, 6.1e-9, 8.1e-9, 8.3e-9, 2.5e-9, 2.55e-9):
+        assert np.min(np.abs(grid - t)) < 1e-18
