@@ -587,8 +587,29 @@ def native_fields(st: Structure, leaf: int) -> dict[str, np.ndarray]:
         lib.vxs_plan_destroy(h)
 
 
-def _split(ptr: np.ndarray, idx: np.ndarray) -> list[np.ndarray]:
-    return np.split(idx, ptr[1:-1]) if len(ptr) > 1 else []
+class _Split(Sequence):
+    """The rows of a CSR pair (``ptr``, ``idx``) as array views, made on
+    access: a plan's supernode and border lists without one small array per
+    supernode (the device upload reads the flat arrays)."""
+
+    def __init__(self, ptr: np.ndarray, idx: np.ndarray):
+        self._ptr, self._idx = ptr, idx
+
+    def __len__(self) -> int:
+        return max(len(self._ptr) - 1, 0)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[j] for j in range(*i.indices(len(self)))]
+        if i < 0:
+            i += len(self)
+        if not 0 <= i < len(self):
+            raise IndexError(i)
+        return self._idx[self._ptr[i]:self._ptr[i + 1]]
+
+
+def _split(ptr: np.ndarray, idx: np.ndarray) -> _Split:
+    return _Split(ptr, idx)
 
 
 class _Levels(Sequence):
