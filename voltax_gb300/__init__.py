@@ -15,6 +15,6 @@ from .circuit import Circuit, Layout  # noqa: F401
 from .elements import (VT_300K, Capacitor, Conductance, CurrentSource,  # noqa: F401
                        BJT, CCCS, CCVS, VCCS, VCVS, Diode, IdealOpAmp, OpAmp, Switch,
                        Transformer, EKVMOSFET, Element, Inductor, Level1MOSFET,
-                       MOSProcess, Resistor, VoltageSource)
+                       MOSProcess, Resistor, VoltageSource, concatenate)
 
 __version__ = "0.1.0"
