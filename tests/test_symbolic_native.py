@@ -169,3 +169,18 @@ def test_plan_is_identical_for_any_thread_count(monkeypatch):
         assert runs[0].keys() == other.keys()
         for k in runs[0]:
             assert np.array_equal(runs[0][k], other[k]), k
+
+
+@pytest.mark.parametrize("indptr,indices,why", [
+    ([1, 1, 2], [0, 1], "indptr[0]"),
+    ([0, 2, 1], [0, 1], "non-decreasing"),
+    ([0, 1, 2], [0, 7], "column index"),
+])
+def test_malformed_pattern_is_rejected(indptr, indices, why):
+    lib = symbolic._symlib()
+    ip = np.array(indptr, np.int64)
+    ix = np.array(indices, np.int64)
+    h = C.c_void_p()
+    rc = lib.vxs_plan_create(2, ip.ctypes.data, ix.ctypes.data, 0, None, None, 16, C.byref(h))
+    assert rc == 1 and h.value is None
+    assert why in lib.vxs_last_error().decode()
