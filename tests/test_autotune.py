@@ -4,7 +4,6 @@ caller owns, and a tuned analysis agrees with every pinned engine/width."""
 
 import numpy as np
 import pytest
-import torch
 
 pytestmark = pytest.mark.gpu
 
