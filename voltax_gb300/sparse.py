@@ -17,7 +17,6 @@ instances that share the pattern. Everything runs in the CUDA kernels of
 
 from __future__ import annotations
 
-
 import numpy as np
 import torch
 
