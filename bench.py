@@ -360,6 +360,67 @@ def h2d_bytes(c):
                          (el.value.params() if hasattr(el, "value") else [])))
 
 
+def oracle_check(w, circuit, z, ts, ic, count=16):
+    """Acceptance of the GPU's chosen-form results on a sample of instances
+    against the compiled FP64 oracle (oracle/cvx.c): the oracle solves each
+    sampled instance itself (largest node-voltage difference, relative with a
+    1 mV floor), and evaluates the FP64 residual r(z*) at the GPU's solution
+    (largest KCL residual) and one more Newton step from it (largest
+    |dz| / (atol + rtol |z*|); <= 1 passes voltax's convergence test).
+    `z`: (B, n_t, S) or (B, S) numpy trajectories of the GPU run."""
+    from oracle import cbase
+    from voltax_gb300 import symbolic
+    st = symbolic.structure(circuit)
+    B = circuit.batch
+    pick = sorted(set(np.linspace(0, B - 1, min(count, B)).round().astype(int).tolist()))
+    z0 = None if isinstance(ic, str) else ic.numpy()
+    method = w.method or "dc"
+    nv = circuit.n_nodes
+    worst = {"rel": 0.0, "kcl": 0.0, "ratio": 0.0}
+    t0 = time.perf_counter()
+    for b in pick:
+        cs = cbase.CSystem(circuit, st, st.plan, b)
+        zb = z[b].reshape(len(ts), circuit.size)
+        if w.analysis == "dc":
+            zr, okr, _ = cs.run(ts[:1], dc_first=True)
+        else:
+            zr, okr, _ = cs.run(ts, z0=z0, method=method, dc_first=z0 is None)
+        a, r = zb[:, :nv], zr[:, :nv]
+        worst["rel"] = max(worst["rel"], float(np.max(np.abs(a - r) / np.maximum(np.abs(r),
+                                                                                 1e-3))))
+        kcl, ratio = cs.check(ts[: len(zb)], zb, method=method if w.analysis != "dc" else "dc",
+                              dc_first=z0 is None)
+        worst["kcl"] = max(worst["kcl"], float(np.max(kcl)))
+        worst["ratio"] = max(worst["ratio"], float(np.max(ratio)))
+    return {"instances": len(pick), "time_points": len(ts),
+            "max_rel_node_v": worst["rel"], "max_kcl_residual_a": worst["kcl"],
+            "max_newton_step_ratio": worst["ratio"],
+            "pass": bool(worst["rel"] <= 1e-9 and worst["ratio"] <= 1.0),
+            "oracle": "oracle/cvx.c, FP64, 1 thread", "seconds": time.perf_counter() - t0}
+
+
+def fused_phases(lib, torch, dev, run, total_iters):
+    """Per-phase SM cycles of the fused kernel over one profiled run
+    (vxg_fused_set_profile): shares of the kernel time and CTA cycles per
+    Newton iteration."""
+    cyc = torch.zeros(8, dtype=torch.int64, device=dev)
+    lib.vxg_fused_set_profile(cyc.data_ptr())
+    try:
+        run()
+        torch.cuda.synchronize()
+    finally:
+        lib.vxg_fused_set_profile(None)
+    c = cyc.cpu().numpy().astype(float)
+    names = ["eval", "assemble", "factor", "solve", "update"]
+    total = c[5]
+    out = {n: {"share": c[i] / total, "cycles_per_newton_iter": c[i] / total_iters}
+           for i, n in enumerate(names)}
+    rest = total - c[:5].sum()
+    out["other"] = {"share": rest / total, "cycles_per_newton_iter": rest / total_iters}
+    out["kernel_cta_cycles"] = total
+    return out
+
+
 # ----------------------------------------------------------------- GPU arm
 def main():
     a = parse()
@@ -463,6 +524,13 @@ def main():
         s32.iterations.reshape(-1, 1).float()
     iters = float(it[:, 1:].mean()) if w.analysis == "transient" else float(it.mean())
     total_iters = int(it.sum())  # Newton iterations of one step, all instances
+    phases = None
+    if engine_used == "fused":
+        phases = {"chosen": fused_phases(lib, torch, dev, lambda: step(dev_circuit, opts32),
+                                         total_iters)}
+        it64 = s64.iterations.reshape(-1).double().sum()
+        phases["plain_fp64"] = fused_phases(lib, torch, dev, lambda: step(dev_circuit, opts64),
+                                            float(it64))
 
     # roofline of the dominant kernel. Algorithmic bytes per Newton iteration
     # and instance: 8 nnz (stamp write) + 4 (nnz + 2 factor_entries) (panel
@@ -508,6 +576,10 @@ def main():
 
     if rank != 0:
         return
+    zs = s32.z.cpu().numpy()
+    if zs.ndim == 1 or (w.analysis == "transient" and zs.ndim == 2):
+        zs = zs[None]
+    ocheck = oracle_check(w, circuit, zs, ts, ic)
     # voltax publishes this one workload: 499 us per step on one CPU thread
     # (benchmarks/README.md:217), i.e. 2004 Newton solves/s
     vs_baseline = value / (1.0 / 499e-6) if w.name == "ring101_l1" else None
@@ -525,6 +597,7 @@ def main():
         "plain_fp64": {"value": value64, "unit": UNIT, "speedup": value / value64},
         "match": {"max_abs_node_v_diff_vs_fp64": match, "converged": conv,
                   "mean_newton_iters": iters},
+        "oracle_check": ocheck,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(out_host.numel() * 8)},
         "gpu_launches": int(launches),
@@ -534,6 +607,8 @@ def main():
     }
     if superlu:
         line["cpu_superlu"] = superlu
+    if phases:
+        line["phases"] = phases
     print(json.dumps(line))
 
 

@@ -285,6 +285,16 @@ int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
                   int32_t direct_steps, double gmin, const vxg_newton_opts* opts,
                   double* z_out, int32_t* converged, int32_t* iters, void* stream);
 
+/* Phase timing of the fused kernel (a diagnostic; no counterpart in the
+ * reference). With `cycles` != NULL (device, 8 int64, zeroed by the
+ * caller), every later vxg_fused_run of the calling thread adds, summed
+ * over its CTAs, the SM clock cycles spent in device evaluation [0],
+ * assembly of the CSR values, panels and right-hand side [1],
+ * factorization [2], solves and refinement [3], the damped update and
+ * convergence test [4], and the whole kernel [5] (the rest: state
+ * writes, trapezoidal f(z_prev), instance changes). NULL switches it off. */
+int vxg_fused_set_profile(int64_t* cycles);
+
 /* vxg_factor for callers that cannot allocate device memory when they
  * refactor (allocation-free plugin or custom-call hooks, real-time loops,
  * hosts whose allocator is owned by another runtime). No counterpart in

@@ -59,6 +59,9 @@ def lib():
         _lib.cvx_run.argtypes = [C.POINTER(Sys), C.POINTER(Opts), C.c_int, C.c_int, C.c_void_p,
                                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.cvx_run.restype = C.c_int
+        _lib.cvx_check.argtypes = [C.POINTER(Sys), C.POINTER(Opts), C.c_int, C.c_int,
+                                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.cvx_check.restype = C.c_int
     return _lib
 
 
@@ -251,3 +254,23 @@ class CSystem:
         if rc:
             raise MemoryError("cvx_run could not allocate its workspace")
         return z_out, conv.astype(bool), iters
+
+    def check(self, ts, z_traj, method="be", dc_first=True, rtol=1e-6, atol=1e-9,
+              gmin=1e-12):
+        """Acceptance of a trajectory computed elsewhere: per time point the
+        largest FP64 residual entry |r(z_n)| (the KCL residual, in A on node
+        rows) and the largest |dz_i| / (atol + rtol |z_i|) of one more
+        Newton step from z_n (<= 1: voltax's convergence test passes,
+        voltax/analysis.py:224-229). Point 0 is checked as a DC solve when
+        `dc_first`, else skipped (an initial condition)."""
+        ts = np.ascontiguousarray(np.atleast_1d(np.asarray(ts, np.float64)))
+        z = np.ascontiguousarray(np.asarray(z_traj, np.float64).reshape(len(ts), self.S))
+        o = Opts(100, rtol, atol, 1.0, gmin, 0, 0, None)
+        kcl = np.zeros(len(ts))
+        ratio = np.zeros(len(ts))
+        mode = {"dc": 0, "be": 1, "trap": 2}[method]
+        rc = lib().cvx_check(C.byref(self.sys), C.byref(o), mode, len(ts), ts.ctypes.data,
+                             z.ctypes.data, int(dc_first), kcl.ctypes.data, ratio.ctypes.data)
+        if rc:
+            raise MemoryError("cvx_check could not allocate its workspace")
+        return kcl, ratio

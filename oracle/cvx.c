@@ -625,3 +625,78 @@ int cvx_run(const cvx_sys* s, const cvx_opts* o, int mode, int n_t, const double
   free(w.tmp); free(w.perm); free(z);
   return 0;
 }
+
+/* ---------------------------------------------------- acceptance check
+ * KCL residual and Newton-step test of a trajectory computed elsewhere
+ * (the GPU): for each time point n, the residual r of `mode` at z_n
+ * (voltax/analysis.py:333-378; point 0 is the DC residual f + gmin v when
+ * dc_first, else it is skipped), evaluated with z_{n-1} as the previous
+ * state, and one Newton step dz = -J(z_n)^-1 r. Writes
+ *   kcl[n]   = max_i |r_i|                       (A for KCL rows)
+ *   ratio[n] = max_i |dz_i| / (atol + rtol |z_n,i|)
+ * so ratio <= 1 means z_n passes voltax's own convergence test
+ * (voltax/analysis.py:224-229) once more, at the oracle's FP64 residual. */
+int cvx_check(const cvx_sys* s, const cvx_opts* o, int mode, int n_t, const double* ts,
+              const double* z_traj, int dc_first, double* kcl, double* ratio) {
+  const int S = s->S;
+  int maxk = 1;
+  for (int j = 0; j < s->n_sn; ++j) {
+    if (s->k[j] > maxk) maxk = s->k[j];
+    if (s->r[j] > maxk) maxk = s->r[j];
+  }
+  ws_t w;
+  w.f = calloc(S, sizeof(double));
+  w.q = calloc(S, sizeof(double));
+  w.fp = calloc(S, sizeof(double));
+  w.qp = calloc(S, sizeof(double));
+  w.dz = calloc(S, sizeof(double));
+  w.data = calloc(s->nnz + 1, sizeof(double));
+  w.work = calloc(s->work > 0 ? s->work : 1, sizeof(double));
+  w.tmp = calloc(maxk + S, sizeof(double));
+  w.perm = calloc(maxk, sizeof(int));
+  if (!w.f || !w.q || !w.fp || !w.qp || !w.dz || !w.data || !w.work || !w.tmp || !w.perm)
+    return 1;
+  for (int n = 0; n < n_t; ++n) {
+    const double* z = z_traj + (long long)n * S;
+    kcl[n] = 0.0;
+    ratio[n] = 0.0;
+    int md = mode;
+    double t = ts[n], tp = 0.0;
+    if (n == 0) {
+      if (!dc_first) continue;
+      md = M_DC;
+    } else {
+      tp = ts[n - 1];
+      stamp(s, z - S, tp, 1.0, 0.0, 0.0, mode == M_TRAP ? w.fp : 0, w.qp, 0);
+    }
+    const double cf = md == M_TRAP ? 0.5 : 1.0;
+    const double cq = md == M_DC ? 0.0 : 1.0 / (t - tp);
+    const double h = t - tp;
+    stamp(s, z, t, cf, cq, o->gmin, w.f, md == M_DC ? 0 : w.q, w.data);
+    double rmax = 0.0;
+    int bad = 0;
+    for (int i = 0; i < S; ++i) {
+      const double gm = i < s->nv ? o->gmin * z[i] : 0.0;
+      double r;
+      if (md == M_DC) r = w.f[i] + gm;
+      else if (md == M_BE) r = (w.q[i] - w.qp[i]) / h + w.f[i] + gm;
+      else r = (w.q[i] - w.qp[i]) / h + 0.5 * (w.f[i] + w.fp[i]) + gm;
+      if (isnan(r)) bad = 1;
+      else if (fabs(r) > rmax) rmax = fabs(r);
+      w.dz[i] = -r;
+    }
+    factor(s, w.data, w.work, w.perm, w.tmp);
+    solve(s, w.work, w.dz, w.tmp);
+    double worst = 0.0;
+    for (int i = 0; i < S; ++i) {
+      const double q = fabs(w.dz[i]) / (o->atol + o->rtol * fabs(z[i]));
+      if (isnan(q)) bad = 1;
+      else if (q > worst) worst = q;
+    }
+    kcl[n] = bad ? NAN : rmax;
+    ratio[n] = bad ? NAN : worst;
+  }
+  free(w.f); free(w.q); free(w.fp); free(w.qp); free(w.dz); free(w.data); free(w.work);
+  free(w.tmp); free(w.perm);
+  return 0;
+}

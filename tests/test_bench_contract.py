@@ -70,3 +70,31 @@ def test_clock_summary_reads_throttle_reasons():
     s = clk.summary()
     assert s["sm_mhz"] == 1980 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
     assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+
+
+@pytest.mark.parametrize("name", ["adder_mc", "ring101", "grid100"])
+def test_oracle_check_accepts_oracle_results_and_rejects_a_planted_error(name):
+    """bench.py's oracle_check on CPU: trajectories the oracle produced
+    itself pass; the same trajectories with one node voltage moved by 10 uV
+    at one time point fail both the 1e-9 match and the Newton-step test."""
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+    import bench
+    from oracle import cbase
+    from voltax_gb300 import symbolic
+    w = bench.WORKLOADS[name]
+    c = w.circuit(3 if name == "adder_mc" else 1)
+    ts = w.times()[:51]  # the workload's own time step, first 50 steps
+    ic = w.ic(c)
+    z0 = None if isinstance(ic, str) else ic.numpy()
+    st = symbolic.structure(c)
+    z = np.stack([cbase.CSystem(c, st, st.plan, b).run(
+        ts if w.analysis == "transient" else ts[:1], z0=z0, method=w.method or "be",
+        dc_first=z0 is None)[0] for b in range(c.batch)])
+    good = bench.oracle_check(w, c, z, ts, ic, count=3)
+    assert good["pass"] and good["max_rel_node_v"] == 0.0
+    assert good["max_newton_step_ratio"] <= 1.0 and good["instances"] == c.batch
+    bad = z.copy()
+    bad[0, -1, 1] += 1e-5
+    worse = bench.oracle_check(w, c, bad, ts, ic, count=3)
+    assert not worse["pass"] and worse["max_newton_step_ratio"] > 1.0

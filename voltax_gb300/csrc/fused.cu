@@ -38,9 +38,17 @@ static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
   return VXG_ERR_TOO_LARGE;
 }
 
+// Phase-timing target of this thread's vxg_fused_run calls (null: off).
+static thread_local long long* t_phase_clk = nullptr;
+
 }  // namespace vxg
 
 using namespace vxg;
+
+extern "C" int vxg_fused_set_profile(int64_t* cycles) {
+  t_phase_clk = reinterpret_cast<long long*>(cycles);
+  return VXG_OK;
+}
 
 extern "C" int vxg_fused_smem(const vxg_handle* h, int32_t precision, size_t* bytes) {
   if (!h || !bytes || (precision != VXG_F64 && precision != VXG_F32)) return VXG_ERR_INVALID;
@@ -123,6 +131,7 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   a.z_out = z_out;
   a.conv = converged;
   a.iters = iters;
+  a.phase_clk = t_phase_clk;
   cudaStream_t s = (cudaStream_t)stream;
   int dev = 0, sms = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));

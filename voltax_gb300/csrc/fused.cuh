@@ -60,7 +60,13 @@ struct FusedArgs {
   double* z_out;
   int* conv;
   int* iters;
+  // phase timing (a diagnostic, normally null): SM clock cycles of each CTA
+  // per phase, summed over CTAs -- eval, assemble, factor, solve, update,
+  // and the whole kernel -- see vxg_fused_set_profile
+  long long* phase_clk;
 };
+
+enum { PH_EVAL = 0, PH_ASSEMBLE, PH_FACTOR, PH_SOLVE, PH_UPDATE, PH_TOTAL, PH_COUNT = 8 };
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline int sbuf_values(int nw) { return 64 * nw > 2 * kCtaK ? 64 * nw : 2 * kCtaK; }
@@ -68,7 +74,8 @@ __host__ __device__ inline int sbuf_records(int nw) { return 32 * nw > kCtaK ? 3
 
 // Shared-memory layout of one instance.
 struct FusedLayout {
-  size_t blob, z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, sbuf, total;
+  size_t blob, z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, prof, sbuf,
+      total;
 };
 
 template <typename T>
@@ -111,6 +118,7 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.xt = take(sizeof(T) * S);
   if (o < contrib_end) o = contrib_end;
   L.red = take(64 * sizeof(double));
+  L.prof = take(PH_COUNT * sizeof(long long));
   // per-warp column/row buffers (64 values) and pivot records (32) of nw
   // warps, or the whole CTA's (2 kCtaK values, kCtaK records)
   L.sbuf = take(sizeof(T) * sbuf_values(nw) + sizeof(int) * sbuf_records(nw));
@@ -520,7 +528,18 @@ struct Instance {
   double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *cf, *cq, *red;
   T *data, *cj, *work, *scr, *xt, *sbuf;
   int* ibuf;
+  long long* prof;  // per-CTA phase cycles (shared memory), used when A.phase_clk
   const u16* tb;  // shared-memory tables
+
+  // Thread 0 adds the cycles since *t0 to phase p; every phase ends with a
+  // CTA barrier, so thread 0's clock at its end is the CTA's.
+  __device__ __forceinline__ void mark(int p, long long* t0) const {
+    if (A.phase_clk && threadIdx.x == 0) {
+      const long long t = clock64();
+      prof[p] += t - *t0;
+      *t0 = t;
+    }
+  }
 
   // a staged table section (shared memory; the Schur gather sections may
   // instead stay in global memory, see apply_schur)
@@ -941,13 +960,19 @@ struct Instance {
     const double cqc = dc ? 0.0 : 1.0 / (t - t_prev);
     const double h = t - t_prev;
     int done = 0, it = 0;
+    long long t0 = A.phase_clk ? clock64() : 0;
     while (it < max_steps && !done) {
       eval(z, t, cfc, cqc, true, !dc, true);
       __syncthreads();
+      mark(PH_EVAL, &t0);
       assemble_system(mode, gmin, h, it == 0);
+      mark(PH_ASSEMBLE, &t0);
       factor();
+      mark(PH_FACTOR, &t0);
       solve(sizeof(T) == sizeof(float) ? A.refine : 0);
+      mark(PH_SOLVE, &t0);
       done = update();
+      mark(PH_UPDATE, &t0);
       ++it;
     }
     *iters_out = it;
@@ -992,6 +1017,9 @@ __global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
   I.scr = reinterpret_cast<T*>(smem + L.scr);
   I.xt = reinterpret_cast<T*>(smem + L.xt);
   I.red = reinterpret_cast<double*>(smem + L.red);
+  I.prof = reinterpret_cast<long long*>(smem + L.prof);
+  const long long k_start = clock64();
+  if (A.phase_clk && threadIdx.x < PH_COUNT) I.prof[threadIdx.x] = 0;
   I.sbuf = reinterpret_cast<T*>(smem + L.sbuf);
   I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * sbuf_values(NT / 32));
   const long long BS = (long long)A.B * A.S;
@@ -1036,6 +1064,12 @@ __global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
       }
     }
     __syncthreads();
+  }
+  if (A.phase_clk && threadIdx.x == 0) {
+    I.prof[PH_TOTAL] = clock64() - k_start;
+    for (int p = 0; p < PH_COUNT; ++p)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.phase_clk + p),
+                (unsigned long long)I.prof[p]);
   }
 }
 
