@@ -136,6 +136,9 @@ def parse():
     ap.add_argument("--instances", type=int, default=None)
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
+    ap.add_argument("--block", type=int, default=0, choices=[0, 32, 128, 256, 512],
+                    help="fused kernel threads per instance (32: one warp per instance; "
+                         "0: the library's or the autotuner's choice)")
     ap.add_argument("--refine", type=int, default=None,
                     help="FP64 refinement sweeps per solve of the FP32-factor form "
                          "(default: the library's choice per engine)")
@@ -462,8 +465,8 @@ def main():
 
     dev_circuit = to_device(circuit, dev)
     host_circuit = to_device(circuit, None, pin=True)
-    opts32 = vx.Options(precision="f32", engine=a.engine, refine=a.refine)
-    opts64 = vx.Options(precision="f64", engine=a.engine)
+    opts32 = vx.Options(precision="f32", engine=a.engine, refine=a.refine, block=a.block)
+    opts64 = vx.Options(precision="f64", engine=a.engine, block=a.block)
     from voltax_gb300 import symbolic
     from voltax_gb300.analysis import _Call
     st = symbolic.structure(circuit)
@@ -591,6 +594,7 @@ def main():
         "config": {"workload": w.label(B, len(ts)), "instances": B,
                    "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,
+                   "block": _Call(dev_circuit, opts32).block if engine_used == "fused" else None,
                    "refine": _Call(dev_circuit, opts32).refine,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},

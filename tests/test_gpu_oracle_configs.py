@@ -15,7 +15,8 @@ checks every instance and every time point against the compiled oracle
 
 Workloads: the 101-stage EKV ring oscillator, trapezoidal, all 2001 points;
 the 4-bit mirror-adder Monte Carlo (8 instances of the 4096-instance draw)
-over all 501 backward-Euler points, both precisions and both engines; the
+over all 501 backward-Euler points, both precisions, on the generic engine
+and the fused kernel with one CTA or one warp per instance; the
 100 x 100 power grid DC; and the first four grids of the 512-grid uneven
 batch (sides 263, 209, 178, 117), solved as one segmented batch on the GPU
 and each alone by the oracle.
@@ -47,12 +48,15 @@ def accept(csys, ts, z, method, dc_first):
     return float(np.max(kcl)), float(np.max(ratio))
 
 
+@pytest.mark.parametrize("block", [0, 32], ids=["auto", "fused-warp"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_ring101_trapezoidal_2001_points_matches_oracle(precision):
+def test_ring101_trapezoidal_2001_points_matches_oracle(precision, block):
     ring, nodes = workloads.ring_oscillator(101)
     z0 = workloads.ring_initial_state(ring, nodes)
     ts = np.linspace(0.0, 2e-9, 2001)
-    sol = vx.transient(ring, ts, ic=z0, method="trap", options=vx.Options(precision=precision))
+    engine = "fused" if block else "auto"
+    sol = vx.transient(ring, ts, ic=z0, method="trap",
+                       options=vx.Options(precision=precision, engine=engine, block=block))
     z = sol.z.cpu().numpy()
     st = symbolic.structure(ring)
     cs = cbase.CSystem(ring, st, st.plan)
@@ -67,14 +71,15 @@ def test_ring101_trapezoidal_2001_points_matches_oracle(precision):
     assert kcl < 1e-9, f"ring101 KCL residual {kcl:.3e} A"
 
 
-@pytest.mark.parametrize("engine", ["fused", "generic"])
+@pytest.mark.parametrize("engine,block", [("fused", 128), ("fused", 32), ("generic", 0)],
+                         ids=["fused-cta", "fused-warp", "generic"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_mirror_adder_mc_501_points_matches_oracle(precision, engine):
+def test_mirror_adder_mc_501_points_matches_oracle(precision, engine, block):
     B = 8
     c = workloads.mirror_adder_mc(B, seed=0)
     ts = np.linspace(0.0, 1e-9, 501)
     sol = vx.transient(c, ts, ic="dc", method="be",
-                       options=vx.Options(precision=precision, engine=engine))
+                       options=vx.Options(precision=precision, engine=engine, block=block))
     z = sol.z.cpu().numpy()
     its = sol.iterations.cpu().numpy().reshape(B, len(ts))
     conv = sol.converged.cpu().numpy().reshape(B, len(ts))

@@ -193,3 +193,42 @@ def test_time_grid_properties():
     # a pulse corner every period: 1, 1.1, 3.1, 3.3 ns and again 5 ns later
     for t in (1e-9, 1.1e-9, 3.1e-9, 3.3e-9, 6e-9, 6.1e-9, 8.1e-9, 8.3e-9, 2.5e-9, 2.55e-9):
         assert np.min(np.abs(grid - t)) < 1e-18
+
+
+def test_builder_group_fusion_and_naming_rule():
+    """Group names the state layout depends on: explicit groups keep their
+    names; automatic groups take base, base_2, base_3, ... in order of their
+    first device, skipping names already in use; node indices follow first
+    appearance; devices of one explicit group must be fusable."""
+    import pytest
+    from voltax_gb300 import elements as el
+    from voltax_gb300.builder import CircuitBuilder
+    from voltax_gb300.signals import Step
+    other = el.MOSProcess.nmos(vth=0.3)  # a second process: a second nmos group
+    b = CircuitBuilder()
+    b.nmos("d1", "g", "0")                          # bucket A: EKVMOSFET_n
+    b.resistor("d1", "x", 1e3, group="EKVMOSFET_n_2")  # explicit, takes _2
+    b.nmos("d2", "g", "0", process=other)             # bucket B: _2 taken -> _3
+    b.vsource("g", "0", Step(0.0, 1.0, 1e-9, 1e-10))  # VoltageSource_Step
+    b.vsource("vdd", "0", 1.2)                        # VoltageSource
+    with b.scope("blk"):
+        inner = b.node("mid")
+        b.capacitor(inner, "0", 1e-15)
+    c = b.build()
+    names = sorted(c.elements)
+    assert type(c.elements["EKVMOSFET_n_2"]).__name__ == "Resistor"
+    assert c.layout.device("M1") == ("EKVMOSFET_n", 0)
+    assert c.layout.device("M2") == ("EKVMOSFET_n_3", 0)
+    assert "VoltageSource_Step" in names and "VoltageSource" in names
+    assert c.layout.node_names[:3] == ("d1", "g", "x")
+    assert inner == "blk.mid" and "blk.mid" in c.layout.node_names
+    assert c.devices("Capacitor") == ["blk.C1"]
+    with pytest.raises(ValueError, match="cannot be fused"):
+        b2 = CircuitBuilder()
+        b2.resistor("a", "0", 1.0, group="mix")
+        b2.capacitor("a", "0", 1e-12, group="mix")
+        b2.build()
+    with pytest.raises(ValueError, match="duplicate device name"):
+        b3 = CircuitBuilder()
+        b3.resistor("a", "0", 1.0, name="R")
+        b3.resistor("b", "0", 1.0, name="R")

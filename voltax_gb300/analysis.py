@@ -52,7 +52,10 @@ class Options:
     `engine` picks the fused persistent kernel or the generic level kernels;
     with ``"auto"`` and `autotune`, the faster one (and the fused kernel's
     CTA width) is timed per topology and batch size (`autotune.choose`).
-    `block` pins the fused kernel's threads per CTA (0: library choice)."""
+    `block` pins the fused kernel's threads per instance: 128, 256 or 512
+    (one CTA per instance), 32 (one warp per instance, several instances per
+    CTA; topologies whose supernodes are at most 32 wide), 0: library
+    choice."""
 
     max_steps: int = 100
     rtol: float = 1e-6
@@ -76,8 +79,8 @@ class Options:
         if self.solver not in ("auto", "dense", "sparse"):
             raise ValueError("solver must be 'auto', 'dense' or 'sparse', "
                              f"got {self.solver!r}")
-        if self.block not in (0, 128, 256, 512):
-            raise ValueError(f"block must be 0, 128, 256 or 512, got {self.block!r}")
+        if self.block not in (0, 32, 128, 256, 512):
+            raise ValueError(f"block must be 0, 32, 128, 256 or 512, got {self.block!r}")
         if self.precision not in ("f64", "f32"):
             raise ValueError(f"precision must be 'f64' or 'f32', got {self.precision!r}")
 
@@ -452,11 +455,13 @@ def transient(circuit, ts, ic="dc", method: str = "be",
         if circuit.batch == 1:
             return Solution(tt, z_out[:, 0], conv[:, 0].bool(), circuit.layout, iters[:, 0])
         return Solution(tt, z_out.permute(1, 0, 2), conv.T.bool(), circuit.layout, iters.T)
+    dc_sol = None
     if isinstance(ic, Solution):
         z0 = ic.z
     elif isinstance(ic, str):
         if ic == "dc":
-            z0 = dc(circuit, float(ts_np[0]), options=options).z
+            dc_sol = dc(circuit, float(ts_np[0]), options=options)
+            z0 = dc_sol.z
         elif ic == "zero":
             z0 = torch.zeros((B, S), dtype=torch.float64, device=dev)
         else:
@@ -475,6 +480,9 @@ def transient(circuit, ts, ic="dc", method: str = "be",
         call.eng.handle, B, call.params, mode, T, ts_np.ctypes.data_as(L.PF64), z0.data_ptr(),
         options.gmin, C.byref(o), z_out.data_ptr(), conv.data_ptr(), iters.data_ptr(),
         call.ws.data_ptr(), stream_ptr()), "vxg_transient")
+    if dc_sol is not None:  # row 0 reports the DC solve, as the fused engine does
+        conv[0] = 1
+        iters[0] = dc_sol.iterations.reshape(-1).to(torch.int32)
     z_out = _attach_adjoint(call, ts_np, mode, isinstance(ic, str) and ic == "dc", options, z_out)
     tt = torch.as_tensor(ts_np)
     if circuit.batch == 1:

@@ -5,8 +5,10 @@ topology and the batch: the fused persistent kernel keeps an instance on
 one CTA (best when several CTAs fit an SM), the generic level kernels
 spread every instance over the whole GPU (best when the fused kernel's
 shared-memory footprint leaves one narrow CTA per SM). `choose` times the
-candidates -- the fused kernel at 128, 256 and 512 threads per CTA, and
-the generic engine -- on a few DC Newton iterations of the caller's own
+candidates -- the fused kernel at 128, 256 and 512 threads per instance
+(one CTA each), the fused kernel with one warp per instance (several per
+CTA; only topologies whose supernodes are at most 32 wide), and the
+generic engine -- on a few DC Newton iterations of the caller's own
 instances, and keeps the fastest per (topology, precision, batch size
 class). Each trial runs on scratch copies; nothing the caller owns is
 written.
@@ -28,7 +30,7 @@ from .runtime import stream_ptr
 
 TRIAL_STEPS = 3
 TRIAL_INSTANCES = 4096
-BLOCKS = (128, 256, 512)
+BLOCKS = (32, 128, 256, 512)
 
 _cache: dict[tuple, tuple[str, int]] = {}
 
@@ -68,11 +70,15 @@ def choose(call) -> tuple[str, int]:
         nat.block = block
 
         def fused():
-            L.check(eng.lib.vxg_fused_run(
+            return eng.lib.vxg_fused_run(
                 eng.handle, n, call.params, L.VXG_MODE_DC, 1, ts.data_ptr(), z0.data_ptr(), 1,
                 None, 0, TRIAL_STEPS, o.gmin, C.byref(nat), z_out.data_ptr(), conv.data_ptr(),
-                iters.data_ptr(), stream_ptr()), "vxg_fused_run")
+                iters.data_ptr(), stream_ptr())
 
+        status = fused()
+        if status == L.VXG_ERR_TOO_LARGE:  # the warp kernel: a supernode wider than 32
+            continue
+        L.check(status, "vxg_fused_run")
         ms = _time(fused)
         results[("fused", block)] = ms / max(int(iters.sum()), 1)
     z = torch.empty_like(z0)

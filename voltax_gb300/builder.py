@@ -1,41 +1,77 @@
 """`CircuitBuilder`: describe a circuit device by device with named nodes
-(voltax/builder.py:52-256).
+(the interface of voltax/builder.py:52-256).
 
-Devices of the same type and static configuration are fused into one element
-group at `build`; group names follow voltax (``EKVMOSFET_n``,
-``VoltageSource_Step``, ``Resistor``, ...), so the state layout -- groups in
-sorted-name order -- is the one voltax would build.
+The circuit's state layout depends on how devices are fused into element
+groups and what the groups are called (groups are laid out in sorted-name
+order), so `build` follows voltax's rule exactly:
+
+1. Node indices follow the first appearance of each non-ground node name,
+   in the order devices were added (or nodes declared with `node`).
+2. A device joins the group it was given explicitly, else the automatic
+   group of its fusion key (element type + static configuration). Devices
+   in one explicit group must share a fusion key.
+3. Explicit groups keep their names. Automatic groups are named afterwards,
+   in order of their first device: the base name is the class name, with
+   ``_<polarity>`` for transistors or ``_<waveform class>`` for sources
+   with a non-constant waveform. Each base has a cursor over the names
+   ``base, base_2, base_3, ...``: a group takes the first name at or after
+   the cursor that no group has yet, and the cursor moves on past the
+   names it tried.
 """
 
 from __future__ import annotations
 
 import contextlib
-from collections import defaultdict
+import itertools
+from dataclasses import dataclass
 
 from . import elements as el
 from .circuit import GROUND, Circuit
 from .elements import Element, concatenate
 from .signals import Constant, Signal
 
-_PREFIX = {
-    el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C",
-    el.VoltageSource: "V", el.CurrentSource: "I", el.EKVMOSFET: "M", el.Level1MOSFET: "M",
-    el.Inductor: "L", el.Diode: "D", el.VCCS: "G", el.BJT: "Q", el.VCVS: "E", el.CCCS: "F",
-    el.CCVS: "H", el.Transformer: "K", el.IdealOpAmp: "U", el.OpAmp: "U", el.Switch: "S",
+# SPICE letter of each element type for default device names (R1, M3, ...)
+_LETTER = {
+    el.Conductance: "R", el.Resistor: "R", el.Capacitor: "C", el.Inductor: "L",
+    el.Transformer: "K", el.VoltageSource: "V", el.CurrentSource: "I", el.Diode: "D",
+    el.BJT: "Q", el.EKVMOSFET: "M", el.Level1MOSFET: "M", el.VCVS: "E", el.VCCS: "G",
+    el.CCCS: "F", el.CCVS: "H", el.IdealOpAmp: "U", el.OpAmp: "U", el.Switch: "S",
 }
 
 
-def _default_group_name(element: Element) -> str:
-    """Class name, plus polarity for transistors or the waveform for non-DC
-    sources (voltax/builder.py:39-49)."""
-    name = type(element).__name__
-    polarity = getattr(element, "polarity", None)
-    if isinstance(polarity, str):
-        return f"{name}_{polarity}"
+def group_base_name(element: Element) -> str:
+    """The automatic group name of `element` before any ``_2`` suffix."""
+    cls = type(element).__name__
+    pol = getattr(element, "polarity", None)
+    if isinstance(pol, str):
+        return cls + "_" + pol
     wave = getattr(element, "value", None)
     if isinstance(wave, Signal) and not isinstance(wave, Constant):
-        return f"{name}_{type(wave).__name__}"
-    return name
+        return cls + "_" + type(wave).__name__
+    return cls
+
+
+@dataclass
+class _Pending:
+    """A device added to the builder: its full name, the element with node
+    names as terminals, and its explicit group (or None)."""
+    name: str
+    element: Element
+    group: str | None
+
+
+class _NameCursor:
+    """Candidate names ``base, base_2, base_3, ...`` of one base, consumed
+    in order across the groups that share the base."""
+
+    def __init__(self, base: str):
+        self._names = itertools.chain([base], (f"{base}_{i}" for i in itertools.count(2)))
+
+    def take(self, taken) -> str:
+        for cand in self._names:
+            if cand not in taken:
+                return cand
+        raise AssertionError("unreachable")
 
 
 class CircuitBuilder:
@@ -43,59 +79,73 @@ class CircuitBuilder:
 
     Args:
         nmos, pmos: Default `MOSProcess` for `nmos` / `pmos` devices.
+        mos_model: MOSFET class used by `nmos` / `pmos` (EKVMOSFET,
+            Level1MOSFET or a partial of one).
     """
 
     def __init__(self, nmos: el.MOSProcess | None = None,
                  pmos: el.MOSProcess | None = None, mos_model=el.EKVMOSFET):
         self.nmos_process = nmos or el.MOSProcess.nmos()
         self.pmos_process = pmos or el.MOSProcess.pmos()
-        self.mos_model = mos_model  # EKVMOSFET, Level1MOSFET or a partial of one
-        self._devices: list[tuple[str, Element, str | None]] = []
-        self._names: set[str] = set()
-        self._nodes: dict[str, None] = {}
-        self._scope: list[str] = []
-        self._counters: dict[str, int] = defaultdict(int)
+        self.mos_model = mos_model
+        self._pending: list[_Pending] = []
+        self._taken_names: set[str] = set()
+        self._node_order: dict[str, int] = {}   # node name -> index (insertion order)
+        self._prefix: list[str] = []            # active scopes
+        self._count: dict[str, int] = {}        # per SPICE letter / anonymous nodes
+
+    def _bump(self, key: str) -> int:
+        self._count[key] = self._count.get(key, 0) + 1
+        return self._count[key]
+
+    def _scoped(self, name: str) -> str:
+        return ".".join(self._prefix + [name])
+
+    def _touch(self, node: str) -> None:
+        if node not in GROUND and node not in self._node_order:
+            self._node_order[node] = len(self._node_order)
 
     # ---------------------------------------------------------------- nodes
     def node(self, name: str | None = None) -> str:
-        if name is None:
-            self._counters["_node"] += 1
-            name = f"_{self._counters['_node']}"
-        full = ".".join([*self._scope, name])
-        self._nodes.setdefault(full, None)
+        """Declare a node (a fresh anonymous one when `name` is None) inside
+        the current scope; returns its full name."""
+        full = self._scoped(name if name is not None else f"_{self._bump('_node')}")
+        self._touch(full)
         return full
 
     @contextlib.contextmanager
     def scope(self, prefix: str):
-        self._scope.append(prefix)
+        """Prefix device names and `node` names with ``prefix.``."""
+        self._prefix.append(prefix)
         try:
             yield
         finally:
-            self._scope.pop()
+            self._prefix.pop()
 
     @property
     def nodes(self) -> list[str]:
-        return list(self._nodes)
+        """Non-ground node names in index order."""
+        return list(self._node_order)
 
     # -------------------------------------------------------------- devices
     def add(self, element: Element, name: str | None = None,
             group: str | None = None) -> str:
+        """Add one device whose terminals are node names; returns its full
+        (scoped) name. Default names are the SPICE letter plus a counter."""
         if element.size != 1:
             raise ValueError("add() takes single-device elements")
         if name is None:
-            prefix = _PREFIX.get(type(element), type(element).__name__)
-            self._counters[prefix] += 1
-            name = f"{prefix}{self._counters[prefix]}"
-        name = ".".join([*self._scope, name])
-        if name in self._names:
-            raise ValueError(f"duplicate device name {name!r}")
-        self._names.add(name)
-        terminals = tuple(str(n) for n in element.nodes[0])
-        for n in terminals:
-            if n not in GROUND:
-                self._nodes.setdefault(n, None)
-        self._devices.append((name, element.with_nodes((terminals,)), group))
-        return name
+            letter = _LETTER.get(type(element), type(element).__name__)
+            name = f"{letter}{self._bump(letter)}"
+        full = self._scoped(name)
+        if full in self._taken_names:
+            raise ValueError(f"duplicate device name {full!r}")
+        self._taken_names.add(full)
+        terminals = tuple(map(str, element.nodes[0]))
+        for t in terminals:
+            self._touch(t)
+        self._pending.append(_Pending(full, element.with_nodes((terminals,)), group))
+        return full
 
     def resistor(self, p, n, r, name=None, group=None) -> str:
         return self.add(el.Resistor((p, n), r), name, group)
@@ -146,50 +196,46 @@ class CircuitBuilder:
     def isource(self, p, n, value=0.0, ac=0.0, ac_phase=0.0, name=None, group=None) -> str:
         return self.add(el.CurrentSource((p, n), value, ac, ac_phase), name, group)
 
+    def _mos(self, polarity, d, g, s, b, w, l, name, group, process, dvth) -> str:
+        proc = process or (self.nmos_process if polarity == "n" else self.pmos_process)
+        dev = self.mos_model((d, g, s, s if b is None else b), w, l, proc, polarity, dvth)
+        return self.add(dev, name, group)
+
     def nmos(self, d, g, s, b=None, w=1e-6, l=0.13e-6, name=None, group=None,
              process=None, dvth=0.0) -> str:
-        dev = self.mos_model((d, g, s, s if b is None else b), w, l,
-                             process or self.nmos_process, "n", dvth)
-        return self.add(dev, name, group)
+        return self._mos("n", d, g, s, b, w, l, name, group, process, dvth)
 
     def pmos(self, d, g, s, b=None, w=1e-6, l=0.13e-6, name=None, group=None,
              process=None, dvth=0.0) -> str:
-        dev = self.mos_model((d, g, s, s if b is None else b), w, l,
-                             process or self.pmos_process, "p", dvth)
-        return self.add(dev, name, group)
+        return self._mos("p", d, g, s, b, w, l, name, group, process, dvth)
 
     # ---------------------------------------------------------------- build
     def build(self) -> Circuit:
-        """Resolve node names, fuse devices into groups (builder.py:224-256)."""
-        index = {name: i for i, name in enumerate(self._nodes)}
+        """Resolve node names to indices, fuse devices into groups and name
+        the groups by the rule in the module docstring."""
+        index = self._node_order
+        explicit: dict[str, list[tuple[str, Element]]] = {}
+        automatic: dict[tuple, list[tuple[str, Element]]] = {}
+        for p in self._pending:
+            dev = p.element.with_nodes(
+                (tuple(-1 if t in GROUND else index[t] for t in p.element.nodes[0]),))
+            if p.group is None:
+                automatic.setdefault(dev.group_key(), []).append((p.name, dev))
+                continue
+            members = explicit.setdefault(p.group, [])
+            if members and members[0][1].group_key() != dev.group_key():
+                raise ValueError(f"devices in group {p.group!r} cannot be fused")
+            members.append((p.name, dev))
 
-        def resolve(n):
-            return -1 if n in GROUND else index[n]
+        named: list[tuple[str, list[tuple[str, Element]]]] = list(explicit.items())
+        taken = set(explicit)
+        cursors: dict[str, _NameCursor] = {}
+        for members in automatic.values():
+            base = group_base_name(members[0][1])
+            gname = cursors.setdefault(base, _NameCursor(base)).take(taken)
+            taken.add(gname)
+            named.append((gname, members))
 
-        buckets: dict = {}
-        for name, dev, group in self._devices:
-            dev = dev.with_nodes((tuple(resolve(n) for n in dev.nodes[0]),))
-            key = group if group is not None else dev.group_key()
-            if group is not None and buckets.get(key):
-                if buckets[key][0][1].group_key() != dev.group_key():
-                    raise ValueError(f"devices in group {group!r} cannot be fused")
-            buckets.setdefault(key, []).append((name, dev))
-
-        groups: dict[str, Element] = {}
-        device_names: dict[str, tuple[str, int]] = {}
-        used: dict[str, int] = defaultdict(int)
-        order = sorted(buckets, key=lambda k: not isinstance(k, str))
-        for key in order:
-            members = buckets[key]
-            if isinstance(key, str):
-                gname = key
-            else:
-                base = _default_group_name(members[0][1])
-                gname = base
-                while gname in groups or gname in buckets:
-                    used[base] += 1
-                    gname = f"{base}_{used[base] + 1}"
-            groups[gname] = concatenate([dev for _, dev in members])
-            for i, (name, _) in enumerate(members):
-                device_names[name] = (gname, i)
-        return Circuit(groups, tuple(self._nodes), device_names)
+        groups = {g: concatenate([dev for _, dev in members]) for g, members in named}
+        where = {dname: (g, i) for g, members in named for i, (dname, _) in enumerate(members)}
+        return Circuit(groups, tuple(index), where)

@@ -38,6 +38,43 @@ static int fused_eligible(const Topo& t, int precision, size_t* smem_out,
   return VXG_ERR_TOO_LARGE;
 }
 
+// The warp-per-instance kernel: topologies whose supernodes are at most 32
+// wide. Warps per CTA (2, 4 or 8) chosen for the most resident instances per
+// SM (ties: more warps, i.e. fewer copies of the staged tables); the Schur
+// gather tables stay in global memory when the rest does not fit otherwise.
+static int launch_warp_kernel(const Topo& t, FusedArgs& a, bool f32, cudaStream_t s) {
+  if (t.kmax > 32) return VXG_ERR_TOO_LARGE;
+  int dev = 0, max_optin = 0, smem_sm = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  const int options[2][2] = {{B_COUNT, t.blob.len},
+                             {B_ST_TGT, (t.blob.off[B_ST_TGT] + 7) / 8 * 8}};
+  int best_inst = 0, best_wpc = 0, best_opt = 0;
+  for (int o = 0; o < 2 && !best_inst; ++o) {
+    a.first_global = options[o][0];
+    a.staged = options[o][1];
+    for (int wpc : {8, 4, 2}) {
+      const size_t smem = f32 ? warp_kernel_smem<float>(a, wpc) : warp_kernel_smem<double>(a, wpc);
+      if (smem > (size_t)max_optin) continue;
+      const int ctas = std::min<int>((int)(smem_sm / (smem + 1024)), VXG_FUSED_WARPS_PER_SM / wpc);
+      if (ctas * wpc > best_inst) {
+        best_inst = ctas * wpc;
+        best_wpc = wpc;
+        best_opt = o;
+      }
+    }
+  }
+  if (!best_inst) return VXG_ERR_TOO_LARGE;
+  a.first_global = options[best_opt][0];
+  a.staged = options[best_opt][1];
+  switch (best_wpc) {
+    case 8: return f32 ? launch_fused_warp<float, 8>(a, s) : launch_fused_warp<double, 8>(a, s);
+    case 4: return f32 ? launch_fused_warp<float, 4>(a, s) : launch_fused_warp<double, 4>(a, s);
+    default: return f32 ? launch_fused_warp<float, 2>(a, s) : launch_fused_warp<double, 2>(a, s);
+  }
+}
+
 // Phase-timing target of this thread's vxg_fused_run calls (null: off).
 static thread_local long long* t_phase_clk = nullptr;
 
@@ -147,6 +184,7 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
     nt = batch < 2 * sms ? 256 : fit <= 1 ? 512 : fit <= 2 ? 256 : 128;
   }
   const bool f32 = o->precision == VXG_F32;
+  if (nt == 32) return launch_warp_kernel(t, a, f32, s);
   switch (nt) {
     case 128: return f32 ? launch_fused<float, 128>(a, s) : launch_fused<double, 128>(a, s);
     case 256: return f32 ? launch_fused<float, 256>(a, s) : launch_fused<double, 256>(a, s);

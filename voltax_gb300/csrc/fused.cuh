@@ -78,10 +78,19 @@ struct FusedLayout {
       total;
 };
 
+// Shared memory of one instance; a warp-owned instance (warp_group) needs
+// only one warp's column/row buffers and pivot records.
+__host__ __device__ inline int inst_sbuf_values(int nw, bool warp_group) {
+  return warp_group ? 64 : sbuf_values(nw);
+}
+__host__ __device__ inline int inst_sbuf_records(int nw, bool warp_group) {
+  return warp_group ? 32 : sbuf_records(nw);
+}
+
 template <typename T>
 __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, int n_jac,
                                                     int work, int max_scr, int blob_len,
-                                                    int nw) {
+                                                    int nw, bool warp_group = false) {
   // T is the panel type; the Jacobian contributions use the same type
   FusedLayout L;
   size_t o = 0;
@@ -121,7 +130,8 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   L.prof = take(PH_COUNT * sizeof(long long));
   // per-warp column/row buffers (64 values) and pivot records (32) of nw
   // warps, or the whole CTA's (2 kCtaK values, kCtaK records)
-  L.sbuf = take(sizeof(T) * sbuf_values(nw) + sizeof(int) * sbuf_records(nw));
+  L.sbuf = take(sizeof(T) * inst_sbuf_values(nw, warp_group) +
+                sizeof(int) * inst_sbuf_records(nw, warp_group));
   L.total = o;
   return L;
 }
@@ -521,20 +531,38 @@ __device__ void tiny_factor(T* P, int k, int r, T* Sout) {
 // ------------------------------------------------------------- one instance
 typedef unsigned short u16;
 
-template <typename T, int NT>
+// One instance worked on by a group of threads: the whole CTA (kWarp false,
+// NT threads) or one warp (kWarp true; the CTA then holds NT / 32 instances,
+// one per warp, sharing the staged tables). tid() / wid() are the thread and
+// warp index inside the group, GT / GW its thread and warp counts, sync()
+// its barrier.
+template <typename T, int NT, bool kWarp = false>
 struct Instance {
+  static constexpr int GT = kWarp ? 32 : NT;
+  static constexpr int GW = kWarp ? 1 : NT / 32;
+  __device__ __forceinline__ static int tid() {
+    return kWarp ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  }
+  __device__ __forceinline__ static int wid() { return kWarp ? 0 : (int)(threadIdx.x >> 5); }
+  __device__ __forceinline__ static void sync() {
+    if (kWarp)
+      __syncwarp();
+    else
+      __syncthreads();
+  }
+
   const FusedArgs& A;
   int b;
   double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *cf, *cq, *red;
   T *data, *cj, *work, *scr, *xt, *sbuf;
   int* ibuf;
-  long long* prof;  // per-CTA phase cycles (shared memory), used when A.phase_clk
+  long long* prof;  // per-instance phase cycles (shared memory), used when A.phase_clk
   const u16* tb;  // shared-memory tables
 
-  // Thread 0 adds the cycles since *t0 to phase p; every phase ends with a
-  // CTA barrier, so thread 0's clock at its end is the CTA's.
+  // The group's thread 0 adds the cycles since *t0 to phase p; every phase
+  // ends with the group's barrier, so that thread's clock is the group's.
   __device__ __forceinline__ void mark(int p, long long* t0) const {
-    if (A.phase_clk && threadIdx.x == 0) {
+    if (A.phase_clk && tid() == 0) {
       const long long t = clock64();
       prof[p] += t - *t0;
       *t0 = t;
@@ -549,7 +577,7 @@ struct Instance {
   // thread per target, sources in a fixed order
   __device__ __forceinline__ void apply_schur(int t0, int t1, const u16* st_tgt,
                                               const u16* st_ptr, const u16* st_src) {
-    for (int t = t0 + threadIdx.x; t < t1; t += NT) {
+    for (int t = t0 + tid(); t < t1; t += GT) {
       T acc = T(0);
       const int p1 = st_ptr[t + 1];
       for (int p = st_ptr[t]; p < p1; ++p) acc += scr[st_src[p]];
@@ -561,14 +589,18 @@ struct Instance {
   // (many tiny supernodes with short borders), one warp each (several
   // supernodes), or the whole CTA (a lone supernode, supernodes wider than
   // 32, or a few with wide borders whose Schur blocks need more than a warp).
+  // A warp-owned instance (kWarp) has no CTA mode: its warp takes the
+  // supernodes one after the other, or its lanes take tiny ones in parallel
+  // (its topologies have no supernode wider than 32).
   enum { LV_TINY = 0, LV_WARP = 1, LV_CTA = 2 };
   __device__ __forceinline__ int level_mode(int L) const {
     const u16* lv_ptr = sec(B_LV_PTR);
     const int n = lv_ptr[L + 1] - lv_ptr[L];
     const int kmax = sec(B_LV_KMAX)[L], rmax = sec(B_LV_RMAX)[L];
+    if (kWarp) return (kmax <= kTiny && rmax <= 8 && n >= 4) ? LV_TINY : LV_WARP;
     if (kmax > 32) return LV_CTA;
-    if (kmax <= kTiny && n >= NT / 32 && rmax <= 8) return LV_TINY;
-    if (n >= 2 && (2 * n >= NT / 32 || rmax <= 16)) return LV_WARP;
+    if (kmax <= kTiny && n >= GW && rmax <= 8) return LV_TINY;
+    if (n >= 2 && (2 * n >= GW || rmax <= 16)) return LV_WARP;
     return LV_CTA;
   }
 
@@ -577,7 +609,7 @@ struct Instance {
                        bool wj) {
     const GroupTable& gt = A.gt;
     const u16* nodes = sec(B_NODES);
-    for (int flat = threadIdx.x; flat < gt.n_dev; flat += NT) {
+    for (int flat = tid(); flat < gt.n_dev; flat += GT) {
       int gi = 0;
       while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
       const GroupDev& g = gt.g[gi];
@@ -617,7 +649,7 @@ struct Instance {
   __device__ void assemble_res(double* fo, double* qo) {
     const u16* ptr = sec(B_RES_PTR);
     const u16* src = sec(B_RES_SRC);
-    for (int i = threadIdx.x; i < A.S; i += NT) {
+    for (int i = tid(); i < A.S; i += GT) {
       const int p0 = ptr[i], p1 = ptr[i + 1];
       if (p1 - p0 > 32) continue;  // long rows: below
       if (fo) {
@@ -633,8 +665,8 @@ struct Instance {
     }
     const u16* longs = sec(B_LONG_RES);
     const int n_long = A.bo.off[B_LONG_RES + 1] - A.bo.off[B_LONG_RES];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int li = warp; li < n_long; li += NT / 32) {
+    const int lane = threadIdx.x & 31, warp = wid();
+    for (int li = warp; li < n_long; li += GW) {
       const int i = longs[li];
       const int p0 = ptr[i], p1 = ptr[i + 1];
       if (fo) {
@@ -660,7 +692,7 @@ struct Instance {
     const u16* jsrc = sec(B_JAC_SRC);
     const u16* rows = sec(B_ROWS);
     const u16* cols = sec(B_INDICES);
-    for (int e = threadIdx.x; e < A.nnz; e += NT) {
+    for (int e = tid(); e < A.nnz; e += GT) {
       const int p0 = jptr[e], p1 = jptr[e + 1];
       if (p1 - p0 > 32) continue;  // long entries: below
       T acc = T(0);
@@ -672,8 +704,8 @@ struct Instance {
     {
       const u16* longs = sec(B_LONG_JAC);
       const int n_long = A.bo.off[B_LONG_JAC + 1] - A.bo.off[B_LONG_JAC];
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      for (int li = warp; li < n_long; li += NT / 32) {
+      const int lane = threadIdx.x & 31, warp = wid();
+      for (int li = warp; li < n_long; li += GW) {
         const int e = longs[li];
         T acc = warp_list_sum<T>(cj, jsrc, jptr[e], jptr[e + 1]);
         const int r = rows[e];
@@ -682,14 +714,14 @@ struct Instance {
       }
     }
     if (first && mode != VXG_MODE_DC)
-      for (int i = threadIdx.x; i < A.S; i += NT) qp[i] = q[i];
-    __syncthreads();
+      for (int i = tid(); i < A.S; i += GT) qp[i] = q[i];
+    sync();
     // the panels overlay the contributions consumed above
-    for (int i = threadIdx.x; i < A.work; i += NT) work[i] = T(0);
-    __syncthreads();
+    for (int i = tid(); i < A.work; i += GT) work[i] = T(0);
+    sync();
     const u16* apos = sec(B_APOS);
-    for (int e = threadIdx.x; e < A.nnz; e += NT) work[apos[e]] = data[e];
-    for (int i = threadIdx.x; i < A.S; i += NT) {
+    for (int e = tid(); e < A.nnz; e += GT) work[apos[e]] = data[e];
+    for (int i = tid(); i < A.S; i += GT) {
       const double gm = i < A.nv ? gmin * z[i] : 0.0;
       double r;
       if (mode == VXG_MODE_DC)
@@ -700,12 +732,12 @@ struct Instance {
         r = (q[i] - qp[i]) / h + 0.5 * (f[i] + fp[i]) + gm;
       rhs[i] = -r;
     }
-    __syncthreads();
+    sync();
   }
 
   __device__ void factor() {
-    constexpr int NW = NT / 32;
-    const int warp = threadIdx.x >> 5;
+    constexpr int NW = GW;
+    const int warp = wid();
     T* colb = sbuf + warp * 64;
     T* rowb = colb + 32;
     int* perm = ibuf + warp * 32;
@@ -716,7 +748,7 @@ struct Instance {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
       const int mode = level_mode(L);
       if (mode == LV_TINY) {
-        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+        for (int p = lo + tid(); p < hi; p += GT) {
           const int j = lv_sn[p];
           tiny_factor<T>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p]);
         }
@@ -726,7 +758,7 @@ struct Instance {
           sn_factor<T, false, NT, 1>(work + sn_panel[j], sn_k[j], sn_r[j], scr + sch_off[p], colb,
                                   rowb, perm);
         }
-      } else {
+      } else if constexpr (!kWarp) {
         for (int p = lo; p < hi; ++p) {
           const int j = lv_sn[p];
           if (sn_k[j] <= 32)
@@ -737,19 +769,19 @@ struct Instance {
                                                scr + sch_off[p], sbuf, sbuf + kCtaK, ibuf);
         }
       }
-      __syncthreads();
+      sync();
       if (A.first_global > B_ST_TGT)  // tables in shared memory
         apply_schur(st_lv[L], st_lv[L + 1], sec(B_ST_TGT), sec(B_ST_PTR), sec(B_ST_SRC));
       else
         apply_schur(st_lv[L], st_lv[L + 1], A.blob + A.bo.off[B_ST_TGT],
                     A.blob + A.bo.off[B_ST_PTR], A.blob + A.bo.off[B_ST_SRC]);
-      __syncthreads();
+      sync();
     }
   }
 
   // in-place solve of xt
   __device__ void solve_t() {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = wid();
     const u16 *lv_ptr = sec(B_LV_PTR), *lv_sn = sec(B_LV_SN);
     const u16 *bord_off = sec(B_LV_BORD_OFF), *sn_k = sec(B_SN_K), *sn_r = sec(B_SN_R);
     const u16 *sn_panel = sec(B_SN_PANEL), *piv_ptr = sec(B_SN_PIV_PTR), *pivs = sec(B_SN_PIV);
@@ -759,7 +791,7 @@ struct Instance {
     for (int L = 0; L < A.n_levels; ++L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
       if (level_mode(L) == LV_TINY) {
-        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+        for (int p = lo + tid(); p < hi; p += GT) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
           const T* W = work + sn_panel[j];
@@ -795,9 +827,9 @@ struct Instance {
           const u16* piv = pivs + piv_ptr[j];
           T* cb = scr + bord_off[p];
           T* y = sbuf;
-          for (int l = threadIdx.x; l < k; l += NT) y[l] = xt[piv[l]];
-          __syncthreads();
-          for (int i = threadIdx.x; i < k + r; i += NT) {
+          for (int l = tid(); l < k; l += GT) y[l] = xt[piv[l]];
+          sync();
+          for (int i = tid(); i < k + r; i += GT) {
             T acc = T(0);
             if (i < k) {
               for (int l = 0; l < k; ++l) acc += W[i * k + l] * y[l];
@@ -807,10 +839,10 @@ struct Instance {
               cb[i - k] = acc;
             }
           }
-          __syncthreads();
+          sync();
         }
       } else {
-        for (int p = lo + warp; p < hi; p += NT / 32) {
+        for (int p = lo + warp; p < hi; p += GW) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
           const T* W = work + sn_panel[j];
@@ -835,19 +867,19 @@ struct Instance {
           if (lane < k) xt[piv[lane]] = acc;
         }
       }
-      __syncthreads();
-      for (int t = bt_lv[L] + threadIdx.x; t < bt_lv[L + 1]; t += NT) {
+      sync();
+      for (int t = bt_lv[L] + tid(); t < bt_lv[L + 1]; t += GT) {
         T acc = T(0);
         const int p1 = bt_ptr[t + 1];
         for (int p = bt_ptr[t]; p < p1; ++p) acc += scr[bt_src[p]];
         xt[bt_tgt[t]] -= acc;
       }
-      __syncthreads();
+      sync();
     }
     for (int L = A.n_levels - 1; L >= 0; --L) {
       const int lo = lv_ptr[L], hi = lv_ptr[L + 1];
       if (level_mode(L) == LV_TINY) {
-        for (int p = lo + threadIdx.x; p < hi; p += NT) {
+        for (int p = lo + tid(); p < hi; p += GT) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
           const T* Ub = work + sn_panel[j] + k * k;
@@ -867,14 +899,14 @@ struct Instance {
           const T* Ub = work + sn_panel[j] + k * k;
           const u16* piv = pivs + piv_ptr[j];
           const u16* brd = bords + bord_ptr[j];
-          for (int i = threadIdx.x; i < k; i += NT) {
+          for (int i = tid(); i < k; i += GT) {
             T acc = T(0);
             for (int a = 0; a < r; ++a) acc += Ub[i * r + a] * xt[brd[a]];
             xt[piv[i]] -= acc;
           }
         }
       } else {
-        for (int p = lo + warp; p < hi; p += NT / 32) {
+        for (int p = lo + warp; p < hi; p += GW) {
           const int j = lv_sn[p];
           const int k = sn_k[j], r = sn_r[j];
           if (r == 0) continue;
@@ -888,31 +920,31 @@ struct Instance {
           }
         }
       }
-      __syncthreads();
+      sync();
     }
   }
 
   // dz = J^-1 rhs with FP64 refinement
   __device__ void solve(int refine) {
-    for (int i = threadIdx.x; i < A.S; i += NT) xt[i] = (T)rhs[i];
-    __syncthreads();
+    for (int i = tid(); i < A.S; i += GT) xt[i] = (T)rhs[i];
+    sync();
     solve_t();
-    for (int i = threadIdx.x; i < A.S; i += NT) dz[i] = (double)xt[i];
-    __syncthreads();
+    for (int i = tid(); i < A.S; i += GT) dz[i] = (double)xt[i];
+    sync();
     const u16* indptr = sec(B_INDPTR);
     const u16* cols = sec(B_INDICES);
     const u16* longs = sec(B_LONG_ROW);
     const int n_long = A.bo.off[B_LONG_ROW + 1] - A.bo.off[B_LONG_ROW];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = wid();
     for (int it = 0; it < refine; ++it) {
-      for (int i = threadIdx.x; i < A.S; i += NT) {
+      for (int i = tid(); i < A.S; i += GT) {
         const int e0 = indptr[i], e1 = indptr[i + 1];
         if (e1 - e0 > 32) continue;  // long rows: a warp each, below
         double acc = 0.0;
         for (int e = e0; e < e1; ++e) acc += (double)data[e] * dz[cols[e]];
         xt[i] = (T)(rhs[i] - acc);
       }
-      for (int li = warp; li < n_long; li += NT / 32) {
+      for (int li = warp; li < n_long; li += GW) {
         const int i = longs[li];
         double acc = 0.0;
         for (int e = indptr[i] + lane; e < indptr[i + 1]; e += 32)
@@ -920,36 +952,47 @@ struct Instance {
         for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
         if (lane == 0) xt[i] = (T)(rhs[i] - acc);
       }
-      __syncthreads();
+      sync();
       solve_t();
-      for (int i = threadIdx.x; i < A.S; i += NT) dz[i] += (double)xt[i];
-      __syncthreads();
+      for (int i = tid(); i < A.S; i += GT) dz[i] += (double)xt[i];
+      sync();
     }
   }
 
-  // damped update; returns converged (uniform across the block)
+  // damped update; returns converged (uniform across the group)
   __device__ int update() {
     double m = 0.0;
     int nanf = 0;
-    for (int i = threadIdx.x; i < A.nv; i += NT) {
+    for (int i = tid(); i < A.nv; i += GT) {
       const double v = fabs(dz[i]);
       if (isnan(v)) nanf = 1;
       else m = fmax(m, v);
     }
     int any_nan = 0;
-    m = block_max_nan<NT>(m, nanf, red, &any_nan);
+    if constexpr (kWarp) {
+      for (int off = 16; off > 0; off >>= 1) {
+        m = fmax(m, __shfl_xor_sync(kFull, m, off));
+        nanf |= __shfl_xor_sync(kFull, nanf, off);
+      }
+      any_nan = nanf;
+    } else {
+      m = block_max_nan<NT>(m, nanf, red, &any_nan);
+    }
     const double dv_max = any_nan ? nan("") : m;
     const double qd = A.max_dv / (dv_max + 1e-300);
     const double scale = isnan(qd) ? qd : fmin(1.0, qd);
     int ok = 1;
-    for (int i = threadIdx.x; i < A.S; i += NT) {
+    for (int i = tid(); i < A.S; i += GT) {
       const double d = dz[i];
       const double zn = z[i] + scale * d;
       if (!(fabs(d) <= A.atol + A.rtol * fabs(zn))) ok = 0;
       if (!isfinite(zn)) ok = 0;
       z[i] = zn;
     }
-    ok = block_all<NT>(ok, red);
+    if constexpr (kWarp)
+      ok = __all_sync(kFull, ok);
+    else
+      ok = block_all<NT>(ok, red);
     return ok && scale == 1.0;
   }
 
@@ -963,7 +1006,7 @@ struct Instance {
     long long t0 = A.phase_clk ? clock64() : 0;
     while (it < max_steps && !done) {
       eval(z, t, cfc, cqc, true, !dc, true);
-      __syncthreads();
+      sync();
       mark(PH_EVAL, &t0);
       assemble_system(mode, gmin, h, it == 0);
       mark(PH_ASSEMBLE, &t0);
@@ -987,53 +1030,53 @@ struct Instance {
 #define VXG_FUSED_THREADS_PER_SM 640
 #endif
 
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
-    fused_kernel(const __grid_constant__ FusedArgs A) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const FusedLayout L =
-      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged, NT / 32);
-  {  // stage the 16-bit tables once per CTA
-    const uint4* src = reinterpret_cast<const uint4*>(A.blob);
-    uint4* dst = reinterpret_cast<uint4*>(smem + L.blob);
-    for (int i = threadIdx.x; i < A.staged / 8; i += NT) dst[i] = src[i];
-  }
-  Instance<T, NT> I{A, 0};
-  I.tb = reinterpret_cast<const unsigned short*>(smem + L.blob);
-  I.z = reinterpret_cast<double*>(smem + L.z);
-  I.zp = reinterpret_cast<double*>(smem + L.zp);
-  I.fp = reinterpret_cast<double*>(smem + L.fp);
-  I.qp = reinterpret_cast<double*>(smem + L.qp);
-  I.f = reinterpret_cast<double*>(smem + L.f);
-  I.q = reinterpret_cast<double*>(smem + L.q);
-  I.rhs = reinterpret_cast<double*>(smem + L.rhs);
-  I.dz = reinterpret_cast<double*>(smem + L.dz);
-  I.res = reinterpret_cast<double*>(smem + L.res);
-  I.data = reinterpret_cast<T*>(smem + L.data);
-  I.cf = reinterpret_cast<double*>(smem + L.cf);
-  I.cq = reinterpret_cast<double*>(smem + L.cq);
-  I.cj = reinterpret_cast<T*>(smem + L.cj);
-  I.work = reinterpret_cast<T*>(smem + L.work);
-  I.scr = reinterpret_cast<T*>(smem + L.scr);
-  I.xt = reinterpret_cast<T*>(smem + L.xt);
-  I.red = reinterpret_cast<double*>(smem + L.red);
-  I.prof = reinterpret_cast<long long*>(smem + L.prof);
-  const long long k_start = clock64();
-  if (A.phase_clk && threadIdx.x < PH_COUNT) I.prof[threadIdx.x] = 0;
-  I.sbuf = reinterpret_cast<T*>(smem + L.sbuf);
-  I.ibuf = reinterpret_cast<int*>(smem + L.sbuf + sizeof(T) * sbuf_values(NT / 32));
+// Point an instance's buffers into its shared-memory region `base`.
+template <typename T, int NT, bool kWarp>
+__device__ __forceinline__ void bind(Instance<T, NT, kWarp>& I, unsigned char* base,
+                                     const FusedLayout& L, const u16* tables) {
+  I.tb = tables;
+  I.z = reinterpret_cast<double*>(base + L.z);
+  I.zp = reinterpret_cast<double*>(base + L.zp);
+  I.fp = reinterpret_cast<double*>(base + L.fp);
+  I.qp = reinterpret_cast<double*>(base + L.qp);
+  I.f = reinterpret_cast<double*>(base + L.f);
+  I.q = reinterpret_cast<double*>(base + L.q);
+  I.rhs = reinterpret_cast<double*>(base + L.rhs);
+  I.dz = reinterpret_cast<double*>(base + L.dz);
+  I.res = reinterpret_cast<double*>(base + L.res);
+  I.data = reinterpret_cast<T*>(base + L.data);
+  I.cf = reinterpret_cast<double*>(base + L.cf);
+  I.cq = reinterpret_cast<double*>(base + L.cq);
+  I.cj = reinterpret_cast<T*>(base + L.cj);
+  I.work = reinterpret_cast<T*>(base + L.work);
+  I.scr = reinterpret_cast<T*>(base + L.scr);
+  I.xt = reinterpret_cast<T*>(base + L.xt);
+  I.red = reinterpret_cast<double*>(base + L.red);
+  I.prof = reinterpret_cast<long long*>(base + L.prof);
+  I.sbuf = reinterpret_cast<T*>(base + L.sbuf);
+  I.ibuf = reinterpret_cast<int*>(base + L.sbuf +
+                                  sizeof(T) * inst_sbuf_values(NT / 32, kWarp));
+}
+
+// The whole analysis of instances first, first + stride, ... by one group:
+// the DC operating point (direct attempt, then gmin stepping restarting from
+// z0), then one Newton solve per time point.
+template <typename T, int NT, bool kWarp>
+__device__ void run_instances(const FusedArgs& A, Instance<T, NT, kWarp>& I, int first,
+                              int stride) {
+  using G = Instance<T, NT, kWarp>;
   const long long BS = (long long)A.B * A.S;
-  for (int b = blockIdx.x; b < A.B; b += gridDim.x) {
+  for (int b = first; b < A.B; b += stride) {
     I.b = b;
-    for (int i = threadIdx.x; i < A.S; i += NT) I.z[i] = A.z0[(long long)b * A.S + i];
-    __syncthreads();
+    for (int i = G::tid(); i < A.S; i += G::GT) I.z[i] = A.z0[(long long)b * A.S + i];
+    G::sync();
     int ok = 1, it = 0;
     if (A.dc_first) {
       const int direct = A.gmin_steps > 0 ? A.direct_steps : A.max_steps;
       ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmin, direct, &it);
       if (!ok && A.gmin_steps > 0) {
-        for (int i = threadIdx.x; i < A.S; i += NT) I.z[i] = A.z0[(long long)b * A.S + i];
-        __syncthreads();
+        for (int i = G::tid(); i < A.S; i += G::GT) I.z[i] = A.z0[(long long)b * A.S + i];
+        G::sync();
         for (int s = 1; s <= A.gmin_steps; ++s) {
           int its = 0;
           ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmins[s], A.max_steps, &its);
@@ -1041,8 +1084,8 @@ __global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
         }
       }
     }
-    for (int i = threadIdx.x; i < A.S; i += NT) A.z_out[(long long)b * A.S + i] = I.z[i];
-    if (threadIdx.x == 0) {
+    for (int i = G::tid(); i < A.S; i += G::GT) A.z_out[(long long)b * A.S + i] = I.z[i];
+    if (G::tid() == 0) {
       A.conv[b] = ok;
       A.iters[b] = it;
     }
@@ -1050,27 +1093,94 @@ __global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
       const double tp = A.ts[n - 1], t = A.ts[n];
       if (A.mode == VXG_MODE_TRAP) {  // f(z_prev, t_prev); q(z_prev) comes from iteration 0
         I.eval(I.z, tp, 1.0, 0.0, true, false, false);
-        __syncthreads();
+        G::sync();
         I.assemble_res(I.fp, nullptr);
-        __syncthreads();
+        G::sync();
       }
       int its = 0;
       const int okn = I.newton(A.mode, t, tp, A.gmin, A.max_steps, &its);
-      for (int i = threadIdx.x; i < A.S; i += NT)
+      for (int i = G::tid(); i < A.S; i += G::GT)
         A.z_out[(long long)n * BS + (long long)b * A.S + i] = I.z[i];
-      if (threadIdx.x == 0) {
+      if (G::tid() == 0) {
         A.conv[(long long)n * A.B + b] = okn;
         A.iters[(long long)n * A.B + b] = its;
       }
     }
-    __syncthreads();
+    G::sync();
   }
-  if (A.phase_clk && threadIdx.x == 0) {
+}
+
+// Thread 0 of a group adds its phase cycles to the global counters.
+template <typename T, int NT, bool kWarp>
+__device__ __forceinline__ void flush_profile(const FusedArgs& A, Instance<T, NT, kWarp>& I,
+                                              long long k_start) {
+  if (A.phase_clk && Instance<T, NT, kWarp>::tid() == 0) {
     I.prof[PH_TOTAL] = clock64() - k_start;
     for (int p = 0; p < PH_COUNT; ++p)
       atomicAdd(reinterpret_cast<unsigned long long*>(A.phase_clk + p),
                 (unsigned long long)I.prof[p]);
   }
+}
+
+// Copy the first A.staged 16-bit table elements into shared memory.
+__device__ __forceinline__ void stage_tables(const FusedArgs& A, unsigned char* dst_bytes) {
+  const uint4* src = reinterpret_cast<const uint4*>(A.blob);
+  uint4* dst = reinterpret_cast<uint4*>(dst_bytes);
+  for (int i = threadIdx.x; i < A.staged / 8; i += blockDim.x) dst[i] = src[i];
+}
+
+// One CTA per instance (grid-stride over the batch).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
+    fused_kernel(const __grid_constant__ FusedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const FusedLayout L =
+      fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, A.staged, NT / 32);
+  stage_tables(A, smem + L.blob);
+  Instance<T, NT> I{A, 0};
+  bind(I, smem, L, reinterpret_cast<const u16*>(smem + L.blob));
+  const long long k_start = clock64();
+  if (A.phase_clk && threadIdx.x < PH_COUNT) I.prof[threadIdx.x] = 0;
+  __syncthreads();
+  run_instances(A, I, blockIdx.x, gridDim.x);
+  flush_profile(A, I, k_start);
+}
+
+// Shared-memory bytes of the warp-per-instance kernel: the staged tables
+// once, then one instance region per warp.
+template <typename T>
+__host__ __device__ inline size_t warp_table_bytes(const FusedArgs& A) {
+  return a16(sizeof(u16) * (size_t)A.staged);
+}
+template <typename T>
+__host__ __device__ inline FusedLayout warp_instance_layout(const FusedArgs& A) {
+  return fused_layout<T>(A.S, A.nnz, A.n_res, A.n_jac, A.work, A.max_scr, 0, 1, true);
+}
+
+// One warp per instance, WPC instances per CTA sharing the staged tables
+// (grid-stride over the batch). No CTA barrier after the tables are staged:
+// each warp runs its instances with warp barriers only, so one instance's
+// latency-bound factorization overlaps other warps' device evaluation.
+#ifndef VXG_FUSED_WARPS_PER_SM
+#define VXG_FUSED_WARPS_PER_SM 16  // register budget: 128 per thread
+#endif
+
+template <typename T, int WPC>
+__global__ void __launch_bounds__(32 * WPC, VXG_FUSED_WARPS_PER_SM / WPC)
+    fused_warp_kernel(const __grid_constant__ FusedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const size_t tab = warp_table_bytes<T>(A);
+  const FusedLayout L = warp_instance_layout<T>(A);
+  stage_tables(A, smem);
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Instance<T, 32 * WPC, true> I{A, 0};
+  bind(I, smem + tab + (size_t)w * L.total, L, reinterpret_cast<const u16*>(smem));
+  const long long k_start = clock64();
+  if (A.phase_clk && lane < PH_COUNT) I.prof[lane] = 0;
+  __syncwarp();
+  run_instances(A, I, blockIdx.x * WPC + w, gridDim.x * WPC);
+  flush_profile(A, I, k_start);
 }
 
 template <typename T, int NT>
@@ -1101,13 +1211,42 @@ int launch_fused(const FusedArgs& a, cudaStream_t s) {
 }
 
 
-// One translation unit per instantiation (fused_<type>_<threads>.cu), so that
-// the six kernels compile in parallel.
+// Shared memory of the warp-per-instance kernel with WPC warps per CTA.
+template <typename T>
+inline size_t warp_kernel_smem(const FusedArgs& a, int wpc) {
+  return warp_table_bytes<T>(a) + (size_t)wpc * warp_instance_layout<T>(a).total;
+}
+
+template <typename T, int WPC>
+int launch_fused_warp(const FusedArgs& a, cudaStream_t s) {
+  auto kern = fused_warp_kernel<T, WPC>;
+  const size_t smem = warp_kernel_smem<T>(a, WPC);
+  VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int dev = 0, sms = 0, per_sm = 0;
+  VXG_CUDA_TRY(cudaGetDevice(&dev));
+  VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  VXG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * WPC, smem));
+  const int ctas = (a.B + WPC - 1) / WPC;
+  const int grid = std::max(1, std::min(ctas, sms * std::max(per_sm, 1)));
+  kern<<<grid, 32 * WPC, smem, s>>>(a);
+  VXG_LAUNCHED();
+  return VXG_OK;
+}
+
+// One translation unit per instantiation (fused_<type>_<threads>.cu and
+// fused_warp_<type>.cu), so that the kernels compile in parallel.
 extern template int launch_fused<float, 128>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<float, 256>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<float, 512>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 128>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 256>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 512>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<float, 2>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<float, 4>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<float, 8>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<double, 2>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<double, 4>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused_warp<double, 8>(const FusedArgs&, cudaStream_t);
 
 }  // namespace vxg
