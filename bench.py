@@ -213,13 +213,18 @@ class Clocks:
 
 # ----------------------------------------------------------------- CPU legs
 def _cpu_systems(w, instances, count, seed=0):
+    """Compiled-oracle systems for the CPU legs. Their plan comes from the
+    oracle's numpy planner, so the CPU legs load no library of the product
+    (only oracle/_build/libcvx.so)."""
     from oracle import cbase
+    from oracle import plan as oplan
     from voltax_gb300 import symbolic
     c = w.cpu_circuit(instances, seed=seed)
     st = symbolic.structure(c)
+    plan = oplan.make_plan_numpy(st)
     ic = w.ic(c)
     z0 = None if isinstance(ic, str) else ic.numpy()
-    return [cbase.CSystem(c, st, st.plan, b % c.batch) for b in range(count)], z0
+    return [cbase.CSystem(c, st, plan, b % c.batch) for b in range(count)], z0
 
 
 def _cpu_run(w, sysm, z0, ts):

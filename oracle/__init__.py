@@ -11,10 +11,17 @@ hot path, so the CUDA path can be checked against it:
   (voltax/sparse.py:474-621)
 * `analysis` -- damped Newton, gmin stepping, DC, BE/trapezoidal transient
   and the implicit-function adjoint (voltax/analysis.py:208-480)
+* `plan`     -- numpy restatement of the symbolic planner (pivot groups,
+  nested dissection, levels, buckets; voltax/sparse.py:257-535), the
+  checker of the product's C++ planner; it builds the product's `Plan`
+  container and reuses its `union_pairs` (the scipy matching that feeds
+  both planners)
+* `cvx.c` / `cbase` -- the compiled C restatement of the whole Newton loop
+  (the timed CPU baseline) and its acceptance check of a given solution
 
 It reads circuits by the reference's attribute names (``layout.groups``,
 ``elements[name].log_r``, ``.value``, ``.log_w``, ``.process.log_kp``, ...),
-so it does not import the product package. Only ``tests/``,
+so apart from `plan` it does not import the product package. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use
 it; the product path never does.
 

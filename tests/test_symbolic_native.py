@@ -12,6 +12,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle import plan as oplan  # the numpy restatement (the C++ planner's checker)
 from voltax_gb300 import build, runtime, symbolic, workloads
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -78,15 +79,15 @@ CASES = {
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_native_plan_equals_restatement(name, leaf):
     st = symbolic.structure(CASES[name](), leaf)
-    assert_same_plan(symbolic.make_plan(st, leaf, native=True),
-                     symbolic.make_plan_numpy(st, leaf))
+    assert_same_plan(symbolic.make_plan(st, leaf),
+                     oplan.make_plan_numpy(st, leaf))
 
 
 def test_segmented_batch_plans_each_segment_apart():
     """Independent sub-circuits never share a supernode or a border."""
     c = workloads.power_grid_batch([9, 14, 6])
     seg = c.unknown_segments()
-    plan = symbolic.make_plan(symbolic.structure(c), native=True)
+    plan = symbolic.make_plan(symbolic.structure(c))
     for s, b in zip(plan.supernodes, plan.borders):
         assert len(np.unique(seg[s])) == 1
         assert len(b) == 0 or np.all(seg[b] == seg[s[0]])
@@ -128,8 +129,8 @@ def test_device_tables_from_native_plan_equal_restatement(name):
     those assembled from the numpy plan's per-level tables."""
     c = CASES[name]()
     st = symbolic.structure(c)
-    a = runtime.Tables(c, st, symbolic.make_plan(st, native=True))
-    b = runtime.Tables(c, st, symbolic.make_plan_numpy(st))
+    a = runtime.Tables(c, st, symbolic.make_plan(st))
+    b = runtime.Tables(c, st, oplan.make_plan_numpy(st))
     keys = [k for k, v in vars(b).items() if isinstance(v, np.ndarray)]
     assert "st_src" in keys and "bt_ptr" in keys and "sn_piv" in keys
     for k in keys:
