@@ -183,12 +183,11 @@ __device__ int block_all(int ok, double* red) {
 // One supernode's block LDU by a group of threads: one warp (CTA = false,
 // the supernodes of a wide level in parallel, k <= 32) or the whole CTA
 // (CTA = true, the lone supernodes of the top levels, k <= kCtaK).
-//   W  = F11^-1 by Gauss-Jordan with partial pivoting (row swaps recorded,
-//        undone as column swaps): with rows in registers (warp_gj) for a
-//        warp, or in shared memory with two barriers per pivot step for the
-//        CTA, lane l owning columns l, l + 32, ... (measured: the register
-//        form is the faster one only when other warps have their own
-//        supernodes to factor);
+//   W  = F11^-1 by Gauss-Jordan with partial pivoting: for k <= 32 by one
+//        warp with the rows in registers (warp_gj; in a CTA group the other
+//        warps wait), for wider blocks by the whole CTA in shared memory
+//        with two barriers per pivot step, lane l owning columns l, l + 32,
+//        ... (row swaps recorded, undone as column swaps);
 //   Ub = W F12 in place (one column per warp, the column held in registers
 //        and broadcast by shuffles);
 //   S  = F21 Ub into Sout;  Lb = F21 W in place (one row per warp).
@@ -200,14 +199,42 @@ __device__ __forceinline__ void group_sync() {
     __syncwarp();
 }
 
+// Warp argmax of |a| over the lanes in `valid` (ties to the lowest lane);
+// -1 when no lane is valid. One warp-wide integer max reduction on the bit
+// pattern (a non-negative float orders like its bits), not five shuffle
+// rounds; doubles compare their high word first and, only between lanes
+// that tie on it, the low word.
+__device__ __forceinline__ int warp_argmax_abs(float a, bool valid) {
+  const unsigned key = valid ? __float_as_uint(fabsf(a)) + 1u : 0u;
+  const unsigned m = __reduce_max_sync(kFull, key);
+  if (m == 0u) return -1;
+  return __ffs(__ballot_sync(kFull, key == m)) - 1;
+}
+__device__ __forceinline__ int warp_argmax_abs(double a, bool valid) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs(a));
+  const unsigned hi = valid ? (unsigned)(bits >> 32) + 1u : 0u;
+  const unsigned mh = __reduce_max_sync(kFull, hi);
+  if (mh == 0u) return -1;
+  unsigned cand = __ballot_sync(kFull, hi == mh);
+  if (__popc(cand) > 1) {
+    const bool in = (cand >> (threadIdx.x & 31)) & 1u;
+    const unsigned lo = in ? (unsigned)bits : 0u;
+    const unsigned ml = __reduce_max_sync(kFull, lo);
+    cand = __ballot_sync(kFull, in && lo == ml);
+  }
+  return __ffs(cand) - 1;
+}
+
 // Gauss-Jordan inverse of the k x k block A (row-major in shared memory,
-// k <= K <= 32) by one warp, one matrix row per lane in registers: partial
-// pivoting (largest |a|, ties to the lower row) with the rows traded by
-// shuffles, the scaled pivot row staged in `prow` (one column per lane, so
-// each step costs each lane one division), and the row swaps undone as a
-// column permutation when the rows are written back. The same operations in
-// the same order as the shared-memory Gauss-Jordan of sn_factor, without a
-// shared-memory round trip per matrix entry and step.
+// k <= K <= 32) by one warp, one matrix row per lane in registers, with
+// partial pivoting (largest |a| in the column among rows not yet used,
+// ties to the lower row). Rows never move: step c exchanges the pivot row
+// p_c with column c in place (the exchange operator: the pivot row becomes
+// x_c in terms of the right-hand side, the other rows are eliminated), so
+// the result is the inverse with its rows in pivot-row order and its
+// columns in pivot-step order; the write-back puts row p_c into row c and
+// column c into column p_c. The pivot row is staged in `prow` (one
+// division per lane per step); perm[c] = p_c.
 template <typename T, int K>
 __device__ __forceinline__ T reg_at(const T (&row)[K], int c) {
   T x = T(0);
@@ -223,59 +250,42 @@ __device__ __forceinline__ void warp_gj(T* A, int k, T* prow, int* perm) {
   T row[K];
 #pragma unroll
   for (int j = 0; j < K; ++j) row[j] = (lane < k && j < k) ? A[lane * k + j] : T(0);
+  const unsigned rows_k = k >= 32 ? kFull : ((1u << k) - 1u);
+  unsigned used = 0u;
+  int my_step = 0;  // the step at which this lane's row is the pivot
 #pragma unroll 1
   for (int c = 0; c < k; ++c) {
-    const T a = tabs_(reg_at(row, c));
-    T v = (lane >= c && lane < k && a == a) ? a : T(-1);
-    int bi = lane;
-    for (int off = 16; off > 0; off >>= 1) {
-      const T ov = __shfl_down_sync(kFull, v, off);
-      const int oi = __shfl_down_sync(kFull, bi, off);
-      if (ov > v || (ov == v && oi < bi)) {
-        v = ov;
-        bi = oi;
-      }
-    }
-    int p = __shfl_sync(kFull, bi, 0);
-    if (p < c || p >= k) p = c;
+    const T a = reg_at(row, c);
+    const bool free_row = ((rows_k & ~used) >> lane) & 1u;
+    int p = warp_argmax_abs(a, free_row && a == a);
+    if (p < 0) p = __ffs(rows_k & ~used) - 1;  // every candidate NaN
+    used |= 1u << p;
     if (lane == 0) perm[c] = p;
-    if (p != c) {  // rows c and p trade places
-      const int src = lane == c ? p : (lane == p ? c : lane);
-#pragma unroll
-      for (int j = 0; j < K; ++j) row[j] = __shfl_sync(kFull, row[j], src);
-    }
-    if (lane == c) {
+    if (lane == p) {
+      my_step = c;
 #pragma unroll
       for (int j = 0; j < K; ++j)
         if (j < k) prow[j] = row[j];
     }
     __syncwarp();
-    const T d = prow[c];
+    const T d = __shfl_sync(kFull, a, p);
     if (lane < k) prow[lane] = ((lane == c) ? T(1) : prow[lane]) / d;
     __syncwarp();
-    const T f = reg_at(row, c);
+    const T f = a;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       if (j < k) {
         const T rj = prow[j];
-        row[j] = (lane == c) ? rj : ((j == c) ? T(0) : row[j]) - f * rj;
+        row[j] = (lane == p) ? rj : ((j == c) ? T(0) : row[j]) - f * rj;
       }
     }
     __syncwarp();  // prow is rewritten by the next step
   }
-  // column j of the result goes to dest(j): the swaps c = k-1 .. 0 composed
-  int dest = lane;
-  for (int c = k - 1; c >= 0; --c) {
-    const int p = perm[c];
-    if (dest == c)
-      dest = p;
-    else if (dest == p)
-      dest = c;
-  }
+  // row p_c holds row c of the inverse with column c' at perm[c']
 #pragma unroll
   for (int j = 0; j < K; ++j) {
-    const int dj = __shfl_sync(kFull, dest, j);
-    if (j < k && lane < k) A[lane * k + dj] = row[j];
+    const int col = perm[j < k ? j : 0];
+    if (j < k && lane < k) A[my_step * k + col] = row[j];
   }
   __syncwarp();
 }
@@ -288,14 +298,17 @@ __device__ void sn_factor(T* P, int k, int r, T* Sout, T* colb, T* rowb, int* pe
   T* A = P;
   T* F12 = P + k * k;
   T* F21 = F12 + k * r;
-  if (!CTA) {  // one warp per supernode (k <= 32): rows in registers
-    if (k <= 8)
-      warp_gj<T, 8>(A, k, rowb, perm);
-    else if (k <= 16)
-      warp_gj<T, 16>(A, k, rowb, perm);
-    else
-      warp_gj<T, 32>(A, k, rowb, perm);
-  } else {  // the whole CTA: shared-memory Gauss-Jordan, rows over warps
+  if (!CTA || k <= 32) {  // one warp (k <= 32): rows in registers
+    if (!CTA || gw == 0) {
+      if (k <= 8)
+        warp_gj<T, 8>(A, k, rowb, perm);
+      else if (k <= 16)
+        warp_gj<T, 16>(A, k, rowb, perm);
+      else
+        warp_gj<T, 32>(A, k, rowb, perm);
+    }
+    group_sync<CTA, NT>();
+  } else {  // the whole CTA (k > 32): shared-memory Gauss-Jordan, rows over warps
   for (int c = 0; c < k; ++c) {
     if (gw == 0) {
       // pivot: largest |A[i][c]| over i >= c, ties to the lower row
