@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -143,13 +144,12 @@ static void free_topo(Topo& t) {
                   t.jac_ptr, t.jac_src, t.seg_ptr, t.seg_of, t.seg_idx, t.sn_k, t.sn_r, t.sn_piv, t.sn_bord,
                   t.sn_panel, t.sn_piv_ptr, t.sn_bord_ptr, t.a_pos, t.lv_sn, t.lv_schur_off,
                   t.lv_bord_off, t.st_tgt, t.st_ptr, t.st_src, t.bt_tgt, t.bt_ptr, t.bt_src,
-                  t.d_flag, t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax,
+                  t.d_lv_ptr, t.d_lv_st_ptr, t.d_lv_bt_ptr, t.d_lv_kmax,
                   t.d_blob};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < t.n_groups; ++i)
     if (t.group_nodes[i]) cudaFree(t.group_nodes[i]);
-  if (t.h_flag) cudaFreeHost(t.h_flag);
   delete[] t.h_lv_ptr;
   delete[] t.h_lv_schur_len;
   delete[] t.h_lv_bord_len;
@@ -466,7 +466,6 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
   UP(bt_tgt, d->bt_tgt, nbt);
   UP(bt_ptr, d->bt_ptr, nbt + 1);
   UP(bt_src, d->bt_src, d->bt_ptr[nbt]);
-  UP(d_flag, (const int*)nullptr, 4);
   UP(d_lv_ptr, d->lv_ptr, nl + 1);
   UP(d_lv_st_ptr, d->lv_st_ptr, nl + 1);
   UP(d_lv_bt_ptr, d->lv_bt_ptr, nl + 1);
@@ -510,13 +509,7 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
     std::vector<unsigned short> blob;
     if (build_blob(d, blob, t.blob)) st = upload(&t.d_blob, blob.data(), blob.size());
   }
-  if (st == VXG_OK) {
-    cudaError_t e = cudaMallocHost((void**)&t.h_flag, sizeof(int) * 4);
-    if (e != cudaSuccess) {
-      set_error(e);
-      st = VXG_ERR_ALLOC;
-    }
-  }
+  if (st == VXG_OK) h->graphs = new_graph_cache();
   if (st != VXG_OK) {
     free_topo(t);
     delete h;
@@ -528,6 +521,7 @@ int vxg_create(const vxg_topology_desc* d, vxg_handle** out) {
 
 int vxg_destroy(vxg_handle* h) {
   if (!h) return VXG_ERR_INVALID;
+  delete_graph_cache(h->graphs);
   free_topo(h->t);
   delete h;
   return VXG_OK;
@@ -624,15 +618,162 @@ __global__ void gdata_kernel(int B, long long nnz, int S, const int* __restrict_
   gd[gid] = -g[(long long)b * S + rows[e]] * x[(long long)b * S + indices[e]];
 }
 
-static int newton_core(const vxg_handle* h, int B, const vxg_group_params* params, int mode,
-                       double t_now, double t_prev, const double* z_prev, const double* gmin,
-                       double gmin_scalar, const vxg_newton_opts* o, double* z,
-                       int* converged, int* iters, void* factors_out, void* ws,
-                       const int* mask, cudaStream_t s) {
-  const Topo& t = h->t;
-  const int prec = o->precision;
-  Layout L = layout(t, B, prec);
-  GroupTable gt = make_table(t, params);
+// ---------------------------------------------------------------------------
+// Device-resident Newton loop (voltax/analysis.py:208-233, a lax.while_loop
+// there). One Newton solve is one CUDA graph:
+//   prologue   per-instance flags; for BE / TRAP, f and q at the previous
+//              state; the iteration counter reset;
+//   WHILE node one Newton iteration -- evaluation and stamping, residual,
+//              refactorization, solve (+ refinement), damped update with the
+//              count of still-active instances -- ending in a one-thread
+//              kernel that counts the iteration and sets the loop condition:
+//              some instance active and the limit not reached;
+//   epilogue   (adjoint only) the factors of the Jacobian at the result.
+// The host launches the graph on the caller's stream and returns; no host
+// round trip per iteration. Counters live in the caller's workspace, so
+// calls on different workspaces and streams are independent. Graphs are
+// instantiated once per distinct argument set and cached on the handle.
+__global__ void fill_int_kernel(int* p, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+__global__ void newton_continue_kernel(cudaGraphConditionalHandle h, const int* n_active,
+                                       int* iter, int max_steps) {
+  const int n = ++iter[0];
+  cudaGraphSetConditional(h, (n_active[0] != 0 && n < max_steps) ? 1u : 0u);
+}
+
+struct NewtonCall {
+  const vxg_handle* h;
+  int B;
+  const vxg_group_params* params;
+  int mode;
+  double t_now, t_prev;
+  const double* z_prev;
+  const double* gmin;
+  double gmin_scalar;
+  const vxg_newton_opts* o;
+  double* z;
+  int* converged;
+  int* iters;
+  void* factors_out;
+  void* ws;
+  const int* mask;
+};
+
+struct GraphEntry {
+  std::vector<unsigned char> key;
+  cudaGraphExec_t exec;
+  unsigned long long kernels;  // kernels of one launch, the loop body counted once
+  unsigned long long used;
+};
+
+struct GraphCache {
+  std::mutex mu;
+  std::vector<GraphEntry> entries;
+  unsigned long long tick = 0;
+};
+
+constexpr size_t kGraphCacheEntries = 16;
+
+GraphCache* new_graph_cache() { return new (std::nothrow) GraphCache(); }
+
+void delete_graph_cache(GraphCache* c) {
+  if (!c) return;
+  for (GraphEntry& e : c->entries) cudaGraphExecDestroy(e.exec);  // freed once idle
+  delete c;
+}
+
+// Every argument the graph bakes in, byte by byte.
+static std::vector<unsigned char> newton_key(const NewtonCall& a) {
+  std::vector<unsigned char> k;
+  auto put = [&](const auto& x) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&x);
+    k.insert(k.end(), p, p + sizeof(x));
+  };
+  put(a.B);
+  put(a.mode);
+  put(a.t_now);
+  put(a.t_prev);
+  put(a.z_prev);
+  put(a.gmin);
+  put(a.gmin_scalar);
+  put(a.o->max_steps);
+  put(a.o->rtol);
+  put(a.o->atol);
+  put(a.o->max_dv);
+  put(a.o->precision);
+  put(a.o->refine);
+  for (int i = 0; i < a.h->t.n_groups; ++i) {
+    put(a.params[i].params);
+    put(a.params[i].row_stride);
+    put(a.params[i].batch_stride);
+  }
+  put(a.z);
+  put(a.converged);
+  put(a.iters);
+  put(a.factors_out);
+  put(a.ws);
+  put(a.mask);
+  return k;
+}
+
+// A private stream per thread and device to record the graphs on (the
+// caller's stream may be the legacy default stream, which cannot capture).
+static cudaStream_t capture_stream() {
+  thread_local std::vector<std::pair<int, cudaStream_t>> streams;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  for (auto& p : streams)
+    if (p.first == dev) return p.second;
+  cudaStream_t cs = nullptr;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  streams.emplace_back(dev, cs);
+  return cs;
+}
+
+static thread_local int t_capturing = 0;
+static thread_local unsigned long long t_captured = 0;
+
+// Record what `body` enqueues on `cs` into a new graph (*out) or into the
+// existing graph `into` (a conditional node's body).
+template <class F>
+static int record(cudaStream_t cs, cudaGraph_t into, cudaGraph_t* out, unsigned long long* n,
+                  F&& body) {
+  cudaError_t e = into ? cudaStreamBeginCaptureToGraph(cs, into, nullptr, nullptr, 0,
+                                                       cudaStreamCaptureModeRelaxed)
+                       : cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    set_error(e);
+    return VXG_ERR_CUDA;
+  }
+  ++t_capturing;
+  t_captured = 0;
+  int st = body(cs);
+  --t_capturing;
+  *n = t_captured;
+  cudaGraph_t got = nullptr;
+  e = cudaStreamEndCapture(cs, &got);
+  if (st == VXG_OK && e != cudaSuccess) {
+    set_error(e);
+    st = VXG_ERR_CUDA;
+  }
+  if (st != VXG_OK) {
+    if (got && !into) cudaGraphDestroy(got);
+    return st;
+  }
+  if (out) *out = got;
+  return VXG_OK;
+}
+
+static int build_newton_graph(const NewtonCall& a, cudaGraphExec_t* exec,
+                              unsigned long long* kernels) {
+  const Topo& t = a.h->t;
+  const int B = a.B, prec = a.o->precision, mode = a.mode;
+  const Layout L = layout(t, B, prec);
+  const GroupTable gt = make_table(t, a.params);
+  void* ws = a.ws;
   double* cfb = at<double>(ws, L.cf);
   double* cqb = at<double>(ws, L.cq);
   double* cjb = at<double>(ws, L.cj);
@@ -648,50 +789,165 @@ static int newton_core(const vxg_handle* h, int B, const vxg_group_params* param
   void* xt = at<void>(ws, L.xt);
   double* r64 = at<double>(ws, L.r64);
   int* active = at<int>(ws, L.active);
-  int* cnt = t.d_flag;
-  const int ninst = B * t.n_seg;
-  int st = launch_newton_init(ninst, mask, active, converged, iters, s);
-  if (st) return st;
+  int* cnt = at<int>(ws, L.cnt);  // [0] active instances, [1] iterations done
   const bool dc = mode == VXG_MODE_DC;
   const double cf = mode == VXG_MODE_TRAP ? 0.5 : 1.0;
-  const double cq = dc ? 0.0 : 1.0 / (t_now - t_prev);
-  const double hstep = t_now - t_prev;
-  if (!dc) {
-    st = launch_eval(t, gt, B, z_prev, t_prev, 1.0, 0.0, mode == VXG_MODE_TRAP, true, false,
-                     cfb, cqb, cjb, s);
-    if (st) return st;
-    st = launch_gather(t, B, cfb, cqb, cjb, nullptr, 0.0, mode == VXG_MODE_TRAP ? fp : nullptr,
-                       qp, nullptr, s);
-    if (st) return st;
+  const double cq = dc ? 0.0 : 1.0 / (a.t_now - a.t_prev);
+  const double hstep = a.t_now - a.t_prev;
+  cudaStream_t cs = capture_stream();
+  if (!cs) {
+    set_error(cudaErrorUnknown);
+    return VXG_ERR_CUDA;
   }
-  for (int it = 0; it < o->max_steps; ++it) {
-    st = launch_eval(t, gt, B, z, t_now, cf, cq, true, !dc, true, cfb, cqb, cjb, s);
-    if (st) return st;
-    st = launch_gather(t, B, cfb, cqb, cjb, gmin, gmin_scalar, f, dc ? nullptr : q, data, s);
-    if (st) return st;
-    st = launch_compose(t, B, mode, hstep, z, f, q, fp, qp, gmin, gmin_scalar, rhs, s);
-    if (st) return st;
-    st = launch_factor(t, B, prec, data, fac, scratch, s);
-    if (st) return st;
-    st = launch_solve(t, B, prec, fac, data, rhs, dz, 0, prec == VXG_F32 ? o->refine : 0, xt,
-                      scratch, r64, s);
-    if (st) return st;
-    VXG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int), s));
-    st = launch_update(t, B, z, dz, active, converged, iters, o->max_dv, o->rtol, o->atol, cnt,
-                       s);
-    if (st) return st;
-    VXG_CUDA_TRY(cudaMemcpyAsync(t.h_flag, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
-    VXG_CUDA_TRY(cudaStreamSynchronize(s));
-    if (t.h_flag[0] == 0) break;
+  cudaGraph_t g = nullptr;
+  VXG_CUDA_TRY(cudaGraphCreate(&g, 0));
+  unsigned long long n_pro = 0, n_body = 0, n_epi = 0;
+  cudaGraph_t pro = nullptr;
+  int st = record(cs, nullptr, &pro, &n_pro, [&](cudaStream_t s) -> int {
+    int r = launch_newton_init(B * t.n_seg, a.mask, active, a.converged, a.iters, s);
+    if (r) return r;
+    VXG_CUDA_TRY(cudaMemsetAsync(cnt + 1, 0, sizeof(int), s));
+    if (dc) return VXG_OK;
+    r = launch_eval(t, gt, B, a.z_prev, a.t_prev, 1.0, 0.0, mode == VXG_MODE_TRAP, true, false,
+                    cfb, cqb, cjb, s);
+    if (r) return r;
+    return launch_gather(t, B, cfb, cqb, cjb, nullptr, 0.0,
+                         mode == VXG_MODE_TRAP ? fp : nullptr, qp, nullptr, s);
+  });
+  cudaGraphNode_t n0 = nullptr, n1 = nullptr, n2 = nullptr;
+  cudaGraphConditionalHandle hc = 0;
+  union ZeroedParams {  // the struct's reserved bytes must be zero
+    cudaGraphNodeParams p;
+    unsigned char raw[sizeof(cudaGraphNodeParams)];
+    ZeroedParams() { std::memset(raw, 0, sizeof(raw)); }
+  } params_buf;
+  cudaGraphNodeParams& cp = params_buf.p;
+  auto cuda_ok = [&](cudaError_t e) {
+    if (e == cudaSuccess) return true;
+    set_error(e);
+    st = VXG_ERR_CUDA;
+    return false;
+  };
+  if (st == VXG_OK && cuda_ok(cudaGraphAddChildGraphNode(&n0, g, nullptr, 0, pro)) &&
+      cuda_ok(cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault))) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cuda_ok(cudaGraphAddNode(&n1, g, &n0, nullptr, 1, &cp));
   }
-  if (factors_out) {  // factors of the Jacobian at the returned state (adjoint)
-    st = launch_eval(t, gt, B, z, t_now, cf, cq, false, false, true, cfb, cqb, cjb, s);
-    if (st) return st;
-    st = launch_gather(t, B, cfb, cqb, cjb, gmin, gmin_scalar, nullptr, nullptr, data, s);
-    if (st) return st;
-    st = launch_factor(t, B, prec, data, factors_out, scratch, s);
-    if (st) return st;
+  if (pro) cudaGraphDestroy(pro);  // the child node holds a copy
+  if (st == VXG_OK) {
+    const int max_steps = a.o->max_steps;
+    st = record(cs, cp.conditional.phGraph_out[0], nullptr, &n_body, [&](cudaStream_t s) -> int {
+      int r = launch_eval(t, gt, B, a.z, a.t_now, cf, cq, true, !dc, true, cfb, cqb, cjb, s);
+      if (r) return r;
+      r = launch_gather(t, B, cfb, cqb, cjb, a.gmin, a.gmin_scalar, f, dc ? nullptr : q, data,
+                        s);
+      if (r) return r;
+      r = launch_compose(t, B, mode, hstep, a.z, f, q, fp, qp, a.gmin, a.gmin_scalar, rhs, s);
+      if (r) return r;
+      r = launch_factor(t, B, prec, data, fac, scratch, s);
+      if (r) return r;
+      r = launch_solve(t, B, prec, fac, data, rhs, dz, 0, prec == VXG_F32 ? a.o->refine : 0,
+                       xt, scratch, r64, s);
+      if (r) return r;
+      VXG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int), s));
+      r = launch_update(t, B, a.z, dz, active, a.converged, a.iters, a.o->max_dv, a.o->rtol,
+                        a.o->atol, cnt, s);
+      if (r) return r;
+      newton_continue_kernel<<<1, 1, 0, s>>>(hc, cnt, cnt + 1, max_steps);
+      VXG_LAUNCHED();
+      return VXG_OK;
+    });
   }
+  if (st == VXG_OK && a.factors_out) {  // factors of the Jacobian at the returned state
+    cudaGraph_t epi = nullptr;
+    st = record(cs, nullptr, &epi, &n_epi, [&](cudaStream_t s) -> int {
+      int r = launch_eval(t, gt, B, a.z, a.t_now, cf, cq, false, false, true, cfb, cqb, cjb, s);
+      if (r) return r;
+      r = launch_gather(t, B, cfb, cqb, cjb, a.gmin, a.gmin_scalar, nullptr, nullptr, data, s);
+      if (r) return r;
+      return launch_factor(t, B, prec, data, a.factors_out, scratch, s);
+    });
+    if (st == VXG_OK) {
+      cuda_ok(cudaGraphAddChildGraphNode(&n2, g, &n1, 1, epi));
+      cudaGraphDestroy(epi);
+    }
+  }
+  if (st == VXG_OK) cuda_ok(cudaGraphInstantiate(exec, g, 0));
+  cudaGraphDestroy(g);
+  *kernels = n_pro + n_body + n_epi;
+  return st;
+}
+
+static int newton_core(const NewtonCall& a, cudaStream_t s, bool cache) {
+  const Topo& t = a.h->t;
+  if (a.o->max_steps == 0) {  // no iteration: flags, and the factors if asked
+    const Layout L = layout(t, a.B, a.o->precision);
+    int st = launch_newton_init(a.B * t.n_seg, a.mask, at<int>(a.ws, L.active), a.converged,
+                                a.iters, s);
+    if (st || !a.factors_out) return st;
+    const GroupTable gt = make_table(t, a.params);
+    const bool dc = a.mode == VXG_MODE_DC;
+    const double cf = a.mode == VXG_MODE_TRAP ? 0.5 : 1.0;
+    const double cq = dc ? 0.0 : 1.0 / (a.t_now - a.t_prev);
+    st = launch_eval(t, gt, a.B, a.z, a.t_now, cf, cq, false, false, true,
+                     at<double>(a.ws, L.cf), at<double>(a.ws, L.cq), at<double>(a.ws, L.cj), s);
+    if (st) return st;
+    st = launch_gather(t, a.B, at<double>(a.ws, L.cf), at<double>(a.ws, L.cq),
+                       at<double>(a.ws, L.cj), a.gmin, a.gmin_scalar, nullptr, nullptr,
+                       at<double>(a.ws, L.data), s);
+    if (st) return st;
+    return launch_factor(t, a.B, a.o->precision, at<double>(a.ws, L.data), a.factors_out,
+                         at<void>(a.ws, L.scratch), s);
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VXG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone) {  // a graph with a loop cannot be nested
+    std::snprintf(last_error_buffer(), 256,
+                  "vxg_newton: the caller's stream is being captured; the Newton loop is "
+                  "itself a graph with a conditional node and cannot be nested");
+    return VXG_ERR_INVALID;
+  }
+  GraphCache* gc = a.h->graphs;
+  if (!cache || !gc) {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long kernels = 0;
+    int st = build_newton_graph(a, &exec, &kernels);
+    if (st) return st;
+    const cudaError_t e = cudaGraphLaunch(exec, s);
+    cudaGraphExecDestroy(exec);  // freed once the launch completes
+    if (e != cudaSuccess) {
+      set_error(e);
+      return VXG_ERR_CUDA;
+    }
+    count_launches(kernels);
+    return VXG_OK;
+  }
+  std::vector<unsigned char> key = newton_key(a);
+  std::lock_guard<std::mutex> lock(gc->mu);
+  GraphEntry* hit = nullptr;
+  for (GraphEntry& e : gc->entries)
+    if (e.key == key) hit = &e;
+  if (!hit) {
+    GraphEntry e{std::move(key), nullptr, 0, 0};
+    int st = build_newton_graph(a, &e.exec, &e.kernels);
+    if (st) return st;
+    if (gc->entries.size() >= kGraphCacheEntries) {  // evict the least recently used
+      auto old = std::min_element(gc->entries.begin(), gc->entries.end(),
+                                  [](const GraphEntry& x, const GraphEntry& y) {
+                                    return x.used < y.used;
+                                  });
+      cudaGraphExecDestroy(old->exec);
+      gc->entries.erase(old);
+    }
+    gc->entries.push_back(std::move(e));
+    hit = &gc->entries.back();
+  }
+  hit->used = ++gc->tick;
+  VXG_CUDA_TRY(cudaGraphLaunch(hit->exec, s));
+  count_launches(hit->kernels);
   return VXG_OK;
 }
 
@@ -723,8 +979,9 @@ int vxg_newton(const vxg_handle* h, int32_t batch, const vxg_group_params* param
   if (!h || batch <= 0 || !params || !z || !converged || !iters || !workspace ||
       !opts_ok(opts) || mode < 0 || mode > 2 || (mode != VXG_MODE_DC && !z_prev))
     return VXG_ERR_INVALID;
-  return newton_core(h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts, z,
-                     converged, iters, factors, workspace, nullptr, (cudaStream_t)stream);
+  const NewtonCall a{h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts,
+                     z, converged, iters, factors, workspace, nullptr};
+  return newton_core(a, (cudaStream_t)stream, true);
 }
 
 int vxg_newton_masked(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
@@ -735,8 +992,9 @@ int vxg_newton_masked(const vxg_handle* h, int32_t batch, const vxg_group_params
   if (!h || batch <= 0 || !params || !z || !converged || !iters || !workspace ||
       !opts_ok(opts) || mode < 0 || mode > 2 || (mode != VXG_MODE_DC && !z_prev))
     return VXG_ERR_INVALID;
-  return newton_core(h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts, z,
-                     converged, iters, nullptr, workspace, mask, (cudaStream_t)stream);
+  const NewtonCall a{h, batch, params, mode, t_now, t_prev, z_prev, gmin, gmin_scalar, opts,
+                     z, converged, iters, nullptr, workspace, mask};
+  return newton_core(a, (cudaStream_t)stream, true);
 }
 
 int vxg_transient(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
@@ -750,21 +1008,20 @@ int vxg_transient(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
   const size_t nS = (size_t)batch * h->t.S;
   const int ninst = batch * h->t.n_seg;
   VXG_CUDA_TRY(cudaMemcpyAsync(z_out, z0, sizeof(double) * nS, cudaMemcpyDeviceToDevice, s));
-  std::vector<int> ones(ninst, 1), zeros(ninst, 0);
-  VXG_CUDA_TRY(cudaMemcpyAsync(converged, ones.data(), sizeof(int) * ninst,
-                               cudaMemcpyHostToDevice, s));
-  VXG_CUDA_TRY(cudaMemcpyAsync(iters, zeros.data(), sizeof(int) * ninst,
-                               cudaMemcpyHostToDevice, s));
+  // row 0 is the initial state: converged, no iterations
+  fill_int_kernel<<<(ninst + 255) / 256, 256, 0, s>>>(converged, ninst, 1);
+  VXG_LAUNCHED();
+  VXG_CUDA_TRY(cudaMemsetAsync(iters, 0, sizeof(int) * ninst, s));
   for (int n = 1; n < n_t; ++n) {
     double* prev = z_out + (size_t)(n - 1) * nS;
     double* cur = z_out + (size_t)n * nS;
     VXG_CUDA_TRY(cudaMemcpyAsync(cur, prev, sizeof(double) * nS, cudaMemcpyDeviceToDevice, s));
-    int st = newton_core(h, batch, params, mode, ts[n], ts[n - 1], prev, nullptr, gmin_scalar,
-                         opts, cur, converged + (size_t)n * ninst, iters + (size_t)n * ninst,
-                         nullptr, workspace, nullptr, s);
+    const NewtonCall a{h, batch, params, mode, ts[n], ts[n - 1], prev, nullptr, gmin_scalar,
+                       opts, cur, converged + (size_t)n * ninst, iters + (size_t)n * ninst,
+                       nullptr, workspace, nullptr};
+    int st = newton_core(a, s, false);  // one graph per step, not cached
     if (st) return st;
   }
-  VXG_CUDA_TRY(cudaStreamSynchronize(s));
   return VXG_OK;
 }
 
@@ -780,7 +1037,14 @@ int vxg_param_vjp(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
 
 namespace vxg {
 static std::atomic<unsigned long long> g_launches{0};
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// Launches recorded into a graph are counted when the graph is launched.
+void count_launch() {
+  if (t_capturing)
+    ++t_captured;
+  else
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 }  // namespace vxg
 
 extern "C" uint64_t vxg_launch_count(void) { return vxg::g_launches.load(); }

@@ -79,9 +79,6 @@ struct Topo {
   long long max_schur, max_bord;  // largest per-level scratch
   int kmax, rmax;
   int max_m;  // largest local block (terminals + internals) over the groups
-  // pinned host word for loop control
-  int* h_flag;
-  int* d_flag;
   // 16-bit tables of the fused kernel (null when some index does not fit)
   unsigned short* d_blob;
   Blob blob;
@@ -89,13 +86,21 @@ struct Topo {
 
 }  // namespace vxg
 
+namespace vxg {
+struct GraphCache;  // instantiated Newton-loop graphs of a handle (capi.cu)
+}
+
 struct vxg_handle {
   vxg::Topo t;
+  vxg::GraphCache* graphs = nullptr;
 };
 
 namespace vxg {
 void count_launch();
-char* last_error_buffer();  // this thread's vxg_last_error text (256 bytes)
+void count_launches(unsigned long long n);
+char* last_error_buffer();
+GraphCache* new_graph_cache();
+void delete_graph_cache(GraphCache* c);  // this thread's vxg_last_error text (256 bytes)
 }
 
 // Count one kernel launch and surface launch errors.
