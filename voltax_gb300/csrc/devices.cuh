@@ -83,6 +83,90 @@ namespace vxg {
 // JT (double for the plain form, float for the FP32-factor form, whose
 // Jacobian only feeds the FP32 factorization and the refinement matrix).
 // --------------------------------------------------------------------------
+// The quantities the EKV local Jacobian is built from, in the Jacobian's
+// type: derivatives of the forward/reverse arguments, the softplus values
+// and sigmoids, the drain-current factors, and the charge-sheet terms.
+template <typename JT>
+struct EkvTerms {
+  JT af_g, af_s, af_b;  // d af / d (vg, vs, vb); ar has the same with vd for vs
+  JT dif, dir;          // d i_f / d af, d i_r / d ar
+  JT isp, mf, dI, dsa, lam;
+  JT xf, xr, s, nd, ns, sc, kb, cox, cw;
+};
+
+// Local Jacobian of one EKV device (voltax/elements/mosfet.py:171-205 by
+// the chain rule), J[i][j] = cf dI_i/du_j + cq dQ_i/du_j in the device's
+// mirrored n-frame; the sign flips of a PMOS cancel in J.
+template <typename JT>
+__device__ __forceinline__ void ekv_jac_write(const EkvTerms<JT>& e, double cf, double cq,
+                                              bool need_i, bool need_q, int n, int d, JT* jo) {
+  JT ji[4] = {JT(0), JT(0), JT(0), JT(0)};
+  if (need_i && cf != 0.0) {
+    ji[0] = e.isp * ((-e.dir * e.af_s) * e.mf + e.dI * e.lam * e.dsa);
+    ji[1] = e.isp * ((e.dif - e.dir) * e.af_g * e.mf);
+    ji[2] = e.isp * ((e.dif * e.af_s) * e.mf - e.dI * e.lam * e.dsa);
+    ji[3] = e.isp * ((e.dif - e.dir) * e.af_b * e.mf);
+  }
+  JT dq0[4] = {JT(0), JT(0), JT(0), JT(0)}, dq1[4] = {JT(0), JT(0), JT(0), JT(0)};
+  JT dq2[4] = {JT(0), JT(0), JT(0), JT(0)}, dq3[4] = {JT(0), JT(0), JT(0), JT(0)};
+  if (need_q && cq != 0.0) {
+    const JT fx = e.xf, rx = e.xr, ss = e.s, s3 = ss * ss * ss;
+    const JT gd_f = ((JT(6) * rx * rx + JT(8) * rx * fx + JT(6) * fx * fx) * ss - JT(2) * e.nd) / s3;
+    const JT gd_r = ((JT(9) * rx * rx + JT(12) * rx * fx + JT(4) * fx * fx) * ss - JT(2) * e.nd) / s3;
+    const JT gs_f = ((JT(9) * fx * fx + JT(12) * fx * rx + JT(4) * rx * rx) * ss - JT(2) * e.ns) / s3;
+    const JT gs_r = ((JT(6) * fx * fx + JT(8) * fx * rx + JT(6) * rx * rx) * ss - JT(2) * e.ns) / s3;
+    const JT dxf_da = e.dif / (JT(2) * fx), dxr_da = e.dir / (JT(2) * rx);
+    const JT c415 = JT(4) / JT(15);
+    const JT dafk[4] = {JT(0), e.af_g, e.af_s, e.af_b};
+    const JT dark[4] = {e.af_s, e.af_g, JT(0), e.af_b};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const JT dxf = dxf_da * dafk[k], dxr = dxr_da * dark[k];
+      const JT dqd = -e.sc * c415 * (gd_f * dxf + gd_r * dxr);
+      const JT dqs = -e.sc * c415 * (gs_f * dxf + gs_r * dxr);
+      const JT dqi = dqd + dqs;
+      const JT dvgb = (k == 1 ? JT(1) : JT(0)) - (k == 3 ? JT(1) : JT(0));
+      const JT dqb = e.kb * (e.cox * dvgb + dqi);
+      const JT dqg = -(dqi + dqb);
+      const JT dgs = e.cw * ((k == 1 ? JT(1) : JT(0)) - (k == 2 ? JT(1) : JT(0)));
+      const JT dgd = e.cw * ((k == 1 ? JT(1) : JT(0)) - (k == 0 ? JT(1) : JT(0)));
+      dq0[k] = dqd - dgd;
+      dq1[k] = dqg + (dgs + dgd);
+      dq2[k] = dqs - dgs;
+      dq3[k] = dqb;
+    }
+  }
+  const JT cfj = (JT)cf, cqj = (JT)cq;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    JT r0 = cf != 0.0 ? cfj * ji[j] : JT(0);
+    JT r2 = cf != 0.0 ? cfj * -ji[j] : JT(0);
+    JT r1 = JT(0), r3 = JT(0);
+    if (cq != 0.0) {
+      r0 = r0 + cqj * dq0[j];
+      r1 = r1 + cqj * dq1[j];
+      r2 = r2 + cqj * dq2[j];
+      r3 = r3 + cqj * dq3[j];
+    }
+    jo[(0 * 4 + j) * n + d] = r0;
+    jo[(1 * 4 + j) * n + d] = r1;
+    jo[(2 * 4 + j) * n + d] = r2;
+    jo[(3 * 4 + j) * n + d] = r3;
+  }
+}
+
+// Charge-sheet terms of the EKV charges from the normalised currents.
+template <typename X>
+__device__ __forceinline__ void ekv_charge_terms(X i_f, X i_r, X* xf, X* xr, X* s, X* nd,
+                                                 X* ns) {
+  *xf = sqrt(X(0.25) + i_f);
+  *xr = sqrt(X(0.25) + i_r);
+  *s = *xf + *xr;
+  const X xf2 = *xf * *xf, xr2 = *xr * *xr;
+  *nd = xr2 * (X(3) * *xr + X(6) * *xf) + xf2 * (X(4) * *xr + X(2) * *xf);
+  *ns = xf2 * (X(3) * *xf + X(6) * *xr) + xr2 * (X(4) * *xf + X(2) * *xr);
+}
+
 template <typename JT>
 __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const double* u,
                                         double cf, double cq, bool wf, bool wq, bool wj,
@@ -90,7 +174,7 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
   const int n = g.n;
   const bool neg = prm(g, 0, b, d) < 0.0;  // PMOS: evaluate in the mirrored n-frame
   const double i_spec = prm(g, 1, b, d), vth = prm(g, 2, b, d), dvth = prm(g, 3, b, d);
-  const double nn = prm(g, 4, b, d), lam = prm(g, 6, b, d), c_ox = prm(g, 7, b, d);
+  const double lam = prm(g, 6, b, d), c_ox = prm(g, 7, b, d);
   const double cov_w = prm(g, 8, b, d), inv_n = prm(g, 9, b, d), inv_2vt = prm(g, 10, b, d);
   const double scale = prm(g, 11, b, d), kb = prm(g, 12, b, d);
   const double vd = neg ? -u[0] : u[0], vg = neg ? -u[1] : u[1];
@@ -118,14 +202,7 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
     fo[3 * n + d] = 0.0;
   }
   double xf = 0.0, xr = 0.0, s = 1.0, nd = 0.0, ns = 0.0;
-  if (need_q) {
-    xf = sqrt(0.25 + i_f);
-    xr = sqrt(0.25 + i_r);
-    s = xf + xr;
-    const double xf2 = xf * xf, xr2 = xr * xr;
-    nd = xr2 * (3 * xr + 6 * xf) + xf2 * (4 * xr + 2 * xf);
-    ns = xf2 * (3 * xf + 6 * xr) + xr2 * (4 * xf + 2 * xr);
-  }
+  if (need_q) ekv_charge_terms(i_f, i_r, &xf, &xr, &s, &nd, &ns);
   if (wq) {
     const double w415 = (4.0 / 15.0) / (s * s);
     const double q_d = -scale * (w415 * nd - 0.5);
@@ -141,70 +218,76 @@ __device__ __forceinline__ void ekv_soa(const GroupDev& g, int b, int d, const d
     qo[3 * n + d] = neg ? -q_b : q_b;
   }
   if (!wj) return;
-  // derivatives in JT
-  const JT tv2 = (JT)inv_2vt;
-  const JT g1 = (JT)inv_n;
-  const JT af_g = g1 * tv2, af_s = -tv2, af_b = (JT(1) - g1) * tv2;
+  EkvTerms<JT> e;
+  const JT tv2 = (JT)inv_2vt, g1 = (JT)inv_n;
+  e.af_g = g1 * tv2;
+  e.af_s = -tv2;
+  e.af_b = (JT(1) - g1) * tv2;
   const JT sgf = af >= 0.0 ? JT(1) / (JT(1) + (JT)ef) : (JT)ef / (JT(1) + (JT)ef);
   const JT sgr = ar >= 0.0 ? JT(1) / (JT(1) + (JT)er) : (JT)er / (JT(1) + (JT)er);
-  const JT dif = JT(2) * (JT)spf * sgf, dir = JT(2) * (JT)spr * sgr;
-  const JT cfj = (JT)cf, cqj = (JT)cq;
-  JT ji[4] = {JT(0), JT(0), JT(0), JT(0)};
-  if (need_i && cf != 0.0) {
-    const JT isp = (JT)i_spec, mf = (JT)mfac, dI = (JT)(i_f - i_r);
-    const JT dsa = (JT)vds / (JT)root, lmj = (JT)lam;
-    ji[0] = isp * ((-dir * af_s) * mf + dI * lmj * dsa);
-    ji[1] = isp * ((dif - dir) * af_g * mf);
-    ji[2] = isp * ((dif * af_s) * mf - dI * lmj * dsa);
-    ji[3] = isp * ((dif - dir) * af_b * mf);
-  }
-  JT dq0[4] = {JT(0), JT(0), JT(0), JT(0)}, dq1[4] = {JT(0), JT(0), JT(0), JT(0)};
-  JT dq2[4] = {JT(0), JT(0), JT(0), JT(0)}, dq3[4] = {JT(0), JT(0), JT(0), JT(0)};
-  if (need_q && cq != 0.0) {
-    const JT fx = (JT)xf, rx = (JT)xr, ss = (JT)s, s3 = ss * ss * ss;
-    const JT ndj = (JT)nd, nsj = (JT)ns, sc = (JT)scale, kbj = (JT)kb, cox = (JT)c_ox;
-    const JT cw = (JT)cov_w;
-    const JT gd_f = ((JT(6) * rx * rx + JT(8) * rx * fx + JT(6) * fx * fx) * ss - JT(2) * ndj) / s3;
-    const JT gd_r = ((JT(9) * rx * rx + JT(12) * rx * fx + JT(4) * fx * fx) * ss - JT(2) * ndj) / s3;
-    const JT gs_f = ((JT(9) * fx * fx + JT(12) * fx * rx + JT(4) * rx * rx) * ss - JT(2) * nsj) / s3;
-    const JT gs_r = ((JT(6) * fx * fx + JT(8) * fx * rx + JT(6) * rx * rx) * ss - JT(2) * nsj) / s3;
-    const JT dxf_da = dif / (JT(2) * fx), dxr_da = dir / (JT(2) * rx);
-    const JT c415 = JT(4) / JT(15);
-    const JT dafk[4] = {JT(0), af_g, af_s, af_b};
-    const JT dark[4] = {af_s, af_g, JT(0), af_b};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const JT dxf = dxf_da * dafk[k], dxr = dxr_da * dark[k];
-      const JT dqd = -sc * c415 * (gd_f * dxf + gd_r * dxr);
-      const JT dqs = -sc * c415 * (gs_f * dxf + gs_r * dxr);
-      const JT dqi = dqd + dqs;
-      const JT dvgb = (k == 1 ? JT(1) : JT(0)) - (k == 3 ? JT(1) : JT(0));
-      const JT dqb = kbj * (cox * dvgb + dqi);
-      const JT dqg = -(dqi + dqb);
-      const JT dgs = cw * ((k == 1 ? JT(1) : JT(0)) - (k == 2 ? JT(1) : JT(0)));
-      const JT dgd = cw * ((k == 1 ? JT(1) : JT(0)) - (k == 0 ? JT(1) : JT(0)));
-      dq0[k] = dqd - dgd;
-      dq1[k] = dqg + (dgs + dgd);
-      dq2[k] = dqs - dgs;
-      dq3[k] = dqb;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    JT r0 = cf != 0.0 ? cfj * ji[j] : JT(0);
-    JT r2 = cf != 0.0 ? cfj * -ji[j] : JT(0);
-    JT r1 = JT(0), r3 = JT(0);
-    if (cq != 0.0) {
-      r0 = r0 + cqj * dq0[j];
-      r1 = r1 + cqj * dq1[j];
-      r2 = r2 + cqj * dq2[j];
-      r3 = r3 + cqj * dq3[j];
-    }
-    jo[(0 * 4 + j) * n + d] = r0;
-    jo[(1 * 4 + j) * n + d] = r1;
-    jo[(2 * 4 + j) * n + d] = r2;
-    jo[(3 * 4 + j) * n + d] = r3;
-  }
+  e.dif = JT(2) * (JT)spf * sgf;
+  e.dir = JT(2) * (JT)spr * sgr;
+  e.isp = (JT)i_spec;
+  e.mf = (JT)mfac;
+  e.dI = (JT)(i_f - i_r);
+  e.dsa = need_i ? (JT)vds / (JT)root : JT(0);
+  e.lam = (JT)lam;
+  e.xf = (JT)xf;
+  e.xr = (JT)xr;
+  e.s = (JT)s;
+  e.nd = (JT)nd;
+  e.ns = (JT)ns;
+  e.sc = (JT)scale;
+  e.kb = (JT)kb;
+  e.cox = (JT)c_ox;
+  e.cw = (JT)cov_w;
+  ekv_jac_write(e, cf, cq, need_i, need_q, n, d, jo);
+}
+
+// The EKV local Jacobian alone, from FP32 intermediates: the chosen form's
+// second evaluation pass (its FP64 currents and charges come from ekv_soa
+// with wj = false). Only the bias differences are formed in FP64; the
+// exponentials, logarithms and roots run on the FP32 pipes. The Jacobian
+// only steers Newton (the residual stays FP64), so its FP32 rounding changes
+// at most the convergence rate, which the FP32 factorization already sets.
+__device__ __forceinline__ void ekv_jac_f32(const GroupDev& g, int b, int d, const double* u,
+                                            double cf, double cq, float* jo) {
+  const int n = g.n;
+  const bool neg = prm(g, 0, b, d) < 0.0;
+  const double vd = neg ? -u[0] : u[0], vg = neg ? -u[1] : u[1];
+  const double vs = neg ? -u[2] : u[2], vb = neg ? -u[3] : u[3];
+  const double inv_n = prm(g, 9, b, d), inv_2vt = prm(g, 10, b, d);
+  const double vp = (vg - vb - prm(g, 2, b, d) - prm(g, 3, b, d)) * inv_n;
+  const float af = (float)((vp - (vs - vb)) * inv_2vt);
+  const float ar = (float)((vp - (vd - vb)) * inv_2vt);
+  const float vds = (float)(vd - vs);
+  const bool need_i = cf != 0.0, need_q = cq != 0.0;
+  const float ef = __expf(-fabsf(af)), er = __expf(-fabsf(ar));
+  const float spf = fmaxf(af, 0.0f) + log1pf(ef), spr = fmaxf(ar, 0.0f) + log1pf(er);
+  const float i_f = spf * spf, i_r = spr * spr;
+  EkvTerms<float> e;
+  const float tv2 = (float)inv_2vt, g1 = (float)inv_n;
+  e.af_g = g1 * tv2;
+  e.af_s = -tv2;
+  e.af_b = (1.0f - g1) * tv2;
+  const float sgf = af >= 0.0f ? 1.0f / (1.0f + ef) : ef / (1.0f + ef);
+  const float sgr = ar >= 0.0f ? 1.0f / (1.0f + er) : er / (1.0f + er);
+  e.dif = 2.0f * spf * sgf;
+  e.dir = 2.0f * spr * sgr;
+  e.isp = (float)prm(g, 1, b, d);
+  e.lam = (float)prm(g, 6, b, d);
+  const float root = sqrtf(vds * vds + 1e-6f);
+  e.mf = 1.0f + e.lam * (root - 1e-3f);
+  e.dI = i_f - i_r;
+  e.dsa = vds / root;
+  e.xf = e.xr = e.s = 1.0f;
+  e.nd = e.ns = 0.0f;
+  if (need_q) ekv_charge_terms(i_f, i_r, &e.xf, &e.xr, &e.s, &e.nd, &e.ns);
+  e.sc = (float)prm(g, 11, b, d);
+  e.kb = (float)prm(g, 12, b, d);
+  e.cox = (float)prm(g, 7, b, d);
+  e.cw = (float)prm(g, 8, b, d);
+  ekv_jac_write(e, cf, cq, need_i, need_q, n, d, jo);
 }
 
 // Level 1 (Shichman-Hodges) MOSFET, smoothed (voltax/elements/mosfet.py:208-257):

@@ -74,9 +74,16 @@ __host__ __device__ inline int sbuf_records(int nw) { return 32 * nw > kCtaK ? 3
 
 // Shared-memory layout of one instance.
 struct FusedLayout {
-  size_t blob, z, zp, fp, qp, f, q, rhs, dz, res, data, cf, cq, cj, work, scr, xt, red, prof, sbuf,
-      total;
+  size_t blob, z, fp, qp, f, q, rhs, dz, data, cf, cq, cj, work, scr, xt, red, prof, sbuf, total;
 };
+
+// The chosen form (FP32 panels) evaluates its devices in two passes -- FP64
+// currents and charges, then the FP32 local Jacobians -- so its Jacobian
+// contributions reuse the storage of the current and charge contributions.
+template <typename T>
+__host__ __device__ constexpr bool split_eval() {
+  return sizeof(T) == sizeof(float);
+}
 
 // Shared memory of one instance; a warp-owned instance (warp_group) needs
 // only one warp's column/row buffers and pivot records.
@@ -103,24 +110,25 @@ __host__ __device__ inline FusedLayout fused_layout(int S, int nnz, int n_res, i
   };
   const size_t d = sizeof(double);
   L.z = take(d * S);
-  L.zp = take(d * S);
   L.fp = take(d * S);
   L.qp = take(d * S);
   L.f = take(d * S);
   L.q = take(d * S);
   L.rhs = take(d * S);
   L.dz = take(d * S);
-  L.res = take(d * S);
   L.data = take(sizeof(T) * nnz);
   // The device contributions (written by the evaluation, read by the
   // assembly) and the panels, Schur scratch and solve vector (written after
   // the assembly, read until the solve ends) are never live at the same
-  // time, so they share one region.
+  // time, so they share one region; so do the current/charge and the
+  // Jacobian contributions when they are evaluated in two passes.
   const size_t shared_at = o;
   L.cf = take(d * n_res);
   L.cq = take(d * n_res);
+  size_t contrib_end = o;
+  if (split_eval<T>()) o = shared_at;
   L.cj = take(sizeof(T) * n_jac);
-  const size_t contrib_end = o;
+  if (o > contrib_end) contrib_end = o;
   o = shared_at;
   L.work = take(sizeof(T) * work);
   L.scr = take(sizeof(T) * (max_scr > 0 ? max_scr : 1));
@@ -566,7 +574,7 @@ struct Instance {
 
   const FusedArgs& A;
   int b;
-  double *z, *zp, *fp, *qp, *f, *q, *rhs, *dz, *res, *cf, *cq, *red;
+  double *z, *fp, *qp, *f, *q, *rhs, *dz, *cf, *cq, *red;
   T *data, *cj, *work, *scr, *xt, *sbuf;
   int* ibuf;
   long long* prof;  // per-instance phase cycles (shared memory), used when A.phase_clk
@@ -693,14 +701,67 @@ struct Instance {
     }
   }
 
-  // CSR values (+gmin), panels and rhs = -r. On the first iteration of a
-  // time step the state is still z_prev, so q(z_prev) is taken from this
-  // evaluation instead of a separate one.
-  __device__ void assemble_system(int mode, double gmin, double h, bool first) {
+  // The Jacobian contributions alone (the chosen form's second pass): EKV
+  // devices from FP32 intermediates, the other kinds from their ordinary
+  // evaluation with the value outputs switched off.
+  __device__ void eval_jac(const double* zz, double t, double cfc, double cqc) {
+    const GroupTable& gt = A.gt;
+    const u16* nodes = sec(B_NODES);
+    for (int flat = tid(); flat < gt.n_dev; flat += GT) {
+      int gi = 0;
+      while (gi + 1 < gt.n_groups && gt.g[gi + 1].dev_base <= flat) ++gi;
+      const GroupDev& g = gt.g[gi];
+      const int d = flat - (int)g.dev_base;
+      const u16* nd = nodes + A.bo.node_off[gi] + d * g.T;
+      double u[kFusedMaxM];
+#pragma unroll
+      for (int i = 0; i < kFusedMaxM; ++i) {
+        if (i < g.T) {
+          const u16 node = nd[i];
+          u[i] = node != 0xFFFF ? zz[node] : 0.0;
+        } else if (i < g.m) {
+          u[i] = zz[g.int_offset + d * g.K + (i - g.T)];
+        } else {
+          u[i] = 0.0;
+        }
+      }
+      if constexpr (sizeof(T) == sizeof(float)) {
+        if (g.kind == VXG_KIND_EKV) {
+          ekv_jac_f32(g, b, d, u, cfc, cqc, cj + g.jac_base);
+          continue;
+        }
+      }
+      eval_soa<T>(g, b, d, u, t, cfc, cqc, false, false, true, nullptr, nullptr,
+                  cj + g.jac_base);
+    }
+  }
+
+  // Residual rows f (and q), the captured q(z_prev) and rhs = -r. On the
+  // first iteration of a time step the state is still z_prev, so q(z_prev)
+  // is taken from this evaluation instead of a separate one.
+  __device__ void assemble_residual(int mode, double gmin, double h, bool first) {
     assemble_res(f, mode == VXG_MODE_DC ? nullptr : q);
-    // Jacobian values in the panel type: FP64 in the plain form; FP32 in the
-    // chosen form, where they feed the FP32 factorization and the FP64
-    // refinement residual rhs - J dz (accumulated in FP64)
+    sync();
+    for (int i = tid(); i < A.S; i += GT) {
+      if (first && mode != VXG_MODE_DC) qp[i] = q[i];
+      const double gm = i < A.nv ? gmin * z[i] : 0.0;
+      double r;
+      if (mode == VXG_MODE_DC)
+        r = f[i] + gm;
+      else if (mode == VXG_MODE_BE)
+        r = (q[i] - qp[i]) / h + f[i] + gm;
+      else
+        r = (q[i] - qp[i]) / h + 0.5 * (f[i] + fp[i]) + gm;
+      rhs[i] = -r;
+    }
+    sync();
+  }
+
+  // CSR values (+gmin) and the panels. Jacobian values in the panel type:
+  // FP64 in the plain form; FP32 in the chosen form, where they feed the
+  // FP32 factorization and the FP64 refinement residual rhs - J dz
+  // (accumulated in FP64).
+  __device__ void assemble_jacobian(double gmin) {
     const u16* jptr = sec(B_JAC_PTR);
     const u16* jsrc = sec(B_JAC_SRC);
     const u16* rows = sec(B_ROWS);
@@ -726,25 +787,12 @@ struct Instance {
         if (lane == 0) data[e] = acc;
       }
     }
-    if (first && mode != VXG_MODE_DC)
-      for (int i = tid(); i < A.S; i += GT) qp[i] = q[i];
     sync();
     // the panels overlay the contributions consumed above
     for (int i = tid(); i < A.work; i += GT) work[i] = T(0);
     sync();
     const u16* apos = sec(B_APOS);
     for (int e = tid(); e < A.nnz; e += GT) work[apos[e]] = data[e];
-    for (int i = tid(); i < A.S; i += GT) {
-      const double gm = i < A.nv ? gmin * z[i] : 0.0;
-      double r;
-      if (mode == VXG_MODE_DC)
-        r = f[i] + gm;
-      else if (mode == VXG_MODE_BE)
-        r = (q[i] - qp[i]) / h + f[i] + gm;
-      else
-        r = (q[i] - qp[i]) / h + 0.5 * (f[i] + fp[i]) + gm;
-      rhs[i] = -r;
-    }
     sync();
   }
 
@@ -1018,10 +1066,22 @@ struct Instance {
     int done = 0, it = 0;
     long long t0 = A.phase_clk ? clock64() : 0;
     while (it < max_steps && !done) {
-      eval(z, t, cfc, cqc, true, !dc, true);
-      sync();
-      mark(PH_EVAL, &t0);
-      assemble_system(mode, gmin, h, it == 0);
+      if constexpr (split_eval<T>()) {  // FP64 values, then the FP32 Jacobian
+        eval(z, t, cfc, cqc, true, !dc, false);
+        sync();
+        mark(PH_EVAL, &t0);
+        assemble_residual(mode, gmin, h, it == 0);
+        mark(PH_ASSEMBLE, &t0);
+        eval_jac(z, t, cfc, cqc);
+        sync();
+        mark(PH_EVAL, &t0);
+      } else {
+        eval(z, t, cfc, cqc, true, !dc, true);
+        sync();
+        mark(PH_EVAL, &t0);
+        assemble_residual(mode, gmin, h, it == 0);
+      }
+      assemble_jacobian(gmin);
       mark(PH_ASSEMBLE, &t0);
       factor();
       mark(PH_FACTOR, &t0);
@@ -1049,14 +1109,12 @@ __device__ __forceinline__ void bind(Instance<T, NT, kWarp>& I, unsigned char* b
                                      const FusedLayout& L, const u16* tables) {
   I.tb = tables;
   I.z = reinterpret_cast<double*>(base + L.z);
-  I.zp = reinterpret_cast<double*>(base + L.zp);
   I.fp = reinterpret_cast<double*>(base + L.fp);
   I.qp = reinterpret_cast<double*>(base + L.qp);
   I.f = reinterpret_cast<double*>(base + L.f);
   I.q = reinterpret_cast<double*>(base + L.q);
   I.rhs = reinterpret_cast<double*>(base + L.rhs);
   I.dz = reinterpret_cast<double*>(base + L.dz);
-  I.res = reinterpret_cast<double*>(base + L.res);
   I.data = reinterpret_cast<T*>(base + L.data);
   I.cf = reinterpret_cast<double*>(base + L.cf);
   I.cq = reinterpret_cast<double*>(base + L.cq);
