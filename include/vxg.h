@@ -307,7 +307,9 @@ int vxg_fused_set_profile(int64_t* cycles);
  * element size exceeds 8 MiB. Every GPU that loads the library holds the
  * 8 MiB until exit. All calls share the array: calls that overlap on a GPU
  * race, so serialise them. The first call on a device looks up the array's
- * address; make it before any stream capture. */
+ * address; make it before any stream capture. The address is kept per
+ * device and context: after a cudaDeviceReset the next call looks it up
+ * again, so it too must precede any capture. */
 int vxg_factor_static(const vxg_handle* h, int32_t batch, int32_t precision,
                       const double* data, void* factors, void* stream);
 

@@ -21,8 +21,11 @@
 //    on a GPU (different streams or threads) race on it and corrupt each
 //    other's factors. Serialise them;
 //  * the first call on a device looks up the array's device address once
-//    (cudaGetSymbolAddress with that device current) and caches it. Make
-//    that first call before any stream capture;
+//    (cudaGetSymbolAddress with that device current) and caches it with the
+//    device's current context. Make that first call before any stream
+//    capture. After a cudaDeviceReset (or any teardown that gives the device
+//    a new primary context) the next call sees a new context and looks the
+//    address up again; that call, too, must come before any capture;
 //  * nothing in the scratch has to start at zero: every Schur block a level
 //    writes is read back only by the same call, after it is written.
 
@@ -40,17 +43,42 @@ static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
 static std::mutex g_scratch_mu;
 static void* g_scratch_ptr[kMaxDevices];
+static void* g_scratch_ctx[kMaxDevices];  // the context the address belongs to
 
-// Device address of g_static_scratch on the current device (looked up once).
+// The current driver context (an opaque identity), through the runtime's
+// driver entry point so that the library links against libcudart only.
+static int current_context(void** ctx) {
+  using GetCurrent = int (*)(void**);  // CUresult cuCtxGetCurrent(CUcontext*)
+  static GetCurrent fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    VXG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000,
+                                                  cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) return VXG_ERR_CUDA;
+    fn = reinterpret_cast<GetCurrent>(p);
+  }
+  *ctx = nullptr;
+  return fn(ctx) == 0 ? VXG_OK : VXG_ERR_CUDA;
+}
+
+// Device address of g_static_scratch on the current device, looked up once
+// per device and context.
 static int static_scratch(void** out) {
   int dev = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return VXG_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  void* ctx = nullptr;
+  int st = current_context(&ctx);
+  if (st) return st;
+  if (!g_scratch_ptr[dev] || !ctx || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
-    VXG_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+    VXG_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));  // makes the context current
+    st = current_context(&ctx);
+    if (st) return st;
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return VXG_OK;
