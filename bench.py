@@ -143,6 +143,8 @@ def parse():
                     help="FP64 refinement sweeps per solve of the FP32-factor form "
                          "(default: the library's choice per engine)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="adder_mc: skip the bounded runs of the other configurations")
     ap.add_argument("--train", type=int, default=None, help="ota_warm: training instances")
     ap.add_argument("--epochs", type=int, default=40, help="ota_warm: training epochs")
     ap.add_argument("--grid-sides", type=int, nargs=2, default=None, metavar=("LO", "HI"),
@@ -337,7 +339,10 @@ def run_reference(a):
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w.label(a.instances, len(ts)), "sample": sample},
+            "config": {"workload": w.label(a.instances, len(ts)), "instances": a.instances,
+                       "time_points": len(ts), "method": w.method or "dc",
+                       "t_stop_s": w.t_stop, "solves_per_step": a.instances * len(ts),
+                       "sample": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -407,6 +412,46 @@ def oracle_check(w, circuit, z, ts, ic, count=16):
             "oracle": "oracle/cvx.c, FP64, 1 thread", "seconds": time.perf_counter() - t0}
 
 
+def wl_sides(instances):
+    from voltax_gb300 import workloads
+    return workloads.grid_sides(instances, *GRID_SIDES, seed=0)
+
+
+def oracle_check_grids(batch, z, sides, seed, count=4):
+    """oracle_check for an uneven grid batch: the first `count` grids, each
+    solved alone by the compiled oracle and checked at the batch's solution
+    (node voltages and pad currents of that grid)."""
+    from oracle import cbase
+    from oracle import plan as oplan
+    from voltax_gb300 import symbolic, workloads
+    worst = {"rel": 0.0, "kcl": 0.0, "ratio": 0.0}
+    t0 = time.perf_counter()
+    ts = np.zeros(1)
+    n = min(count, len(sides))
+    for k in range(n):
+        c = workloads.power_grid(sides[k], seed=seed + k)
+        st = symbolic.structure(c)
+        cs = cbase.CSystem(c, st, oplan.make_plan_numpy(st))
+        zr, _, _ = cs.run(ts, dc_first=True)
+        zk = np.empty(c.size)
+        zk[: c.n_nodes] = z[[batch.node(f"g{k}_{nm}") for nm in c.layout.node_names]]
+        pads = c.devices("VoltageSource")
+        zk[[c.layout.internal(p) for p in pads]] = \
+            z[[batch.layout.internal(f"g{k}_{p}") for p in pads]]
+        a, r = zk[: c.n_nodes], zr[0, : c.n_nodes]
+        worst["rel"] = max(worst["rel"], float(np.max(np.abs(a - r) /
+                                                      np.maximum(np.abs(r), 1e-3))))
+        kcl, ratio = cs.check(ts, zk[None], method="dc", dc_first=True)
+        worst["kcl"] = max(worst["kcl"], float(np.max(kcl)))
+        worst["ratio"] = max(worst["ratio"], float(np.max(ratio)))
+    return {"instances": n, "grids": [int(x) for x in sides[:n]], "time_points": 1,
+            "max_rel_node_v": worst["rel"], "max_kcl_residual_a": worst["kcl"],
+            "max_newton_step_ratio": worst["ratio"],
+            "pass": bool(worst["rel"] <= 1e-9 and worst["ratio"] <= 1.0),
+            "oracle": "oracle/cvx.c, FP64, 1 thread, each grid alone",
+            "seconds": time.perf_counter() - t0}
+
+
 def fused_phases(lib, torch, dev, run, total_iters):
     """Per-phase SM cycles of the fused kernel over one profiled run
     (vxg_fused_set_profile): shares of the kernel time and CTA cycles per
@@ -430,146 +475,141 @@ def fused_phases(lib, torch, dev, run, total_iters):
 
 
 # ----------------------------------------------------------------- GPU arm
-def main():
-    a = parse()
-    if a.impl == "reference":
-        run_reference(a)
-        return
-    # CPU baseline first (before any CUDA work), rank 0 only
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    w = WORKLOADS[a.workload]
-    cpu = cpu_baseline(w, a.time_points, a.instances) if rank == 0 and not a.no_cpu else None
-    if w.name == "ota_warm":
-        main_warm(a, w, cpu)
-        return
-    if w.name == "grids":
-        main_grids(a, w, cpu)
-        return
-    superlu = cpu_superlu(w, a.instances) if rank == 0 and not a.no_cpu else None
+class GPU:
+    """The device, process group, library and helpers one GPU run shares."""
 
-    import torch
+    def __init__(self):
+        import torch
+        from voltax_gb300 import _lib
+        self.torch = torch
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+            self.dist = dist
+        self.dev = torch.device("cuda", self.local)
+        self.lib = _lib.load()
+        self.peaks = {}
+        pk = ROOT / "MEASURED_PEAKS.json"
+        if pk.exists():
+            self.peaks = json.loads(pk.read_text())
+        # inputs and states are far below L2; a 256 MB write flushes it
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=self.dev)
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+        self.torch.cuda.synchronize()
+
+    def timed(self, fn, k):
+        """Device time (s) of k calls of fn, L2 flushed before each, CUDA
+        events on the current stream bracketed by a barrier and a
+        synchronize; the maximum over ranks."""
+        torch = self.torch
+        ms = []
+        for _ in range(k):
+            self.flush.zero_()
+            self.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            self.barrier()
+            ms.append(e0.elapsed_time(e1))
+        t = float(np.sum(ms)) / 1e3
+        if self.dist is not None:
+            tt = torch.tensor([t], device=self.dev)
+            self.dist.all_reduce(tt, op=self.dist.ReduceOp.MAX)
+            t = float(tt)
+        return t
+
+    def fp64_peak(self):
+        """FP64 rate this GPU reaches in cuBLAS (torch float64 matmul 4096^3,
+        best of 5): the denominator of the fused kernel's FP64 roofline."""
+        torch = self.torch
+        n = 4096
+        x = torch.randn(n, n, dtype=torch.float64, device=self.dev)
+        y = torch.randn(n, n, dtype=torch.float64, device=self.dev)
+        torch.matmul(x, y)
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(x, y)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        return 2.0 * n ** 3 / best / 1e12
+
+
+# FP64 work of the fused kernel's chosen form per Newton iteration of one
+# instance, counted by ncu on the 512-instance x 21-point mirror-adder case
+# (profiles/fused_kernel_adder_mc512.md): FP64 lane operations (DFMA counted
+# twice) of that launch divided by its Newton iterations. Used as the
+# algorithmic FP64 work of the roofline below.
+FUSED_FP64_FLOP_PER_ITER = None
+FUSED_NCU = None
+
+
+def measure_circuit(g, a, w, instances, n_t, steps, warmup, cpu=None, full=True):
+    """One circuit workload (the adder Monte Carlo, the ring oscillator, the
+    100 x 100 grid): the chosen form timed with inputs resident in HBM, the
+    plain FP64 form, their match, the oracle check, the end-to-end figure
+    through the public API, and (full) phase cycles and the roofline."""
+    torch = g.torch
     import voltax_gb300 as vx
-    from voltax_gb300 import _lib, workloads
-
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    dev = torch.device("cuda", local)
-    lib = _lib.load()
-
-    circuit = w.circuit(a.instances, seed=rank)
+    from voltax_gb300 import symbolic
+    from voltax_gb300.analysis import _Call
+    lib = g.lib
+    circuit = w.circuit(instances, seed=g.rank)
     B = circuit.batch
-    ts = w.times(a.time_points)
+    ts = w.times(n_t)
     ic = w.ic(circuit)
     out_nodes = ([circuit.node(n) for n in w.outputs] if w.outputs
                  else list(range(circuit.n_nodes)))
-
-    dev_circuit = to_device(circuit, dev)
+    dev_circuit = to_device(circuit, g.dev)
     host_circuit = to_device(circuit, None, pin=True)
     opts32 = vx.Options(precision="f32", engine=a.engine, refine=a.refine, block=a.block)
     opts64 = vx.Options(precision="f64", engine=a.engine, block=a.block)
-    from voltax_gb300 import symbolic
-    from voltax_gb300.analysis import _Call
     st = symbolic.structure(circuit)
-    engine_used = "fused" if _Call(dev_circuit, opts32).fused else "generic"
-    peaks = {}
-    pk = ROOT / "MEASURED_PEAKS.json"
-    if pk.exists():
-        peaks = json.loads(pk.read_text())
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    call32 = _Call(dev_circuit, opts32)
+    engine_used = "fused" if call32.fused else "generic"
 
     def step(c, opts):
         if w.analysis == "dc":
             return vx.dc(c, options=opts)
         return vx.transient(c, ts, ic=ic, method=w.method, options=opts)
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def timed(fn, k):
-        ms = []
-        for _ in range(k):
-            flush.zero_()
-            barrier()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            fn()
-            e1.record()
-            barrier()
-            ms.append(e0.elapsed_time(e1))
-        return ms
-
-    for _ in range(a.warmup):
+    for _ in range(warmup):
         step(dev_circuit, opts32)
     n0 = lib.vxg_launch_count()
-    with Clocks(local) as clk:
-        ms32 = timed(lambda: step(dev_circuit, opts32), a.steps)
-    launches = (lib.vxg_launch_count() - n0) // a.steps
+    with Clocks(g.local) as clk:
+        t32 = g.timed(lambda: step(dev_circuit, opts32), steps)
+    launches = (lib.vxg_launch_count() - n0) // steps
     solves_per_step = B * len(ts)
-    t32 = float(np.sum(ms32)) / 1e3
-    if dist is not None:
-        tt = torch.tensor([t32], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t32 = float(tt)
-    value = world * solves_per_step * a.steps / t32
+    value = g.world * solves_per_step * steps / t32
 
-    # plain FP64 path on the same workload (fewer steps), and the match
+    # the plain FP64 form on the same workload (fewer steps), and the match
     step(dev_circuit, opts64)
-    ms64 = timed(lambda: step(dev_circuit, opts64), max(1, min(a.steps, 2)))
-    value64 = solves_per_step * len(ms64) / (float(np.sum(ms64)) / 1e3)
+    k64 = max(1, min(steps, 2))
+    t64 = g.timed(lambda: step(dev_circuit, opts64), k64)
+    value64 = g.world * solves_per_step * k64 / t64
     s32 = step(dev_circuit, opts32)
     s64 = step(dev_circuit, opts64)
     nv = circuit.n_nodes
     match = float((s32.z[..., :nv] - s64.z[..., :nv]).abs().max())
-    conv = bool(s32.converged.all())
-    it = s32.iterations.reshape(-1, len(ts)).float() if w.analysis == "transient" else \
-        s32.iterations.reshape(-1, 1).float()
+    it = s32.iterations.reshape(-1, len(ts)).double() if w.analysis == "transient" else \
+        s32.iterations.reshape(-1, 1).double()
     iters = float(it[:, 1:].mean()) if w.analysis == "transient" else float(it.mean())
     total_iters = int(it.sum())  # Newton iterations of one step, all instances
-    phases = None
-    if engine_used == "fused":
-        phases = {"chosen": fused_phases(lib, torch, dev, lambda: step(dev_circuit, opts32),
-                                         total_iters)}
-        it64 = s64.iterations.reshape(-1).double().sum()
-        phases["plain_fp64"] = fused_phases(lib, torch, dev, lambda: step(dev_circuit, opts64),
-                                            float(it64))
+    it64 = float(s64.iterations.double().sum())
 
-    # roofline of the dominant kernel. Algorithmic bytes per Newton iteration
-    # and instance: 8 nnz (stamp write) + 4 (nnz + 2 factor_entries) (panel
-    # fill, factor write + read in the solve) + 8 * 6 S (z, r, dz, b, x and
-    # the residual); the fused kernel keeps all of it on chip, so this is the
-    # traffic an unfused HBM-streaming implementation of the same step moves.
-    fe = int(st.plan.stats["factor_entries"])
-    bytes_per_iter = 8 * st.nnz + 4 * (st.nnz + 2 * fe) + 8 * 6 * st.size
-    flops_per_iter = float(st.plan.stats["flops"]) + 2 * 2 * fe
-    step_s = t32 / a.steps
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = bytes_per_iter * total_iters / step_s / 1e9
-    # DRAM traffic of one fused launch: the packed parameter rows read once per
-    # instance, the states written per time point, converged + iterations. An
-    # ncu capture of 512 instances x 21 points read 5.8 MB = the packed rows;
-    # its 6.4 MB of states stayed in L2, at this size they do not.
-    traffic = None
-    if engine_used == "fused":
-        packed = sum(t.numel() * 8 for t in _Call(dev_circuit, opts32).keep)
-        traffic = packed + B * len(ts) * (8 * st.size + 8)
-    roofline = {"bound": "hbm", "kernel": "fused_kernel<float>" if engine_used == "fused"
-                else "factor/solve level kernels", "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                "peak_source": "measured" if peaks else "fallback",
-                "algorithmic_bytes_per_launch": bytes_per_iter * total_iters,
-                "newton_iterations_per_launch": total_iters,
-                "factor_flops_per_launch": flops_per_iter * total_iters,
-                "achieved_factor_tflops": flops_per_iter * total_iters / step_s / 1e12}
-
-    # end to end through the public API: params from pinned host memory, output
-    # node waveforms back to pinned host memory
+    # end to end through the public API: parameters from pinned host memory,
+    # the output node waveforms back to pinned host memory
     h2d = h2d_bytes(host_circuit)
     out_host = torch.empty(tuple(s32.z[..., out_nodes].shape), dtype=torch.float64,
                            pin_memory=True)
@@ -579,64 +619,159 @@ def main():
         out_host.copy_(s.z[..., out_nodes], non_blocking=True)
 
     e2e_step()
-    ms_e2e = timed(e2e_step, a.steps)
-    e2e_value = world * solves_per_step * a.steps / (float(np.sum(ms_e2e)) / 1e3)
+    t_e2e = g.timed(e2e_step, steps)
+    e2e_value = g.world * solves_per_step * steps / t_e2e
 
-    if rank != 0:
-        return
-    zs = s32.z.cpu().numpy()
-    if zs.ndim == 1 or (w.analysis == "transient" and zs.ndim == 2):
-        zs = zs[None]
-    ocheck = oracle_check(w, circuit, zs, ts, ic)
-    # voltax publishes this one workload: 499 us per step on one CPU thread
-    # (benchmarks/README.md:217), i.e. 2004 Newton solves/s
-    vs_baseline = value / (1.0 / 499e-6) if w.name == "ring101_l1" else None
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": 1e3 * t32 / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": vs_baseline,
-        "dtype": "f32 LU + f64 residual/refinement", "data": "synthetic",
-        "config": {"workload": w.label(B, len(ts)), "instances": B,
-                   "time_points": len(ts), "method": w.method or "dc", "t_stop_s": w.t_stop,
+    phases = None
+    if full and engine_used == "fused":
+        phases = {"chosen": fused_phases(lib, torch, g.dev, lambda: step(dev_circuit, opts32),
+                                         total_iters),
+                  "plain_fp64": fused_phases(lib, torch, g.dev,
+                                             lambda: step(dev_circuit, opts64), it64)}
+    out = {
+        "value": value, "unit": UNIT, "ms_per_step": 1e3 * t32 / steps, "steps": steps,
+        "warmup": warmup,
+        "config": {"workload": w.label(B, len(ts)), "instances": B, "time_points": len(ts),
+                   "method": w.method or "dc", "t_stop_s": w.t_stop,
                    "solves_per_step": solves_per_step, "engine": engine_used,
-                   "block": _Call(dev_circuit, opts32).block if engine_used == "fused" else None,
-                   "refine": _Call(dev_circuit, opts32).refine,
+                   "block": call32.block if engine_used == "fused" else None,
+                   "refine": call32.refine,
                    "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if g.world > 1 else "single GPU"},
         "plain_fp64": {"value": value64, "unit": UNIT, "speedup": value / value64},
-        "match": {"max_abs_node_v_diff_vs_fp64": match, "converged": conv,
+        "match": {"max_abs_node_v_diff_vs_fp64": match, "converged": bool(s32.converged.all()),
                   "mean_newton_iters": iters},
-        "oracle_check": ocheck,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(out_host.numel() * 8)},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
-        "cpu_baseline": cpu,
-        "roofline": roofline,
     }
-    if superlu:
-        line["cpu_superlu"] = superlu
     if phases:
-        line["phases"] = phases
+        out["phases"] = phases
+    if full:
+        out["roofline"] = roofline(g, st, engine_used, call32, B, len(ts), total_iters,
+                                   t32 / steps, phases)
+    if g.rank == 0:
+        zs = s32.z.cpu().numpy()
+        if zs.ndim == 1 or (w.analysis == "transient" and zs.ndim == 2):
+            zs = zs[None]
+        out["oracle_check"] = oracle_check(w, circuit, zs, ts, ic)
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    return out
+
+
+def roofline(g, st, engine_used, call32, B, n_t, total_iters, step_s, phases):
+    """Roofline of the dominant kernel. The fused kernel keeps every Newton
+    iteration on chip (its DRAM traffic is the parameters in and the states
+    out), and ncu shows its busiest pipe is FP64 (the device currents and
+    charges, the residual and the convergence test); so it is placed against
+    the GPU's FP64 rate (cuBLAS DGEMM, measured here). Its FP64 work per
+    Newton iteration is the ncu count of FP64 operations of the 512-instance
+    capture divided by that launch's Newton iterations. The HBM frame of an
+    unfused implementation is kept for context."""
+    fe = int(st.plan.stats["factor_entries"])
+    bytes_per_iter = 8 * st.nnz + 4 * (st.nnz + 2 * fe) + 8 * 6 * st.size
+    hbm_peak = float(g.peaks.get("hbm_gbs", 6800.0))
+    hbm = {"achieved_gbs": bytes_per_iter * total_iters / step_s / 1e9, "peak_gbs": hbm_peak,
+           "peak_source": "measured" if g.peaks else "fallback",
+           "algorithmic_bytes_per_launch": bytes_per_iter * total_iters}
+    if engine_used != "fused" or FUSED_FP64_FLOP_PER_ITER is None:
+        return {"bound": "hbm", "kernel": "factor/solve level kernels"
+                if engine_used != "fused" else "fused_kernel<float>",
+                "achieved": hbm["achieved_gbs"], "peak": hbm_peak, "unit": "GB/s",
+                "frac": hbm["achieved_gbs"] / hbm_peak, "traffic": None,
+                "peak_source": hbm["peak_source"],
+                "newton_iterations_per_launch": total_iters}
+    packed = sum(t.numel() * 8 for t in call32.keep)
+    traffic = packed + B * n_t * (8 * st.size + 8)
+    peak = g.fp64_peak()
+    flops = FUSED_FP64_FLOP_PER_ITER * total_iters
+    achieved = flops / step_s / 1e12
+    return {"bound": "fp64", "kernel": f"fused_kernel<float,{call32.block}>"
+            if call32.block != 32 else "fused_warp_kernel<float>",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch float64 matmul)",
+            "fp64_flop_per_newton_iter": FUSED_FP64_FLOP_PER_ITER,
+            "newton_iterations_per_launch": total_iters,
+            "unfused_hbm_frame": hbm,
+            "ncu": FUSED_NCU}
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    # CPU legs first (before any CUDA work), rank 0 only
+    rank = int(os.environ.get("RANK", "0"))
+    w = WORKLOADS[a.workload]
+    cpu = cpu_baseline(w, a.time_points, a.instances) if rank == 0 and not a.no_cpu else None
+    superlu = None
+    if w.name not in ("ota_warm", "grids"):
+        superlu = cpu_superlu(w, a.instances) if rank == 0 and not a.no_cpu else None
+    g = GPU()
+    if w.name == "ota_warm":
+        res = measure_warm(g, a, w, a.instances, a.train or OTA_TRAIN, a.epochs, a.steps,
+                           a.warmup, cpu)
+    elif w.name == "grids":
+        res = measure_grids(g, a, w, cpu)
+    else:
+        res = measure_circuit(g, a, w, a.instances, a.time_points, a.steps, a.warmup, cpu)
+    if superlu:
+        res["cpu_superlu"] = superlu
+    if w.name == "adder_mc" and not a.no_extra:
+        res["configs"] = other_configs(g, a)
+    if g.rank != 0:
+        return
+    # voltax publishes one workload: 499 us per step on one CPU thread
+    # (benchmarks/README.md:217), i.e. 2004 Newton solves/s
+    vs_baseline = res["value"] / (1.0 / 499e-6) if w.name == "ring101_l1" else None
+    dtype = "f32 LU + f64 residual/refinement"
+    if w.name == "ota_warm":
+        dtype += "; MLP bf16 x bf16 -> f32"
+    line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": g.world,
+            "steps": res["steps"], "warmup": res["warmup"], "ms_per_step": res["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": vs_baseline,
+            "dtype": dtype, "data": "synthetic"}
+    line.update({k: v for k, v in res.items() if k not in line})
     print(json.dumps(line))
 
 
+def other_configs(g, a):
+    """Bounded runs of the other single-GPU benchmark configurations, each
+    with its own timing and oracle check: the 101-stage ring oscillator
+    (one 2001-point trapezoidal transient per step), the 100 x 100 power
+    grid DC, and the learned warm start on 10,000 held-out OTA-chain
+    instances with a network trained first on 20,000 operating points of the
+    plain solver (training reported separately, not timed)."""
+    steps, warmup = max(1, min(a.steps, 5)), max(1, min(a.warmup, 3))
+    out = {}
+    ring = WORKLOADS["ring101"]
+    out["ring101_trap2001"] = measure_circuit(g, a, ring, 1, ring.n_t, min(steps, 3), warmup,
+                                              full=False)
+    grid = WORKLOADS["grid100"]
+    out["power_grid100_dc"] = measure_circuit(g, a, grid, 1, 1, 2 * steps, warmup, full=False)
+    ota = WORKLOADS["ota_warm"]
+    out["ota_chain_warm_start"] = measure_warm(g, a, ota, ota.default_instances, 20_000, 40,
+                                               steps, warmup)
+    return out
+
+
+
 # --------------------------------------------------- learned warm start arm
-def main_warm(a, w, cpu):
+def measure_warm(g, a, w, instances, n_train, epochs, steps, warmup, cpu=None):
     """DC operating points of held-out OTA-chain instances from the MLP's
     predicted guess (inference + Newton + fallback, one step) against Newton
-    from the default guess. The network is trained first (untimed) on
-    operating points the plain FP64 solver produces for other parameters."""
-    import torch
+    from the default guess. The network is trained first (untimed, reported
+    separately) on operating points the plain FP64 solver produces for
+    other parameters."""
+    torch = g.torch
     import voltax_gb300 as vx
-    from voltax_gb300 import _lib, warmstart, workloads
+    from voltax_gb300 import warmstart, workloads
 
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    lib = _lib.load()
-    n_train = a.train or OTA_TRAIN
+    rank, dev, lib = g.rank, g.dev, g.lib
     base = workloads.ota_chain(OTA_STAGES)
 
     def make(P):
@@ -655,44 +790,31 @@ def main_warm(a, w, cpu):
     model = warmstart.WarmStartMLP(Xtr.shape[1], Vtr.shape[1], hidden=512, seed=0)
     t0 = time.perf_counter()
     hist = model.fit(Xtr[keep], Vtr[torch.as_tensor(keep, device=Vtr.device)],
-                     epochs=a.epochs, batch=1024, lr=2e-3, lr_final=2e-5)
+                     epochs=epochs, batch=1024, lr=2e-3, lr_final=2e-5)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
 
-    X = workloads.ota_params(a.instances, seed=OTA_TEST_SEED + rank)
+    X = workloads.ota_params(instances, seed=OTA_TEST_SEED + rank)
     c_host = make(X)
     c = to_device(c_host, dev)  # parameters resident in HBM for `value`
     Xd = torch.as_tensor(X, device=dev)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-
-    def timed(fn, k):
-        ms = []
-        for _ in range(k):
-            flush.zero_()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            fn()
-            e1.record()
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        return float(np.sum(ms)) / 1e3
 
     warm = lambda: warmstart.dc(c, Xd, model, options=chosen)  # noqa: E731
     cold = lambda: vx.dc(c, options=chosen)  # noqa: E731
     cold64 = lambda: vx.dc(c, options=plain)  # noqa: E731
-    for _ in range(a.warmup):
+    for _ in range(warmup):
         warm()
     n0 = lib.vxg_launch_count()
-    with Clocks(local) as clk:
-        t_warm = timed(warm, a.steps)
-    launches = (lib.vxg_launch_count() - n0) // a.steps
+    with Clocks(g.local) as clk:
+        t_warm = g.timed(warm, steps)
+    launches = (lib.vxg_launch_count() - n0) // steps
+    k_cold = max(1, min(steps, 2))
     cold()
-    t_cold = timed(cold, max(1, min(a.steps, 2)))
+    t_cold = g.timed(cold, k_cold)
     cold64()
-    t_cold64 = timed(cold64, max(1, min(a.steps, 2)))
-    B = a.instances
-    value = B * a.steps / t_warm
+    t_cold64 = g.timed(cold64, k_cold)
+    B = instances
+    value = B * steps / t_warm
     s_warm, s_cold, s_ref = warm(), cold(), cold64()
     nv = c.layout.n_nodes
     ref_v = s_ref.z[:, :nv]
@@ -713,24 +835,18 @@ def main_warm(a, w, cpu):
         out.copy_(s.z[:, :nv], non_blocking=True)
 
     e2e()
-    t_e2e = timed(e2e, a.steps)
-    if rank != 0:
-        return
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": 1e3 * t_warm / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 LU + f64 residual/refinement; MLP bf16 x bf16 -> f32",
-        "data": "synthetic",
+    t_e2e = g.timed(e2e, steps)
+    res = {
+        "value": value, "unit": UNIT, "ms_per_step": 1e3 * t_warm / steps, "steps": steps,
+        "warmup": warmup,
         "config": {"workload": w.label(B, 1), "instances": B, "stages": OTA_STAGES,
-                   "nodes": nv, "train_instances": n_train, "epochs": a.epochs,
+                   "nodes": nv, "train_instances": n_train, "epochs": epochs,
                    "mlp": f"{Xtr.shape[1]}-512-512-{Vtr.shape[1]} GELU",
                    "l2": "flushed between timed steps (256 MB write)"},
-        "default_guess": {"value": B / (t_cold / max(1, min(a.steps, 2))),
-                          "unit": UNIT, "mean_newton_iters": float(it_c.mean()),
+        "default_guess": {"value": B * k_cold / t_cold, "unit": UNIT,
+                          "mean_newton_iters": float(it_c.mean()),
                           "max_newton_iters": int(it_c.max())},
-        "plain_fp64_default_guess": {"value": B / (t_cold64 / max(1, min(a.steps, 2))),
-                                     "unit": UNIT},
+        "plain_fp64_default_guess": {"value": B * k_cold / t_cold64, "unit": UNIT},
         "warm_start": {"mean_newton_iters": float(it_w.mean()),
                        "max_newton_iters": int(it_w.max()),
                        "iteration_reduction": float(it_c.mean() / it_w.mean()),
@@ -741,29 +857,29 @@ def main_warm(a, w, cpu):
                      "data_mean_newton_iters": float(it_tr.double().mean()),
                      "train_s": train_s, "loss_first_epoch": hist[0],
                      "loss_last_epoch": hist[-1]},
-        "e2e": {"value": B * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": B * steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(out.numel() * 8)},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
-        "cpu_baseline": cpu,
     }
-    print(json.dumps(line))
+    if rank == 0:
+        res["oracle_check"] = oracle_check(w, c_host, s_warm.z.cpu().numpy(), np.zeros(1), "dc")
+    if cpu is not None:
+        res["cpu_baseline"] = cpu
+    return res
 
 
 # ------------------------------------------------------- uneven grid batch arm
-def main_grids(a, w, cpu):
+def measure_grids(g, a, w, cpu=None):
     """An uneven batch of power grids in one segmented circuit: DC of every
     grid (one solve per grid), and the adjoint of each grid's largest IR drop
     with respect to all segment conductances (one transposed solve for the
     batch)."""
-    import torch
+    torch = g.torch
     import voltax_gb300 as vx
-    from voltax_gb300 import _lib, symbolic
+    from voltax_gb300 import symbolic
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    lib = _lib.load()
+    dev, lib = g.dev, g.lib
     t0 = time.perf_counter()
     circuit = w.circuit(a.instances, seed=0)
     st = symbolic.structure(circuit)
@@ -775,20 +891,7 @@ def main_grids(a, w, cpu):
                            dtype=torch.long)
     chosen = vx.Options(precision="f32")
     plain = vx.Options(precision="f64")
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-
-    def timed(fn, k):
-        ms = []
-        for _ in range(k):
-            flush.zero_()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            fn()
-            e1.record()
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        return float(np.sum(ms)) / 1e3
+    timed = g.timed
 
     def drops(v):
         """largest IR drop (1 V - v) of each grid, by segment"""
@@ -807,7 +910,7 @@ def main_grids(a, w, cpu):
     for _ in range(a.warmup):
         fwd()
     n0 = lib.vxg_launch_count()
-    with Clocks(local) as clk:
+    with Clocks(g.local) as clk:
         t_fwd = timed(fwd, a.steps)
     launches = (lib.vxg_launch_count() - n0) // a.steps
     vx.dc(c_dev, options=plain)
@@ -830,11 +933,9 @@ def main_grids(a, w, cpu):
     t_e2e = timed(e2e, a.steps)
     sides = [int(round((np.sum(circuit.unknown_segments()[:nv] == k)) ** 0.5))
              for k in range(n_grids)]
-    line = {
-        "metric": METRIC, "value": n_grids * a.steps / t_fwd, "unit": UNIT, "n_gpus": 1,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_fwd / a.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 LU + f64 residual/refinement", "data": "synthetic",
+    res = {
+        "value": n_grids * a.steps / t_fwd, "unit": UNIT, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * t_fwd / a.steps,
         "config": {"workload": w.label(n_grids, 1), "grids": n_grids, "sides": sides,
                    "unknowns": circuit.size, "nnz": st.nnz,
                    "factor_entries": int(st.plan.stats["factor_entries"]),
@@ -852,9 +953,14 @@ def main_grids(a, w, cpu):
                 "h2d_bytes_per_step": int(h2d_bytes(host_c)), "d2h_bytes_per_step": nv * 8},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
-        "cpu_baseline": cpu,
     }
-    print(json.dumps(line))
+    res["plain_fp64"]["speedup"] = res["value"] / res["plain_fp64"]["value"]
+    if g.rank == 0:
+        res["oracle_check"] = oracle_check_grids(circuit, s32.z.cpu().numpy(),
+                                                 wl_sides(a.instances), seed=0)
+    if cpu is not None:
+        res["cpu_baseline"] = cpu
+    return res
 
 
 if __name__ == "__main__":

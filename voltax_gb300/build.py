@@ -69,6 +69,32 @@ def build_symbolic(verbose: bool = False) -> Path:
     return lib
 
 
+def build_xla(verbose: bool = False) -> Path | None:
+    """The XLA FFI shim (libvxg_xla.so), only where jax exposes its FFI
+    headers (jax.ffi.include_dir()); None elsewhere, or when that build
+    fails (the shim is optional: nothing else depends on it)."""
+    try:
+        from jax import ffi
+        include = ffi.include_dir()
+    except Exception:
+        return None
+    lib = OUT / "libvxg_xla.so"
+    src = SRC / "vxg_xla.cc"
+    if lib.exists() and lib.stat().st_mtime > src.stat().st_mtime:
+        return lib
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-shared", "-fPIC",
+           f"-I{include}", f"-I{INCLUDE}", f"-I{cuda / 'include'}", str(src), "-o", str(lib),
+           f"-L{OUT}", "-lvxg", f"-Wl,-rpath,{OUT}"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        print(f"libvxg_xla.so not built (g++ failed):\n{res.stderr[-2000:]}", file=sys.stderr)
+        return None
+    if verbose:
+        print(lib)
+    return lib
+
+
 def build(verbose: bool = False, extra=()) -> Path:
     build_symbolic(verbose)
     OUT.mkdir(exist_ok=True)
@@ -83,6 +109,7 @@ def build(verbose: bool = False, extra=()) -> Path:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     if verbose:
         print(lib)
+    build_xla(verbose)
     return lib
 
 
