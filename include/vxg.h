@@ -376,6 +376,16 @@ int vxg_ac_factor(const vxg_handle* h, int32_t n_freq, const double* G, const do
 int vxg_ac_solve(const vxg_handle* h, int32_t n_freq, const void* factors, const double* b,
                  int64_t b_stride, double* x, void* workspace, void* stream);
 
+/* C[M x N] = A[M x K] B[K x N] (row-major FP32, leading dimensions lda,
+ * ldb, ldc) on the fifth-generation tensor cores with three TF32 products
+ * per term (a_hi b_hi + a_hi b_lo + a_lo b_hi, x = x_hi + x_lo each rounded
+ * to TF32) accumulated in FP32: the panel-update product of wide supernodes
+ * (voltax/sparse.py:566-568 computes these products as einsums), exposed
+ * on its own. *status (device int32) is set to 1 if a wait on the tensor
+ * cores gave up (the result is then invalid); it is not cleared. */
+int vxg_gemm_tf32x3(int32_t M, int32_t N, int32_t K, const float* A, int32_t lda, const float* B,
+                    int32_t ldb, float* C, int32_t ldc, int32_t* status, void* stream);
+
 /* Kernels this library has launched since it was loaded (a diagnostic
  * counter; no counterpart in the reference). */
 uint64_t vxg_launch_count(void);
