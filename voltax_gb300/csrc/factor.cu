@@ -26,6 +26,7 @@
 
 #include "cplx.cuh"
 #include "internal.cuh"
+#include "tc.cuh"
 
 namespace vxg {
 
@@ -72,7 +73,11 @@ __device__ __forceinline__ void tile_product(int nr, int nc, int k, const T* X, 
   }
 }
 
-template <typename T, int NT, bool Wide>
+// Supernodes at least this wide take their Schur product S = F21 Ub on the
+// tensor cores in the FP32 form (3xTF32, tc::product_3xtf32).
+constexpr int kTcMinK = 64;
+
+template <typename T, int NT, bool Wide, bool TC = false>
 __global__ void __launch_bounds__(NT)
     factor_level_kernel(const int* __restrict__ lv_sn, const long long* __restrict__ schur_off,
                         const int* __restrict__ sn_k, const int* __restrict__ sn_r,
@@ -182,13 +187,37 @@ __global__ void __launch_bounds__(NT)
     __syncthreads();
   }
 
+  // ---- S = F21 Ub on the tensor cores (FP32 form, k >= kTcMinK): every
+  // row at once, before Lb overwrites F21. A wait that gives up leaves NaN in
+  // the Schur block, so the factorization reports non-finite values.
+  bool schur_done = false;
+  if constexpr (TC) {
+    if (k >= kTcMinK) {
+      __shared__ uint32_t tmem_slot;
+      const uint32_t used = tc::smem_u32(perm + k);
+      unsigned char* tcbuf = reinterpret_cast<unsigned char*>(perm + k) +
+                             (((used + 1023u) & ~1023u) - used);
+      tc::ProductState ps;
+      tc::product_begin(ps, tcbuf, &tmem_slot);
+      tc::product_3xtf32<NT>(
+          ps, r, r, k, [&](int a, int l) { return (float)F21[(long long)a * k + l]; },
+          [&](int l, int c) { return (float)F12[(long long)l * r + c]; },
+          [&](int a, int c, float v) { Sout[(long long)a * r + c] = (T)v; });
+      tc::product_end(ps);
+      if (!ps.ok)
+        for (long long i = threadIdx.x; i < (long long)r * r; i += NT) Sout[i] = (T)NAN;
+      __syncthreads();
+      schur_done = true;
+    }
+  }
+
   // ---- per row tile of F21: Schur rows S = F21 Ub, then Lb = F21 W
   for (int a0 = 0; a0 < r; a0 += kTile) {
     const int tr = min(kTile, r - a0);
     for (int a = warp; a < tr; a += NW)
       for (int l = lane; l < k; l += 32) tA[a * k + l] = F21[(long long)(a0 + a) * k + l];
     __syncthreads();
-    for (int c0 = 0; c0 < r; c0 += kTile) {
+    for (int c0 = 0; c0 < r && !schur_done; c0 += kTile) {
       const int tw = min(kTile, r - c0);
       for (int i = warp; i < k; i += NW)
         for (int jj = lane; jj < tw; jj += 32)
@@ -223,15 +252,17 @@ __global__ void schur_apply_kernel(int B, long long ntgt, const long long* __res
   work[(long long)b * work_stride + tgt[t]] -= acc;
 }
 
-size_t factor_smem_bytes(int k, size_t es, bool wide = false) {
+size_t factor_smem_bytes(int k, size_t es, bool wide = false, bool tc = false) {
   const size_t a = wide ? 0 : (size_t)k * k;
-  return (a + 2 * (size_t)k + 2 * (size_t)kTile * k) * es + (size_t)k * sizeof(int) + 16;
+  const size_t base =
+      (a + 2 * (size_t)k + 2 * (size_t)kTile * k) * es + (size_t)k * sizeof(int) + 16;
+  return tc ? base + 1024 + tc::kProductSmem : base;  // + the tensor-core tiles, 1 KB aligned
 }
 
-template <typename T, int NT, bool Wide>
+template <typename T, int NT, bool Wide, bool TC = false>
 static int launch_level(dim3 grid, size_t smem, const Topo& t, long long lo, T* work,
                         long long ws, T* scratch, long long ss, cudaStream_t s) {
-  auto kern = factor_level_kernel<T, NT, Wide>;
+  auto kern = factor_level_kernel<T, NT, Wide, TC>;
   VXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<grid, NT, smem, s>>>(t.lv_sn + lo, t.lv_schur_off + lo, t.sn_k, t.sn_r, t.sn_panel, work,
                               ws, scratch, ss);
@@ -280,8 +311,21 @@ static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t
     const int kmax = t.h_lv_kmax[L];
     dim3 grid((unsigned)(hi - lo), (unsigned)B);
     size_t smem = factor_smem_bytes(kmax, sizeof(T));
-    int st;
-    if (smem > (size_t)max_optin) {  // F11 stays in the panel (real factors only)
+    int st = VXG_OK;
+    bool launched = false;
+    if constexpr (std::is_same<T, float>::value) {
+      if (kmax >= kTcMinK && t.h_lv_rmax[L] > 0) {  // Schur products on the tensor cores
+        const bool wide = factor_smem_bytes(kmax, 4, false, true) > (size_t)max_optin;
+        smem = factor_smem_bytes(kmax, 4, wide, true);
+        if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+        st = wide ? launch_level<T, 512, true, true>(grid, smem, t, lo, work, ws, scratch, ss, s)
+                  : launch_level<T, 512, false, true>(grid, smem, t, lo, work, ws, scratch, ss,
+                                                      s);
+        launched = true;
+      }
+    }
+    if (launched) {
+    } else if (smem > (size_t)max_optin) {  // F11 stays in the panel (real factors only)
       if constexpr (std::is_same<T, cplx>::value) {
         return VXG_ERR_TOO_LARGE;
       } else {
