@@ -136,7 +136,7 @@ def parse():
     ap.add_argument("--instances", type=int, default=None)
     ap.add_argument("--time-points", type=int, default=None)
     ap.add_argument("--engine", default="auto", choices=["auto", "generic", "fused"])
-    ap.add_argument("--block", type=int, default=0, choices=[0, 32, 128, 256, 512],
+    ap.add_argument("--block", type=int, default=0, choices=[0, 32, 64, 128, 256, 512],
                     help="fused kernel threads per instance (32: one warp per instance; "
                          "0: the library's or the autotuner's choice)")
     ap.add_argument("--refine", type=int, default=None,

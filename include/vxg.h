@@ -166,8 +166,8 @@ typedef struct {
   double max_dv;      /* damping: largest node-voltage update            */
   int32_t precision;  /* VXG_F64 or VXG_F32                              */
   int32_t refine;     /* FP64 refinement sweeps per solve (VXG_F32)     */
-  int32_t block;      /* vxg_fused_run threads per instance: 128, 256 or
-                         512 (one CTA per instance), 32 (one warp per
+  int32_t block;      /* vxg_fused_run threads per instance: 64, 128, 256
+                         or 512 (one CTA per instance), 32 (one warp per
                          instance, several per CTA; supernodes <= 32 wide),
                          or 0 for the library's choice (no counterpart) */
 } vxg_newton_opts;

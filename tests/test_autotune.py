@@ -20,8 +20,8 @@ def test_choice_is_cached_and_results_agree_across_shapes():
     assert autotune.choose(call) == choice and len(autotune._cache) == 1
     ts = np.linspace(0, 100e-12, 11)
     ref = vx.transient(c, ts, ic="dc", options=vx.Options(precision="f32"))
-    for engine, block in [("fused", 32), ("fused", 128), ("fused", 256), ("fused", 512),
-                          ("generic", 0)]:
+    for engine, block in [("fused", 32), ("fused", 64), ("fused", 128), ("fused", 256),
+                          ("fused", 512), ("generic", 0)]:
         o = vx.Options(precision="f32", engine=engine, block=block)
         s = vx.transient(c, ts, ic="dc", options=o)
         assert bool(s.converged.all())
@@ -39,6 +39,6 @@ def test_fused_block_widths_agree():
     ts = np.linspace(0, 50e-12, 6)
     out = [vx.transient(c, ts, ic="dc", options=vx.Options(precision="f32", engine="fused",
                                                             block=b)).z
-           for b in (128, 256, 512, 32)]
+           for b in (128, 64, 256, 512, 32)]
     for other in out[1:]:
         assert float((out[0] - other).abs().max()) < 1e-12

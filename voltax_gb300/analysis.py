@@ -52,7 +52,7 @@ class Options:
     `engine` picks the fused persistent kernel or the generic level kernels;
     with ``"auto"`` and `autotune`, the faster one (and the fused kernel's
     CTA width) is timed per topology and batch size (`autotune.choose`).
-    `block` pins the fused kernel's threads per instance: 128, 256 or 512
+    `block` pins the fused kernel's threads per instance: 64, 128, 256 or 512
     (one CTA per instance), 32 (one warp per instance, several instances per
     CTA; topologies whose supernodes are at most 32 wide), 0: library
     choice."""
@@ -79,8 +79,8 @@ class Options:
         if self.solver not in ("auto", "dense", "sparse"):
             raise ValueError("solver must be 'auto', 'dense' or 'sparse', "
                              f"got {self.solver!r}")
-        if self.block not in (0, 32, 128, 256, 512):
-            raise ValueError(f"block must be 0, 32, 128, 256 or 512, got {self.block!r}")
+        if self.block not in (0, 32, 64, 128, 256, 512):
+            raise ValueError(f"block must be 0, 32, 64, 128, 256 or 512, got {self.block!r}")
         if self.precision not in ("f64", "f32"):
             raise ValueError(f"precision must be 'f64' or 'f32', got {self.precision!r}")
 

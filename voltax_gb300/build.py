@@ -21,7 +21,7 @@ INCLUDE = HERE.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["stamp.cu", "factor.cu", "solve.cu", "newton.cu", "capi.cu", "fused.cu",
            "factor_static.cu", "mlp.cu", "gemm_tc.cu",
-           *[f"fused_{t}_{n}.cu" for t in ("f32", "f64") for n in (128, 256, 512)],
+           *[f"fused_{t}_{n}.cu" for t in ("f32", "f64") for n in (64, 128, 256, 512)],
            "fused_warp_f32.cu", "fused_warp_f64.cu"]
 
 

@@ -186,6 +186,7 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   const bool f32 = o->precision == VXG_F32;
   if (nt == 32) return launch_warp_kernel(t, a, f32, s);
   switch (nt) {
+    case 64: return f32 ? launch_fused<float, 64>(a, s) : launch_fused<double, 64>(a, s);
     case 128: return f32 ? launch_fused<float, 128>(a, s) : launch_fused<double, 128>(a, s);
     case 256: return f32 ? launch_fused<float, 256>(a, s) : launch_fused<double, 256>(a, s);
     case 512: return f32 ? launch_fused<float, 512>(a, s) : launch_fused<double, 512>(a, s);

@@ -1307,9 +1307,11 @@ int launch_fused_warp(const FusedArgs& a, cudaStream_t s) {
 
 // One translation unit per instantiation (fused_<type>_<threads>.cu and
 // fused_warp_<type>.cu), so that the kernels compile in parallel.
+extern template int launch_fused<float, 64>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<float, 128>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<float, 256>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<float, 512>(const FusedArgs&, cudaStream_t);
+extern template int launch_fused<double, 64>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 128>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 256>(const FusedArgs&, cudaStream_t);
 extern template int launch_fused<double, 512>(const FusedArgs&, cudaStream_t);

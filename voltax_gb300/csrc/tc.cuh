@@ -192,7 +192,7 @@ __device__ __forceinline__ void product_begin(ProductState& s, unsigned char* sm
 
 // Free the TMEM columns (every thread calls; warp 0 frees). After a wait
 // that gave up, first wait (bounded) once more for the MMAs still in flight.
-__device__ __forceinline__ void product_end(ProductState& s, int limit = 1 << 26) {
+__device__ __forceinline__ void product_end(ProductState& s, int limit = 1 << 20) {
   if (!s.ok) mbar_wait(s.bar, s.phase ^ 1u, limit);
   fence_before_sync();
   __syncthreads();
@@ -210,7 +210,7 @@ __device__ __forceinline__ void product_end(ProductState& s, int limit = 1 << 26
 // skipped and the caller must report the failure.
 template <int NT, class LA, class LB, class ST>
 __device__ void product_3xtf32(ProductState& s, int M, int N, int K, LA la, LB lb, ST st,
-                               int limit = 1 << 26) {
+                               int limit = 1 << 20) {
   static_assert(NT % 128 == 0, "product_3xtf32 needs a multiple of 4 warps");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr uint32_t idesc = idesc_tf32(kTileM, kTileN);
