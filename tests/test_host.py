@@ -54,7 +54,7 @@ def test_options_validation():
     with pytest.raises(ValueError):
         vx.Options(engine="turbo")
     with pytest.raises(ValueError):
-        vx.Options(block=64)
+        vx.Options(block=96)
     with pytest.raises(ValueError):
         vx.Options(precision="f16")
     assert vx.Options(refine=None).native(refine=1).refine == 1
