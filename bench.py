@@ -527,32 +527,21 @@ class GPU:
             t = float(tt)
         return t
 
-    def fp64_peak(self):
-        """FP64 rate this GPU reaches in cuBLAS (torch float64 matmul 4096^3,
-        best of 5): the denominator of the fused kernel's FP64 roofline."""
-        torch = self.torch
-        n = 4096
-        x = torch.randn(n, n, dtype=torch.float64, device=self.dev)
-        y = torch.randn(n, n, dtype=torch.float64, device=self.dev)
-        torch.matmul(x, y)
-        best = float("inf")
-        for _ in range(5):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            torch.matmul(x, y)
-            e1.record()
-            torch.cuda.synchronize()
-            best = min(best, e0.elapsed_time(e1) / 1e3)
-        return 2.0 * n ** 3 / best / 1e12
-
 
 # FP64 work of the fused kernel's chosen form per Newton iteration of one
-# instance, counted by ncu on the 512-instance x 21-point mirror-adder case
-# (profiles/fused_kernel_adder_mc512.md): FP64 lane operations (DFMA counted
-# twice) of that launch divided by its Newton iterations. Used as the
-# algorithmic FP64 work of the roofline below.
-FUSED_FP64_FLOP_PER_ITER = None
-FUSED_NCU = None
+# 4-bit mirror-adder instance: 2 DFMA + DADD + DMUL thread instructions that
+# ncu counted on the 512-instance x 21-point launch (fused_kernel<float,128>,
+# profiles/fused_kernel_adder_mc512.md), 2.962e9 FLOP, divided by that
+# launch's 95,827 Newton iterations. It is fixed by the algorithm (the same
+# device equations, residual and update every iteration), so it is the
+# roofline's per-unit work; the FP64 peak is the hardware rate ncu reports
+# (2 DFMA per cycle per SM) at the SM clock sampled during the run.
+FUSED_FP64_FLOP_PER_ITER = {"adder_mc": 30_907.0}
+FUSED_NCU = {"source": "profiles/fused_kernel_adder_mc512.md", "issue_active_pct": 21.2,
+             "fp64_pipe_active_pct": 33.8, "warps_eligible_per_scheduler_cycle": 0.24,
+             "top_stalls_per_issue": {"barrier": 5.92, "short_scoreboard": 4.21,
+                                      "wait": 3.27},
+             "dram_bytes_per_launch_512x21": 5.88e6}
 
 
 def measure_circuit(g, a, w, instances, n_t, steps, warmup, cpu=None, full=True):
@@ -649,8 +638,8 @@ def measure_circuit(g, a, w, instances, n_t, steps, warmup, cpu=None, full=True)
     if phases:
         out["phases"] = phases
     if full:
-        out["roofline"] = roofline(g, st, engine_used, call32, B, len(ts), total_iters,
-                                   t32 / steps, phases)
+        out["roofline"] = roofline(g, w, st, engine_used, call32, B, len(ts), total_iters,
+                                   t32 / steps, out["clocks"])
     if g.rank == 0:
         zs = s32.z.cpu().numpy()
         if zs.ndim == 1 or (w.analysis == "transient" and zs.ndim == 2):
@@ -661,42 +650,37 @@ def measure_circuit(g, a, w, instances, n_t, steps, warmup, cpu=None, full=True)
     return out
 
 
-def roofline(g, st, engine_used, call32, B, n_t, total_iters, step_s, phases):
+def roofline(g, w, st, engine_used, call32, B, n_t, total_iters, step_s, clk):
     """Roofline of the dominant kernel. The fused kernel keeps every Newton
     iteration on chip (its DRAM traffic is the parameters in and the states
-    out), and ncu shows its busiest pipe is FP64 (the device currents and
-    charges, the residual and the convergence test); so it is placed against
-    the GPU's FP64 rate (cuBLAS DGEMM, measured here). Its FP64 work per
-    Newton iteration is the ncu count of FP64 operations of the 512-instance
-    capture divided by that launch's Newton iterations. The HBM frame of an
-    unfused implementation is kept for context."""
+    out), and its busiest pipe is FP64 (device currents and charges, the
+    residual, the update): it is placed against the FP64 rate. The HBM frame
+    of an unfused implementation of the same step is kept for context."""
     fe = int(st.plan.stats["factor_entries"])
     bytes_per_iter = 8 * st.nnz + 4 * (st.nnz + 2 * fe) + 8 * 6 * st.size
     hbm_peak = float(g.peaks.get("hbm_gbs", 6800.0))
     hbm = {"achieved_gbs": bytes_per_iter * total_iters / step_s / 1e9, "peak_gbs": hbm_peak,
            "peak_source": "measured" if g.peaks else "fallback",
            "algorithmic_bytes_per_launch": bytes_per_iter * total_iters}
-    if engine_used != "fused" or FUSED_FP64_FLOP_PER_ITER is None:
+    flop = FUSED_FP64_FLOP_PER_ITER.get(w.name)
+    if engine_used != "fused" or flop is None or call32.block == 32:
         return {"bound": "hbm", "kernel": "factor/solve level kernels"
                 if engine_used != "fused" else "fused_kernel<float>",
                 "achieved": hbm["achieved_gbs"], "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm["achieved_gbs"] / hbm_peak, "traffic": None,
                 "peak_source": hbm["peak_source"],
                 "newton_iterations_per_launch": total_iters}
+    sms = g.torch.cuda.get_device_properties(g.dev).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    peak = 2 * 2 * sms * mhz * 1e6 / 1e12
+    achieved = flop * total_iters / step_s / 1e12
     packed = sum(t.numel() * 8 for t in call32.keep)
-    traffic = packed + B * n_t * (8 * st.size + 8)
-    peak = g.fp64_peak()
-    flops = FUSED_FP64_FLOP_PER_ITER * total_iters
-    achieved = flops / step_s / 1e12
-    return {"bound": "fp64", "kernel": f"fused_kernel<float,{call32.block}>"
-            if call32.block != 32 else "fused_warp_kernel<float>",
+    return {"bound": "fp64", "kernel": f"fused_kernel<float,{call32.block}>",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": traffic,
-            "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch float64 matmul)",
-            "fp64_flop_per_newton_iter": FUSED_FP64_FLOP_PER_ITER,
-            "newton_iterations_per_launch": total_iters,
-            "unfused_hbm_frame": hbm,
-            "ncu": FUSED_NCU}
+            "traffic": packed + B * n_t * (8 * st.size + 8),
+            "peak_source": f"FP64 pipe: 2 DFMA/cycle/SM (ncu peak) x {sms} SMs x {mhz:.0f} MHz",
+            "fp64_flop_per_newton_iter": flop, "newton_iterations_per_launch": total_iters,
+            "unfused_hbm_frame": hbm, "ncu": FUSED_NCU}
 
 
 def main():
