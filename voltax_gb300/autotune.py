@@ -5,9 +5,9 @@ topology and the batch: the fused persistent kernel keeps an instance on
 one CTA (best when several CTAs fit an SM), the generic level kernels
 spread every instance over the whole GPU (best when the fused kernel's
 shared-memory footprint leaves one narrow CTA per SM). `choose` times the
-candidates -- the fused kernel at 64, 128, 256 and 512 threads per
-instance (one CTA each) and the generic engine -- on a few DC Newton
-iterations of the caller's own
+candidates -- the fused kernel at 128, 256 and 512 threads per instance
+(one CTA each) and the generic engine -- on a few DC Newton iterations of
+the caller's own
 instances, and keeps the fastest per (topology, precision, batch size
 class). Each trial runs on scratch copies; nothing the caller owns is
 written.
@@ -29,11 +29,12 @@ from .runtime import stream_ptr
 
 TRIAL_STEPS = 3
 TRIAL_INSTANCES = 4096
-# The fused kernel with one warp per instance (block 32) is not a candidate:
-# a DC trial favours it, but on the transients it runs slower than a CTA per
-# instance (4-bit adder, 4096 instances: 2.35 M vs 2.56 M solves/s). Pin it
-# with Options(block=32).
-BLOCKS = (64, 128, 256, 512)
+# The fused kernel with one warp per instance (block 32) or 64 threads per
+# instance is not a candidate: a DC trial favours them, but on the
+# transients they run slower than 128-thread CTAs (4-bit adder, 4096
+# instances: 2.35 M and 2.18 M vs 2.56 M solves/s). Pin them with
+# Options(block=32) or Options(block=64).
+BLOCKS = (128, 256, 512)
 
 _cache: dict[tuple, tuple[str, int]] = {}
 
