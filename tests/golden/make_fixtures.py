@@ -12,7 +12,9 @@ by ``voltax_gb300.builder`` (the same ``(layout, groups)`` key voltax's
 * the plan: per bucket, each supernode's pivot unknowns and border, and the
   plan statistics (``_make_plan``).
 
-Run from the repository root:  ``python tests/golden/make_fixtures.py``.
+Run from the repository root with the reference's source tree given by the
+``VOLTAX_REFERENCE`` environment variable or the first argument:
+``python tests/golden/make_fixtures.py <voltax source root>``.
 The reference tree is only read here; the fixtures are committed.
 """
 
@@ -28,7 +30,10 @@ from pathlib import Path
 import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
-REF = Path("/root/reference/voltax/sparse.py")
+import os  # noqa: E402
+
+_REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VOLTAX_REFERENCE")
+REF = Path(_REF_ROOT) / "voltax" / "sparse.py" if _REF_ROOT else None
 OUT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -59,6 +64,8 @@ def load_reference_sparse():
     elem.Element = Element
     sys.modules.update({"jax": jax, "jax.numpy": jnp, "voltax": pkg,
                         "voltax.element": elem})
+    if REF is None:
+        raise SystemExit("give the voltax source root as an argument or in VOLTAX_REFERENCE")
     spec = importlib.util.spec_from_file_location("voltax.sparse", REF)
     mod = importlib.util.module_from_spec(spec)
     sys.modules["voltax.sparse"] = mod
