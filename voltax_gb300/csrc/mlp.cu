@@ -5,85 +5,36 @@
 //
 // Layers are y = act(x W^T + b) with W stored [out, in] in BF16, bias in
 // FP32, activations in BF16 and every product accumulated in FP32 on the
-// tensor cores (mma.sync m16n8k16 BF16). One GEMM kernel serves the forward
-// pass and both backward products; it reads its two operands through
-// (outer, reduction) strides, so no operand is ever transposed in memory:
+// fifth-generation tensor cores (tcgen05.mma kind::f16, accumulators in
+// tensor memory, tc::product_bf16). One GEMM kernel serves the forward pass
+// and both backward products; it reads its two operands through (outer,
+// reduction) strides, so no operand is ever transposed in memory:
 //
 //   forward   Y[m,n]  = sum_k X[m,k]  W[n,k]      A = X,    B = W
 //   data grad dX[m,k] = sum_n dY[m,n] W[n,k]      A = dY,   B = W^T (strides)
 //   weight    dW[n,k] = sum_m dY[m,n] X[m,k]      A = dY^T, B = X^T (strides)
 //
-// Each output element is owned by one thread and reduced in a fixed order:
-// every kernel here is bitwise reproducible run to run.
-//
-// Shapes are small (hidden 512): one 64x64 output tile per 128-thread CTA,
-// 32-wide reduction slabs staged in shared memory.
+// The tensor core's accumulation order is fixed and every other reduction
+// here runs in a fixed order: the kernels are bitwise reproducible run to
+// run.
 
 #include <cuda_bf16.h>
 
 #include "internal.cuh"
+#include "tc.cuh"
 
 namespace vxg {
 namespace {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int BM = 64, BN = 64, BK = 32, PAD = 8, NTH = 128;
+constexpr int BM = 64, BN = 64;  // tile sizes of the launch-size checks
 
 // Element (o, r) of an operand is p[o * so + r * sr].
 struct Operand {
   const bf16* p;
   long long so, sr;
 };
-
-__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
-  return *reinterpret_cast<const uint32_t*>(p);
-}
-
-// Stage rows [o0, o0 + 64) x reduction [r0, r0 + 32) of `op` into s; zero
-// outside [0, O) x [0, R). Consecutive threads walk the operand's unit-stride
-// dimension so the global reads coalesce.
-__device__ __forceinline__ void stage(bf16 (*s)[BK + PAD], const Operand& op, long long o0,
-                                      int r0, long long O, int R) {
-  const bf16 zero = __float2bfloat16_rn(0.f);
-  // 16-byte loads when the reduction dimension is contiguous, rows start on
-  // 16-byte boundaries and the slab is complete
-  const bool vec = op.sr == 1 && (op.so & 7) == 0 &&
-                   (reinterpret_cast<uintptr_t>(op.p) & 15) == 0 && r0 + BK <= R;
-  if (vec) {
-    for (int e = threadIdx.x; e < BM * BK / 8; e += NTH) {
-      const int o = e / (BK / 8), c8 = (e % (BK / 8)) * 8;
-      const long long go = o0 + o;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (go < O) v = *reinterpret_cast<const uint4*>(op.p + go * op.so + r0 + c8);
-      *reinterpret_cast<uint4*>(&s[o][c8]) = v;
-    }
-    return;
-  }
-  if (op.sr == 1) {
-    for (int e = threadIdx.x; e < BM * BK; e += NTH) {
-      const int o = e / BK, r = e % BK;
-      const long long go = o0 + o;
-      const int gr = r0 + r;
-      s[o][r] = (go < O && gr < R) ? op.p[go * op.so + gr] : zero;
-    }
-  } else {
-    for (int e = threadIdx.x; e < BM * BK; e += NTH) {
-      const int o = e % BM, r = e / BM;
-      const long long go = o0 + o;
-      const int gr = r0 + r;
-      s[o][r] = (go < O && gr < R) ? op.p[go * op.so + gr * op.sr] : zero;
-    }
-  }
-}
 
 __device__ __forceinline__ float gelu(float v) {
   return 0.5f * v * (1.f + erff(v * 0.70710678118654752f));
@@ -94,65 +45,35 @@ __device__ __forceinline__ float gelu_grad(float v) {
          v * 0.39894228040143268f * expf(-0.5f * v * v);
 }
 
-// C[o1, o2] = sum_r A(o1, r) B(o2, r) for o1 < M1, o2 < M2, r < R; each
-// element handed to `epi(o1, o2, value)`. grid.x: tiles of o1, grid.y: o2.
+// C[o1, o2] = sum_r A(o1, r) B(o2, r) on the fifth-generation tensor cores: BF16 operands from
+// the strided views, FP32 accumulation in tensor memory (tc::product_bf16),
+// 128 x 64 output tiles, 128 threads; every output goes through `epi`.
 template <class Epi>
-__global__ void __launch_bounds__(NTH) gemm_kernel(long long M1, int M2, int R, Operand a,
-                                                   Operand b, Epi epi) {
-  __shared__ __align__(16) bf16 As[BM][BK + PAD];
-  __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
-  const long long m0 = (long long)blockIdx.x * BM;
-  const int n0 = blockIdx.y * BN;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  const int gid = lane >> 2, tig = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+__global__ void __launch_bounds__(128) gemm_tc_kernel(long long M1, int M2, int R, Operand a,
+                                                      Operand b, Epi epi) {
+  extern __shared__ __align__(1024) unsigned char smem_tc[];
+  __shared__ uint32_t tmem_slot;
+  tc::ProductState ps;
+  tc::product_begin(ps, smem_tc, &tmem_slot);
+  tc::product_bf16<128>(
+      ps, M1, M2, R,
+      [&](long long o, int r) { return __bfloat16_as_ushort(a.p[o * a.so + r * a.sr]); },
+      [&](long long o, int r) { return __bfloat16_as_ushort(b.p[o * b.so + r * b.sr]); },
+      [&](long long m, int n, float v) { epi(m, n, v); });
+  tc::product_end(ps);
+}
 
-  for (int r0 = 0; r0 < R; r0 += BK) {
-    stage(As, a, m0, r0, M1, R);
-    stage(Bs, b, n0, r0, M2, R);
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm + i * 16 + gid;
-        af[i][0] = ld_pair(&As[r][kk + tig * 2]);
-        af[i][1] = ld_pair(&As[r + 8][kk + tig * 2]);
-        af[i][2] = ld_pair(&As[r][kk + tig * 2 + 8]);
-        af[i][3] = ld_pair(&As[r + 8][kk + tig * 2 + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = wn + j * 8 + gid;
-        bfr[j][0] = ld_pair(&Bs[c][kk + tig * 2]);
-        bfr[j][1] = ld_pair(&Bs[c][kk + tig * 2 + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const long long row = m0 + wm + i * 16 + gid;
-      const int col = n0 + wn + j * 8 + tig * 2;
-      epi(row, col, acc[i][j][0]);
-      epi(row, col + 1, acc[i][j][1]);
-      epi(row + 8, col, acc[i][j][2]);
-      epi(row + 8, col + 1, acc[i][j][3]);
-    }
+template <class Epi>
+int launch_gemm(long long M1, int M2, int R, const Operand& a, const Operand& b, const Epi& epi,
+                cudaStream_t s) {
+  const size_t smem = tc::kProductSmem + 1024;
+  VXG_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<Epi>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const dim3 grid((unsigned)((M1 + tc::kTileM - 1) / tc::kTileM),
+                  (unsigned)((M2 + tc::kTileN - 1) / tc::kTileN));
+  gemm_tc_kernel<Epi><<<grid, 128, smem, s>>>(M1, M2, R, a, b, epi);
+  VXG_LAUNCHED();
+  return VXG_OK;
 }
 
 // y = act(acc + bias): pre-activation (FP32), activation (BF16), raw output
@@ -319,10 +240,7 @@ extern "C" int vxg_mlp_linear(int64_t M, int32_t N, int32_t K, const void* x_bf1
   if (!grid_ok(mt, nt)) return VXG_ERR_TOO_LARGE;
   FwdEpi epi{M, N, act, bias, pre, (bf16*)y_bf16, y_f32, scale, shift, z, ldz};
   Operand a{(const bf16*)x_bf16, K, 1}, b{(const bf16*)w_bf16, K, 1};
-  gemm_kernel<<<dim3((unsigned)mt, (unsigned)nt), NTH, 0, (cudaStream_t)stream>>>(M, N, K, a, b,
-                                                                                  epi);
-  VXG_LAUNCHED();
-  return VXG_OK;
+  return launch_gemm(M, N, K, a, b, epi, (cudaStream_t)stream);
 }
 
 extern "C" int vxg_mlp_linear_dx(int64_t M, int32_t N, int32_t K, const void* dy_bf16,
@@ -334,10 +252,7 @@ extern "C" int vxg_mlp_linear_dx(int64_t M, int32_t N, int32_t K, const void* dy
   // dX[m, k] = sum_n dY[m, n] W[n, k]: A(m, n) = dy[m*N + n], B(k, n) = w[n*K + k]
   Operand a{(const bf16*)dy_bf16, N, 1}, b{(const bf16*)w_bf16, 1, K};
   DxEpi epi{M, K, pre, (bf16*)dx_bf16};
-  gemm_kernel<<<dim3((unsigned)mt, (unsigned)kt), NTH, 0, (cudaStream_t)stream>>>(M, K, N, a, b,
-                                                                                  epi);
-  VXG_LAUNCHED();
-  return VXG_OK;
+  return launch_gemm(M, K, N, a, b, epi, (cudaStream_t)stream);
 }
 
 extern "C" int vxg_mlp_linear_dw(int64_t M, int32_t N, int32_t K, const void* dy_bf16,
@@ -350,8 +265,8 @@ extern "C" int vxg_mlp_linear_dw(int64_t M, int32_t N, int32_t K, const void* dy
   Operand a{(const bf16*)dy_bf16, 1, N}, b{(const bf16*)x_bf16, 1, K};
   DwEpi epi{N, K, dw};
   cudaStream_t s = (cudaStream_t)stream;
-  gemm_kernel<<<dim3((unsigned)nt, (unsigned)kt), NTH, 0, s>>>(N, K, (int)M, a, b, epi);
-  VXG_LAUNCHED();
+  const int st = launch_gemm(N, K, (int)M, a, b, epi, s);
+  if (st != VXG_OK) return st;
   if (db) {
     colsum_kernel<<<blocks_for(N, 128), 128, 0, s>>>(M, N, (const bf16*)dy_bf16, db);
     VXG_LAUNCHED();

@@ -276,3 +276,106 @@ __device__ void product_3xtf32(ProductState& s, int M, int N, int K, LA la, LB l
 
 }  // namespace tc
 }  // namespace vxg
+
+namespace vxg {
+namespace tc {
+
+// kind::f16 with BF16 operands, FP32 accumulation, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                      // D: FP32
+         | (1u << 7)                    // A: BF16
+         | (1u << 10)                   // B: BF16
+         | ((uint32_t)(N >> 3) << 17)   // N / 8
+         | ((uint32_t)(M >> 4) << 24);  // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "setp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Byte offset of 16-bit element (r, k) of a staged K-major tile whose slab
+// holds 64 elements per row: the same core-matrix layout as tile_offset
+// (8 elements per 16-byte core-matrix row).
+__device__ __forceinline__ uint32_t tile_offset16(int r, int k) {
+  return (uint32_t)(r >> 3) * kSbo + (uint32_t)(k >> 3) * kLbo + (uint32_t)(r & 7) * 16u +
+         (uint32_t)(k & 7) * 2u;
+}
+
+// C = A B with BF16 operands (16-bit patterns from la(m, k), lb(n, k): B is
+// given N x K) accumulated in FP32 on the tensor cores: 128 x 64 output
+// tiles, 64-element slabs (four K = 16 MMAs each), the same staging, waits
+// and read-out as product_3xtf32, in the A-hi / B-hi buffers of `s`.
+template <int NT, class LA, class LB, class ST>
+__device__ void product_bf16(ProductState& s, long long M, int N, int K, LA la, LB lb, ST st,
+                             int limit = 1 << 20) {
+  static_assert(NT % 128 == 0, "product_bf16 needs a multiple of 4 warps");
+  constexpr int kSlab16 = 64;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
+  unsigned char* at = reinterpret_cast<unsigned char*>(s.a_hi);
+  unsigned char* bt = reinterpret_cast<unsigned char*>(s.b_hi);
+  for (long long m0 = (long long)blockIdx.x * kTileM; m0 < M && s.ok;
+       m0 += (long long)gridDim.x * kTileM)
+    for (int n0 = blockIdx.y * kTileN; n0 < N && s.ok; n0 += gridDim.y * kTileN) {
+      for (int k0 = 0; k0 < K && s.ok; k0 += kSlab16) {
+        for (int e = tid; e < kTileM * kSlab16; e += NT) {
+          const int r = e / kSlab16, k = e - r * kSlab16;
+          const uint16_t x = (m0 + r < M && k0 + k < K) ? la(m0 + r, k0 + k) : (uint16_t)0;
+          *reinterpret_cast<uint16_t*>(at + tile_offset16(r, k)) = x;
+        }
+        for (int e = tid; e < kTileN * kSlab16; e += NT) {
+          const int n = e / kSlab16, k = e - n * kSlab16;
+          const uint16_t y = (n0 + n < N && k0 + k < K) ? lb(n0 + n, k0 + k) : (uint16_t)0;
+          *reinterpret_cast<uint16_t*>(bt + tile_offset16(n, k)) = y;
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+          fence_after_sync();
+#pragma unroll
+          for (int step = 0; step < kSlab16 / 16; ++step) {
+            const uint32_t off = 256u * step;
+            mma_bf16(s.tmem, smem_desc(at + off), smem_desc(bt + off), idesc,
+                     (k0 > 0 || step > 0) ? 1u : 0u);
+          }
+          mma_commit(s.bar);
+        }
+        if (!mbar_wait(s.bar, s.phase, limit)) s.ok = 0;
+        s.phase ^= 1u;
+        s.ok = __syncthreads_and(s.ok);
+      }
+      if (!s.ok) break;
+      fence_after_sync();
+      for (int chunk = warp >> 2; chunk < kTileN / 16; chunk += NT / 128) {
+        float v[16];
+        tmem_ld16(s.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 16u * chunk, v);
+        const long long m = m0 + 32 * (warp & 3) + lane;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int n = n0 + 16 * chunk + i;
+          if (m < M && n < N) st(m, n, v[i]);
+        }
+      }
+      fence_before_sync();
+      __syncthreads();
+    }
+  if (!s.ok)  // a wait gave up: every output of this CTA's tiles becomes NaN
+    for (long long m0 = (long long)blockIdx.x * kTileM; m0 < M; m0 += (long long)gridDim.x * kTileM)
+      for (int n0 = blockIdx.y * kTileN; n0 < N; n0 += gridDim.y * kTileN)
+        for (int e = tid; e < kTileM * kTileN; e += NT) {
+          const long long m = m0 + e / kTileN;
+          const int n = n0 + e % kTileN;
+          if (m < M && n < N) st(m, n, __int_as_float(0x7fc00000));
+        }
+}
+
+}  // namespace tc
+}  // namespace vxg
