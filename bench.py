@@ -915,8 +915,7 @@ def measure_grids(g, a, w, cpu=None):
 
     e2e()
     t_e2e = timed(e2e, a.steps)
-    sides = [int(round((np.sum(circuit.unknown_segments()[:nv] == k)) ** 0.5))
-             for k in range(n_grids)]
+    sides = wl_sides(n_grids)
     res = {
         "value": n_grids * a.steps / t_fwd, "unit": UNIT, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * t_fwd / a.steps,
