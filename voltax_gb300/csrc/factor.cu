@@ -73,9 +73,11 @@ __device__ __forceinline__ void tile_product(int nr, int nc, int k, const T* X, 
   }
 }
 
-// Supernodes at least this wide take their Schur product S = F21 Ub on the
-// tensor cores in the FP32 form (3xTF32, tc::product_3xtf32).
-constexpr int kTcMinK = 64;
+// Supernodes at least this wide, with borders at least this long, take
+// their Schur product S = F21 Ub (r x k times k x r) on the tensor cores in
+// the FP32 form (3xTF32, tc::product_3xtf32); narrower products would be
+// mostly padding of the 128 x 64 tensor-core tile.
+constexpr int kTcMinK = 64, kTcMinR = 64;
 
 template <typename T, int NT, bool Wide, bool TC = false>
 __global__ void __launch_bounds__(NT)
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(NT)
   // the Schur block, so the factorization reports non-finite values.
   bool schur_done = false;
   if constexpr (TC) {
-    if (k >= kTcMinK) {
+    if (k >= kTcMinK && r >= kTcMinR) {
       __shared__ uint32_t tmem_slot;
       const uint32_t used = tc::smem_u32(perm + k);
       unsigned char* tcbuf = reinterpret_cast<unsigned char*>(perm + k) +
@@ -314,7 +316,7 @@ static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t
     int st = VXG_OK;
     bool launched = false;
     if constexpr (std::is_same<T, float>::value) {
-      if (kmax >= kTcMinK && t.h_lv_rmax[L] > 0) {  // Schur products on the tensor cores
+      if (kmax >= kTcMinK && t.h_lv_rmax[L] >= kTcMinR) {  // Schur products on the tensor cores
         const bool wide = factor_smem_bytes(kmax, 4, false, true) > (size_t)max_optin;
         smem = factor_smem_bytes(kmax, 4, wide, true);
         if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
