@@ -233,7 +233,14 @@ int vxg_spsolve_gdata(const vxg_handle* h, int32_t batch, const double* g, const
  * converged, iters (B*n_seg int32) are written. Instances that converge are
  * frozen while others iterate (vmap semantics). If factors != NULL the
  * factors of the final Jacobian, at the returned z, are left there (for the
- * adjoint). */
+ * adjoint). The loop runs on the device: the call enqueues one CUDA graph
+ * (a conditional WHILE node over one Newton iteration) on `stream` and
+ * returns without waiting; its counters live in `workspace`, so calls from
+ * several threads on one handle need their own streams and workspaces.
+ * The graph is instantiated on the first call with a given set of
+ * arguments and cached on the handle. A stream that is being captured is
+ * refused (VXG_ERR_INVALID): a graph with a conditional node cannot be
+ * nested in the caller's graph. */
 int vxg_newton(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
                int32_t mode, double t, double t_prev, const double* z_prev,
                const double* gmin, double gmin_scalar, const vxg_newton_opts* opts,
@@ -250,8 +257,10 @@ int vxg_newton_masked(const vxg_handle* h, int32_t batch, const vxg_group_params
                       double* z, int32_t* converged, int32_t* iters, const int32_t* mask,
                       void* workspace, void* stream);
 
-/* Fused transient: for n_t time points ts (host), starting from z0 (B x S),
- * one vxg_newton per step with guess z_prev (voltax/analysis.py:434-480).
+/* Transient: for n_t time points ts (host), starting from z0 (B x S),
+ * one vxg_newton per step with guess z_prev (voltax/analysis.py:434-480),
+ * all enqueued on `stream` without host synchronisation (one uncached
+ * Newton graph per step).
  * z_out: n_t x B x S (row 0 = z0); converged, iters: n_t x B*n_seg. */
 int vxg_transient(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
                   int32_t mode, int32_t n_t, const double* ts, const double* z0,
