@@ -1096,12 +1096,22 @@ struct Instance {
   }
 };
 
-// Threads per SM the register allocation is sized for (resident CTAs x NT):
-// 640 lets five 128-thread CTAs share an SM (measured on the 4096-instance
-// adder: 2.32 M vs 2.14 M solves/s with 512, i.e. four CTAs).
+// Resident CTAs per SM the register allocation is sized for. FP32 with
+// 128-thread CTAs: six (85 registers a thread; on the 4096-instance adder
+// 2.63 M solves/s against 2.57 M with five and 2.14 M with four, the extra
+// spills of the smaller budget notwithstanding). FP64, whose spills grow
+// faster, and larger blocks: 640 threads per SM (five 128-thread CTAs, two
+// 256-thread CTAs at 128 registers, one 512-thread CTA).
 #ifndef VXG_FUSED_THREADS_PER_SM
 #define VXG_FUSED_THREADS_PER_SM 640
 #endif
+#ifndef VXG_FUSED_CTAS_128
+#define VXG_FUSED_CTAS_128 6
+#endif
+template <typename T, int NT>
+constexpr int fused_ctas_per_sm() {
+  return (NT == 128 && sizeof(T) == 4) ? VXG_FUSED_CTAS_128 : VXG_FUSED_THREADS_PER_SM / NT;
+}
 
 // Point an instance's buffers into its shared-memory region `base`.
 template <typename T, int NT, bool kWarp>
@@ -1202,7 +1212,7 @@ __device__ __forceinline__ void stage_tables(const FusedArgs& A, unsigned char* 
 
 // One CTA per instance (grid-stride over the batch).
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, VXG_FUSED_THREADS_PER_SM / NT)
+__global__ void __launch_bounds__(NT, fused_ctas_per_sm<T, NT>())
     fused_kernel(const __grid_constant__ FusedArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const FusedLayout L =
