@@ -72,8 +72,14 @@ enum {
   VXG_KIND_IDEAL_OPAMP = 14,/* IdealOpAmp   [unused], (inp, inn, out) + output current */
   VXG_KIND_OPAMP = 15,      /* OpAmp        [a0, 1/rout, tau, mid, half, 1/half],
                                              (inp, inn, out) + state x          */
-  VXG_KIND_SWITCH = 16      /* Switch       [log roff, log(roff/ron), vth, 1/vwidth],
+  VXG_KIND_SWITCH = 16,     /* Switch       [log roff, log(roff/ron), vth, 1/vwidth],
                                              (p, n, cp, cn)                     */
+  VXG_KIND_COUPLED_L = 17   /* CoupledInductors [l, sqrt l, k], (p, n) + current i.
+                               A non-local group (voltax/element.py:30-34,
+                               sparse.py:245-247): the flux of device d is
+                               sum_e M_de i_e, M_de = k sqrt(l_d l_e) for e != d
+                               and l_d for e = d, so device d's three rows take
+                               all 3 n unknowns of the group as columns.       */
 };
 enum { VXG_WAVE_CONSTANT = 0, VXG_WAVE_STEP = 1, VXG_WAVE_PULSE = 2 };
 
@@ -113,7 +119,8 @@ typedef struct {
   int64_t n_res_slots;    /* sum over groups of n*(T+K) */
   const int64_t* res_ptr; /* S+1 */
   const int64_t* res_src; /* storage slot ids per row, in summation order */
-  int64_t n_jac_slots;    /* sum over groups of n*(T+K)^2 */
+  int64_t n_jac_slots;    /* sum over groups of n*(T+K)^2; (n*(T+K))^2 for a
+                             non-local group (VXG_KIND_COUPLED_L) */
   const int64_t* jac_ptr; /* nnz+1 */
   const int64_t* jac_src; /* storage slot ids per entry, in summation order */
   /* independent sub-circuits (segments) inside the topology */

@@ -15,6 +15,8 @@ F)`` and ``charges(v, x) -> (Q, P)`` written exactly as voltax writes them:
 * BJT                 voltax/elements/semiconductor.py:73-135
 * VCVS, CCCS, CCVS    voltax/elements/controlled.py:27-98
 * Transformer         voltax/elements/passive.py:90-129
+* CoupledInductors    the non-local element of voltax tests/test_sparse.py:90-113
+                      (``local = False``: a full mutual-inductance matrix)
 * IdealOpAmp, OpAmp   voltax/elements/opamp.py:13-103
 * Switch              voltax/elements/switch.py:14-50
 * EKVMOSFET           voltax/elements/mosfet.py:127-205 (softplus is
@@ -99,7 +101,8 @@ class GroupModel:
         self.T = len(el.terminals)
         self.K = el.n_internal
         self.has_charges = self.name in ("Capacitor", "EKVMOSFET", "Level1MOSFET", "Diode",
-                                         "Inductor", "BJT", "Transformer", "OpAmp")
+                                         "Inductor", "BJT", "Transformer", "OpAmp",
+                                         "CoupledInductors")
 
     # ---------------------------------------------------------------- physics
     def currents(self, v, x, t):
@@ -121,6 +124,9 @@ class GroupModel:
             return torch.stack([i, -i], -1), None
         if name == "Capacitor":
             return None, None
+        if name == "CoupledInductors":  # through(i), -(v_p - v_n)
+            i = x[..., 0]
+            return torch.stack([i, -i], -1), (-(v[..., 0] - v[..., 1]))[..., None]
         if name == "VoltageSource":
             i = x[..., 0]
             val = signal_value(el.value, t, b)
@@ -238,6 +244,12 @@ class GroupModel:
         if name == "OpAmp":  # opamp.py:102-103: tau x on the state row
             tau = torch.exp(_inst(el.log_a0, b)) / (2 * math.pi * torch.exp(_inst(el.log_gbw, b)))
             return None, (tau * x[..., 0])[..., None]
+        if name == "CoupledInductors":  # M = k sqrt(l l^T) (1 - I) + diag(l)
+            ll = torch.exp(_inst(el.log_l, b))
+            root = torch.sqrt(ll)
+            n = ll.shape[0]
+            M = el.k * torch.outer(root, root) * (1 - torch.eye(n, dtype=F64)) + torch.diag(ll)
+            return None, (M @ x[..., 0])[..., None]
         if name == "Transformer":  # passive.py:125-129
             i1, i2 = x[..., 0], x[..., 1]
             l1, l2 = torch.exp(_inst(el.log_l1, b)), torch.exp(_inst(el.log_l2, b))
@@ -339,6 +351,13 @@ class GroupModel:
         if cq != 0:
             out = out + cq * part(*self.charges(v, x))
         return out
+
+    def group_jacobian(self, u, t, cf, cq):
+        """A non-local group's ``(N m, N m)`` block ``d out / d u`` over all
+        its unknowns, device-major (voltax/sparse.py:245-247's jacfwd)."""
+        n, m = u.shape
+        flat = lambda uu: self.outputs(uu.reshape(n, m), t, cf, cq).reshape(-1)  # noqa: E731
+        return torch.func.jacfwd(flat)(u.reshape(-1))
 
     def local_jacobian(self, u, t, cf, cq):
         """``(N, m, m)`` blocks ``d out[d, i] / d u[d, j]`` by forward-mode AD

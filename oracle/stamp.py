@@ -66,7 +66,8 @@ def q(circuit, z, b: int = 0) -> np.ndarray:
 
 
 def local_blocks(circuit, st, z, t, cf, cq, b: int = 0):
-    """Per group ``(positions (N, m, m), values (N, m, m))`` in layout order."""
+    """Per group ``(positions, values)`` in layout order: ``(N, m, m)`` local
+    blocks, or one ``(N m, N m)`` block for a non-local group."""
     z = np.asarray(z, np.float64)
     z_ext = np.concatenate([z, [0.0]])
     out = []
@@ -76,7 +77,8 @@ def local_blocks(circuit, st, z, t, cf, cq, b: int = 0):
         if cf == 0 and cq_g == 0:
             continue
         u0 = torch.as_tensor(z_ext[np.where(allv < 0, len(z_ext) - 1, allv)], dtype=F64)
-        vals = model.local_jacobian(u0, t, cf, cq_g).numpy()
+        vals = (model.local_jacobian(u0, t, cf, cq_g) if local
+                else model.group_jacobian(u0, t, cf, cq_g)).numpy()
         out.append((pos, vals))
     return out
 

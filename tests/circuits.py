@@ -113,3 +113,17 @@ def grid_via_builder(n, seed=0, prefix="", b=None, sigma=0.3, sink_max=1e-3, vpa
     for k, (i, j) in enumerate(grid_pads(n)):
         b.vsource(node(i, j), "0", vpad, name=f"{prefix}Vpad{k}")
     return b.build() if own else b
+
+
+def coupled_circuit(k=0.5):
+    """Three inductors sharing one mutual-inductance matrix (a non-local
+    group) behind a stepped source and resistors: nodes in=0, a=1, b=2, c=3
+    (the circuit of voltax tests/test_sparse.py:116-123)."""
+    import torch
+    import voltax_gb300 as vx
+    from voltax_gb300 import signals
+    return vx.Circuit({
+        "V": vx.VoltageSource((0, -1), signals.Step(0.0, 1.0, delay=1e-6, rise=1e-7)),
+        "R": vx.Resistor([(0, 1), (2, -1), (3, -1)], torch.tensor([10.0, 100.0, 1e3])),
+        "K": vx.CoupledInductors([(1, -1), (2, -1), (3, -1)], 1e-3, k=k),
+    }, ["in", "a", "b", "c"])

@@ -101,3 +101,51 @@ def test_linearize_matches_oracle_jacobians():
         ref[rows, st.indices] = ost.jacobian(c, st, z, 0.0, cf, cq)
         np.testing.assert_allclose(M.cpu().numpy(), ref, rtol=1e-12,
                                    atol=1e-15 * max(1.0, np.abs(ref).max()))
+
+
+def _rc_mesh(n, seed=0):
+    """An n x n RC mesh (lognormal branch conductances, a capacitor at every
+    node) driven at one corner by an AC source and tied down at the other."""
+    from voltax_gb300.builder import CircuitBuilder
+    rng = np.random.default_rng(seed)
+    b = CircuitBuilder()
+    b.vsource("n0_0", "0", 1.0, ac=1.0, name="Vin")
+    b.vsource(f"n{n - 1}_{n - 1}", "0", 0.0, name="Vgnd")
+    g = np.exp(rng.normal(0.0, 0.3, (2, n, n)))
+    cap = 1e-12 * (1.0 + rng.random((n, n)))
+    for i in range(n):
+        for j in range(n):
+            if j + 1 < n:
+                b.resistor(f"n{i}_{j}", f"n{i}_{j + 1}", 1.0 / g[0, i, j])
+            if i + 1 < n:
+                b.resistor(f"n{i}_{j}", f"n{i + 1}_{j}", 1.0 / g[1, i, j])
+            b.capacitor(f"n{i}_{j}", "0", cap[i, j])
+    return b.build()
+
+
+def test_ac_wide_supernode_matches_sparse_oracle():
+    """A 140 x 140 RC mesh: its root separator (k = 115) is too wide for the
+    complex factorization's shared memory, so the wide kernel (F11 left in
+    its panel) factors it. Reference: the oracle's stamped G and C solved by
+    scipy's sparse LU at each frequency."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    import voltax_gb300 as vx
+    from voltax_gb300 import symbolic
+    from oracle import stamp as ost
+    c = _rc_mesh(140)
+    st = symbolic.structure(c)
+    assert int(np.max(st.plan.k)) > 104
+    f = np.array([1e8, 1e10])
+    sol = vx.ac(c, f)
+    z_op = sol.op.z.cpu().numpy()
+    rows = np.repeat(np.arange(st.size), np.diff(st.indptr))
+    shape = (st.size, st.size)
+    G = sp.csr_matrix((ost.jacobian(c, st, z_op, 0.0, 1.0, 0.0), (rows, st.indices)), shape)
+    Cm = sp.csr_matrix((ost.jacobian(c, st, z_op, 0.0, 0.0, 1.0), (rows, st.indices)), shape)
+    rhs = -oa._ac_stimulus(c)
+    ref = np.stack([spl.splu((G + 2j * np.pi * fk * Cm).tocsc(), permc_spec="COLAMD").solve(rhs)
+                    for fk in f])
+    z = sol.z.cpu().numpy()
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    assert np.max(np.abs(z - ref) / scale) < 1e-10

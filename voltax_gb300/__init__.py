@@ -13,7 +13,8 @@ from .analysis import (ACSolution, Options, Solution, ac, dc, dc_sweep,  # noqa:
 from .builder import CircuitBuilder  # noqa: F401
 from .circuit import Circuit, Layout  # noqa: F401
 from .elements import (VT_300K, Capacitor, Conductance, CurrentSource,  # noqa: F401
-                       BJT, CCCS, CCVS, VCCS, VCVS, Diode, IdealOpAmp, OpAmp, Switch,
+                       BJT, CCCS, CCVS, VCCS, VCVS, CoupledInductors, Diode, IdealOpAmp,
+                       OpAmp, Switch,
                        Transformer, EKVMOSFET, Element, Inductor, Level1MOSFET,
                        MOSProcess, Resistor, VoltageSource, concatenate)
 

@@ -84,6 +84,12 @@ static P* at(void* base, size_t off) {
   return reinterpret_cast<P*>(static_cast<char*>(base) + off);
 }
 
+// Jacobian contribution slots of a group: an m x m block per device, or for
+// the non-local kind a row block of m rows by all n*m group unknowns.
+static long long jac_slots(int kind, long long n, long long m) {
+  return kind == VXG_KIND_COUPLED_L ? n * m * n * m : n * m * m;
+}
+
 GroupTable make_table(const Topo& t, const vxg_group_params* params) {
   GroupTable gt;
   std::memset(&gt, 0, sizeof(gt));
@@ -111,7 +117,7 @@ GroupTable make_table(const Topo& t, const vxg_group_params* params) {
     }
     dev += d.n;
     res += (long long)d.n * g.m;
-    jac += (long long)d.n * g.m * g.m;
+    jac += jac_slots(d.kind, d.n, g.m);
   }
   gt.n_dev = dev;
   return gt;
@@ -253,10 +259,10 @@ static bool build_blob(const vxg_topology_desc* d, std::vector<unsigned short>& 
 struct KindShape {
   int T, K, rows;
 };
-constexpr KindShape kShapes[VXG_KIND_SWITCH + 1] = {
+constexpr KindShape kShapes[VXG_KIND_COUPLED_L + 1] = {
     {2, 0, 1},  {2, 0, 1},  {2, 1, -1}, {2, 0, -1}, {4, 0, 13}, {4, 0, 12},
     {2, 0, 4},  {2, 1, 2},  {4, 0, 1},  {3, 0, 10}, {4, 1, 1},  {4, 1, 1},
-    {4, 2, 1},  {4, 2, 3},  {3, 1, 0},  {3, 1, 6},  {4, 0, 4}};
+    {4, 2, 1},  {4, 2, 3},  {3, 1, 0},  {3, 1, 6},  {4, 0, 4},  {2, 1, 3}};
 constexpr int kWaveRows[3] = {1, 4, 7};  // constant, step, pulse
 
 // Every index the kernels dereference lies inside its buffer: checked once
@@ -297,7 +303,7 @@ const char* validate(const vxg_topology_desc* d) {
   long long res = 0, jac = 0;
   for (int i = 0; i < d->n_groups; ++i) {
     const vxg_group_desc& g = d->groups[i];
-    if (g.kind < VXG_KIND_CONDUCTANCE || g.kind > VXG_KIND_SWITCH || g.n < 0)
+    if (g.kind < VXG_KIND_CONDUCTANCE || g.kind > VXG_KIND_COUPLED_L || g.n < 0)
       return "group kind or size";
     const KindShape sh = kShapes[g.kind];
     int rows = sh.rows;
@@ -314,7 +320,7 @@ const char* validate(const vxg_topology_desc* d) {
       return "group internal offset";
     const long long m = g.T + g.K;
     res += g.n * m;
-    jac += g.n * m * m;
+    jac += jac_slots(g.kind, g.n, m);
   }
   if (res != d->n_res_slots || jac != d->n_jac_slots) return "n_res_slots or n_jac_slots";
   if (!is_ptr(d->res_ptr, S, d->res_ptr[S]) || !is_ptr(d->jac_ptr, nnz, d->jac_ptr[nnz]))

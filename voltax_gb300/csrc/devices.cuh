@@ -415,12 +415,44 @@ __device__ __forceinline__ void l1_soa(const GroupDev& g, int b, int d, const do
 // Evaluate device d of group g (instance b) reading state zz; write its slots.
 // fo/qo/jo point at the group's first slot in each contribution array.
 // u: the device's local unknowns (terminal voltages, then internals).
+// zz: the instance's state, read by the non-local kind for the other
+// devices' unknowns.
 template <typename JT>
 __device__ __forceinline__ void eval_soa(const GroupDev& g, int b, int d, const double* u,
                                          double t, double cf, double cq, bool wf, bool wq,
-                                         bool wj, double* fo, double* qo, JT* jo) {
+                                         bool wj, double* fo, double* qo, JT* jo,
+                                         const double* zz) {
   const int n = g.n;
   switch (g.kind) {
+    case VXG_KIND_COUPLED_L: {  // u = (vp, vn, i); flux sum_e M_de i_e over the group
+      const double ld = prm(g, 0, b, d), sd = prm(g, 1, b, d), kc = prm(g, 2, b, d);
+      if (wf) {
+        fo[d] = u[2];
+        fo[n + d] = -u[2];
+        fo[2 * n + d] = -(u[0] - u[1]);
+      }
+      if (wq) {
+        double acc = 0.0;
+        for (int e = 0; e < n; ++e)
+          acc += (e == d ? ld : kc * (sd * prm(g, 1, b, e))) * zz[g.int_offset + e];
+        qo[d] = 0.0;
+        qo[n + d] = 0.0;
+        qo[2 * n + d] = acc;
+      }
+      if (wj) {  // rows (p, n, i) of device d; columns (vp, vn, i) of every device e
+        const long long W = 3LL * n;
+        for (long long c = 0; c < 3 * W; ++c) jo[c * n + d] = JT(0);
+        jo[(0 * W + 3 * d + 2) * n + d] = (JT)cf;
+        jo[(1 * W + 3 * d + 2) * n + d] = (JT)(-cf);
+        jo[(2 * W + 3 * d + 0) * n + d] = (JT)(-cf);
+        jo[(2 * W + 3 * d + 1) * n + d] = (JT)cf;
+        if (cq != 0.0)
+          for (int e = 0; e < n; ++e)
+            jo[(2 * W + 3 * e + 2) * n + d] =
+                (JT)(cq * (e == d ? ld : kc * (sd * prm(g, 1, b, e))));
+      }
+      break;
+    }
     case VXG_KIND_CONDUCTANCE: {
       const double gg = prm(g, 0, b, d);
       const double i = (u[0] - u[1]) * gg;

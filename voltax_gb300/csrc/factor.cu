@@ -14,13 +14,13 @@
 // (deterministic, no atomics): work[t] -= sum(S[src]).
 // (voltax/sparse.py:549-572)
 //
-// Wide supernodes of the real factorizations (F11 larger than a CTA's shared
-// memory: k above ~141 in FP64, ~211 in FP32; up to ~437 / ~870) run the
-// same kernel with F11 left in place in its panel (`Wide`): the Gauss-Jordan
-// steps read and write global memory, which the CTA's own barriers order
-// exactly as they order shared memory, and only the pivot row and column and
-// the 32-wide tiles are staged on chip. Every arithmetic operation and its
-// order are unchanged.
+// Wide supernodes (F11 larger than a CTA's shared memory: k above ~141 in
+// FP64, ~211 in FP32, ~104 in the complex AC factorization; up to ~437 /
+// ~870 / ~424) run the same kernel with F11 left in place in its panel
+// (`Wide`): the Gauss-Jordan steps read and write global memory, which the
+// CTA's own barriers order exactly as they order shared memory, and only the
+// pivot row and column and the 32-wide (complex: 16-wide) tiles are staged
+// on chip. Every arithmetic operation and its order are unchanged.
 
 #include <type_traits>
 
@@ -30,7 +30,10 @@
 
 namespace vxg {
 
-constexpr int kTile = 32;
+// Width of the staged F12 column tiles and F21 row tiles: 32 values, 16
+// for the complex (AC) factorization, whose 16-byte values would otherwise
+// leave too little shared memory for wide supernodes.
+__host__ __device__ constexpr int tile_width(size_t es) { return es > 8 ? 16 : 32; }
 
 template <typename T>
 __global__ void fill_panels_kernel(int B, long long nnz, const long long* __restrict__ a_pos,
@@ -101,6 +104,7 @@ __global__ void __launch_bounds__(NT)
   T* A = Wide ? F11 : base;               // k*k (on chip unless wide)
   T* col = Wide ? base : base + k * k;    // k: pivot column
   T* rowb = col + k;                      // k: scaled pivot row
+  constexpr int kTile = tile_width(sizeof(T));
   T* tA = rowb + k;                       // kTile*k
   T* tB = tA + kTile * k;                 // k*kTile
   int* perm = reinterpret_cast<int*>(tB + k * kTile);
@@ -257,7 +261,7 @@ __global__ void schur_apply_kernel(int B, long long ntgt, const long long* __res
 size_t factor_smem_bytes(int k, size_t es, bool wide = false, bool tc = false) {
   const size_t a = wide ? 0 : (size_t)k * k;
   const size_t base =
-      (a + 2 * (size_t)k + 2 * (size_t)kTile * k) * es + (size_t)k * sizeof(int) + 16;
+      (a + 2 * (size_t)k + 2 * (size_t)tile_width(es) * k) * es + (size_t)k * sizeof(int) + 16;
   return tc ? base + 1024 + tc::kProductSmem : base;  // + the tensor-core tiles, 1 KB aligned
 }
 
@@ -327,14 +331,10 @@ static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t
       }
     }
     if (launched) {
-    } else if (smem > (size_t)max_optin) {  // F11 stays in the panel (real factors only)
-      if constexpr (std::is_same<T, cplx>::value) {
-        return VXG_ERR_TOO_LARGE;
-      } else {
-        smem = factor_smem_bytes(kmax, sizeof(T), true);
-        if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
-        st = launch_level<T, 512, true>(grid, smem, t, lo, work, ws, scratch, ss, s);
-      }
+    } else if (smem > (size_t)max_optin) {  // F11 stays in the panel
+      smem = factor_smem_bytes(kmax, sizeof(T), true);
+      if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+      st = launch_level<T, 512, true>(grid, smem, t, lo, work, ws, scratch, ss, s);
     } else if (kmax > 80) {
       st = launch_level<T, 512, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
     } else if (kmax > 48) {

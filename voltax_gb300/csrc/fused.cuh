@@ -649,7 +649,7 @@ struct Instance {
         }
       }
       eval_soa<T>(g, b, d, u, t, cfc, cqc, wf, wq, wj, cf + g.res_base, cq + g.res_base,
-                  cj + g.jac_base);
+                  cj + g.jac_base, zz);
     }
   }
 
@@ -732,7 +732,7 @@ struct Instance {
         }
       }
       eval_soa<T>(g, b, d, u, t, cfc, cqc, false, false, true, nullptr, nullptr,
-                  cj + g.jac_base);
+                  cj + g.jac_base, zz);
     }
   }
 

@@ -416,9 +416,29 @@ __global__ void param_vjp_kernel(GroupTable gt, int B, const double* __restrict_
     u[g.T + i] = zb[g.int_offset + d * g.K + i];
     l[g.T + i] = lb[g.int_offset + d * g.K + i];
   }
+  double* out = grads.p[gi];
+  if (g.kind == VXG_KIND_COUPLED_L) {
+    // Device e's rows (l, sqrt l, k) enter the flux rows of every device:
+    // q_d = l_d i_d + k_d s_d sum_{e != d} s_e i_e (s = sqrt l), scaled by cq.
+    const int e = d, n = g.n;
+    const double* ib = zb + g.int_offset;
+    const double* lmb = lb + g.int_offset;
+    const double se = prm(g, 1, b, e);
+    double others = 0.0, cross = 0.0;  // sum_{e' != e} s_e' i_e'; sum_{d != e} lam_d k_d s_d
+    for (int q = 0; q < n; ++q) {
+      if (q == e) continue;
+      const double sq = prm(g, 1, b, q);
+      others += sq * ib[q];
+      cross += lmb[q] * prm(g, 2, b, q) * sq;
+    }
+    const double ke = prm(g, 2, b, e);
+    out[((long long)0 * B + b) * n + e] = -cq * lmb[e] * ib[e];
+    out[((long long)1 * B + b) * n + e] = -cq * (lmb[e] * ke * others + cross * ib[e]);
+    out[((long long)2 * B + b) * n + e] = -cq * lmb[e] * se * others;
+    return;
+  }
   Dual p[kMaxParams];
   for (int r = 0; r < g.n_params; ++r) p[r] = mk(prm(g, r, b, d));
-  double* out = grads.p[gi];
   for (int r = 0; r < g.n_params; ++r) {
     p[r].d = 1.0;
     Dual o[kMaxM];

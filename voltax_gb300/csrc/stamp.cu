@@ -32,11 +32,12 @@ __global__ void eval_kernel(GroupTable gt, int B, const double* __restrict__ z, 
   const GroupDev& g = gt.g[gi];
   const int d = (int)(flat - g.dev_base);
   double u[kMaxM];
-  gather_u(g, d, z + (long long)b * S, u);
+  const double* zb = z + (long long)b * S;
+  gather_u(g, d, zb, u);
   eval_soa<double>(g, b, d, u, t, cf, cq, want_f, want_q, want_j,
                    cf_buf + (long long)b * n_res_slots + g.res_base,
                    cq_buf + (long long)b * n_res_slots + g.res_base,
-                   cj_buf + (long long)b * n_jac_slots + g.jac_base);
+                   cj_buf + (long long)b * n_jac_slots + g.jac_base, zb);
 }
 
 // data[e] = sum of Jacobian slots of entry e (+ gmin on node diagonals)

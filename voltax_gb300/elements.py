@@ -50,6 +50,7 @@ KIND_XFMR = 13
 KIND_IDEAL_OPAMP = 14
 KIND_OPAMP = 15
 KIND_SWITCH = 16
+KIND_COUPLED_L = 17
 
 
 def _t(x) -> torch.Tensor:
@@ -549,6 +550,46 @@ class Inductor(Element):
 
     def gpu_params(self):
         return [torch.exp(self.log_l), self.rs.expand(self.log_l.shape)]
+
+
+class CoupledInductors(Element):
+    """``N`` inductors with a full mutual-inductance matrix across the group,
+    ``M = k sqrt(l l^T)`` off the diagonal and ``l`` on it: the flux of
+    device d is ``sum_e M_de i_e``. Its devices interact, so the group is
+    non-local (``local = False``, voltax/element.py:30-34, 76-79): its
+    Jacobian is one block over all ``3 N`` group unknowns, stamped at the
+    positions voltax gives a non-local group (voltax/sparse.py:87, 245-247).
+    Terminals ``(p, n)``, internal unknown the branch current ``i``; the
+    branch equation is ``d/dt sum_e M_de i_e - (v_p - v_n) = 0``.
+
+    Kernel parameter rows: l, sqrt(l), k (k shared by the group)."""
+
+    terminals = ("p", "n")
+    n_internal = 1
+    internal_names = ("i",)
+    fields = ("log_l",)
+    static = ("k",)
+    local = False
+    kind = KIND_COUPLED_L
+    has_charges = True
+
+    def __init__(self, nodes, l, k=0.5):
+        self.nodes = self._devices(nodes)
+        self.log_l = self._log_per_device(l)
+        self.k = float(k)
+
+    @property
+    def l(self):
+        return torch.exp(self.log_l)
+
+    def gpu_params(self):
+        l = torch.exp(self.log_l)
+        return [l, torch.sqrt(l), torch.full_like(l, self.k)]
+
+    def group_key(self) -> tuple:
+        """A coupled block never fuses with another one: each is its own
+        mutual-inductance matrix."""
+        return (type(self), id(self))
 
 
 class Diode(Element):

@@ -69,8 +69,6 @@ class Tables:
         res_base = jac_base = 0
         devices = list(zip(st.devices, st.stamps)) if circuit is not None else []
         for (name, allv, T, local), (_, pos, _) in devices:
-            if not local:
-                raise NotImplementedError("coupled (local=False) groups are not supported")
             el = circuit.elements[name]
             n, K, off = offsets[name]
             m = T + K
@@ -87,12 +85,15 @@ class Tables:
             res_tgt.append(tg.ravel())
             dd, ii = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
             res_id.append((res_base + ii * n + dd).ravel())
-            pj = pos.reshape(n, m * m).astype(np.int64)
+            # a non-local group's block covers all n*m group unknowns: device d
+            # owns rows d*m .. d*m+m-1 of it, each with n*m columns
+            w = m if local else n * m
+            pj = pos.reshape(n, m * w).astype(np.int64)
             jac_tgt.append(np.where(pj >= nnz, -1, pj).ravel())
-            dd, ee = np.meshgrid(np.arange(n), np.arange(m * m), indexing="ij")
+            dd, ee = np.meshgrid(np.arange(n), np.arange(m * w), indexing="ij")
             jac_id.append((jac_base + ee * n + dd).ravel())
             res_base += n * m
-            jac_base += n * m * m
+            jac_base += n * m * w
         self.n_res_slots, self.n_jac_slots = res_base, jac_base
         cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0, np.int64)  # noqa: E731
         self.res_ptr, self.res_src = self._pull(cat(res_tgt), cat(res_id), S)
