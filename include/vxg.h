@@ -217,6 +217,27 @@ int vxg_eval(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
 int vxg_factor(const vxg_handle* h, int32_t batch, int32_t precision, const double* data,
                void* factors, void* workspace, void* stream);
 
+/* Launch-shape autotuning of the factorization (no voltax counterpart:
+ * voltax's XLA program has no launch shapes). Each elimination level whose
+ * F11 fits in shared memory and whose Schur product stays on the CUDA
+ * cores runs its factor kernel at a CTA width of 128, 256 or 512 threads;
+ * the size rule picks one from the widest supernode. vxg_tune_factor times
+ * each such level at all three widths (best of three launches, in plan
+ * order, on the panels of `data`, B x nnz) and keeps the fastest for later
+ * factorizations of this handle in this precision (VXG_F64 or VXG_F32).
+ * factors and workspace are scratch of vxg_factor_size / vxg_workspace_size
+ * bytes whose contents are left undefined; widths (optional, n_levels
+ * entries, vxg_level_count) receives the choice, 0 for a level of fixed
+ * shape. The width changes no arithmetic: every sum keeps its order, so the
+ * factors are bitwise those of the size rule. vxg_set_factor_shapes sets the
+ * widths directly (0 = size rule; NULL resets every level). Both drop the
+ * handle's cached Newton graphs and synchronize nothing but the tuning
+ * stream; neither may run while another thread factors with the handle. */
+int vxg_level_count(const vxg_handle* h, int32_t* n_levels);
+int vxg_tune_factor(vxg_handle* h, int32_t batch, int32_t precision, const double* data,
+                    void* factors, void* workspace, int32_t* widths, void* stream);
+int vxg_set_factor_shapes(vxg_handle* h, int32_t precision, const int32_t* widths);
+
 /* x = A^-1 b (or A^-T b) with factors from vxg_factor; b, x are B x S FP64
  * (may alias). With VXG_F32 and data != NULL, `refine` FP64 refinement sweeps
  * r = b - A x follow the first solve. Replaces sparse.solve

@@ -42,3 +42,49 @@ def test_fused_block_widths_agree():
            for b in (128, 64, 256, 512, 32)]
     for other in out[1:]:
         assert float((out[0] - other).abs().max()) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_factor_widths_are_tuned_and_change_no_bits(precision):
+    """The generic engine's tile-shape tuner: one width per elimination
+    level (0 for a level of fixed shape), cached per (topology, precision,
+    batch class); and every width gives bitwise the same factors."""
+    import ctypes as C
+    import torch
+    import voltax_gb300 as vx
+    from voltax_gb300 import _lib as L
+    from voltax_gb300 import autotune, workloads
+    from voltax_gb300.analysis import _Call
+    from voltax_gb300.runtime import stream_ptr
+    autotune.clear()
+    c = workloads.power_grid(100)
+    call = _Call(c, vx.Options(precision=precision, engine="generic"))
+    widths = autotune.tune_factor(call)
+    eng = call.eng
+    nl = C.c_int32()
+    L.check(eng.lib.vxg_level_count(eng.handle, C.byref(nl)), "vxg_level_count")
+    assert len(widths) == nl.value > 0
+    assert set(widths) <= {0, 128, 256, 512} and any(widths)
+    assert autotune.tune_factor(call) == widths and len(autotune._widths) == 1
+    z = torch.zeros((1, eng.S), dtype=torch.float64, device=eng.device)
+    data = torch.empty((1, eng.nnz), dtype=torch.float64, device=eng.device)
+    L.check(eng.lib.vxg_eval(eng.handle, 1, call.params, z.data_ptr(), 0.0, 1.0, 0.0, None,
+                             1e-12, None, None, data.data_ptr(), call.ws.data_ptr(),
+                             stream_ptr()), "vxg_eval")
+    facs = []
+    for w in (None, 128, 256, 512):
+        arr = None if w is None else (C.c_int32 * nl.value)(*[w if x else 0 for x in widths])
+        L.check(eng.lib.vxg_set_factor_shapes(eng.handle, call.prec, arr),
+                "vxg_set_factor_shapes")
+        fac = eng.factor_buffer(1, call.prec)
+        L.check(eng.lib.vxg_factor(eng.handle, 1, call.prec, data.data_ptr(), fac.data_ptr(),
+                                   call.ws.data_ptr(), stream_ptr()), "vxg_factor")
+        facs.append(fac)
+    for other in facs[1:]:
+        assert torch.equal(facs[0], other)
+    bad = (C.c_int32 * nl.value)(*([96] * nl.value))
+    assert eng.lib.vxg_set_factor_shapes(eng.handle, call.prec, bad) == L.VXG_ERR_INVALID
+    autotune.clear()
+    L.check(eng.lib.vxg_set_factor_shapes(eng.handle, call.prec, None), "vxg_set_factor_shapes")
+    s = vx.dc(c, options=vx.Options(precision=precision, engine="generic"))
+    assert bool(s.converged.all())

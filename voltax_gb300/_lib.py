@@ -70,6 +70,9 @@ SIGNATURES = {
     "vxg_factor": ([P, I32, I32, P, P, P, P], I32),
     "vxg_solve": ([P, I32, I32, P, P, P, P, I32, I32, P, P], I32),
     "vxg_spmv": ([P, I32, P, P, P, I32, P], I32),
+    "vxg_level_count": ([P, C.POINTER(I32)], I32),
+    "vxg_tune_factor": ([P, I32, I32, P, P, P, P, P], I32),
+    "vxg_set_factor_shapes": ([P, I32, P], I32),
     "vxg_spsolve_gdata": ([P, I32, P, P, P, P], I32),
     "vxg_newton": ([P, I32, C.POINTER(GroupParams), I32, F64, F64, P, P, F64,
                     C.POINTER(NewtonOpts), P, P, P, P, P, P], I32),

@@ -51,7 +51,9 @@ class Options:
 
     `engine` picks the fused persistent kernel or the generic level kernels;
     with ``"auto"`` and `autotune`, the faster one (and the fused kernel's
-    CTA width) is timed per topology and batch size (`autotune.choose`).
+    CTA width) is timed per topology and batch size (`autotune.choose`), and
+    on the generic engine `autotune` also times each elimination level's
+    factor CTA width (`autotune.tune_factor`).
     `block` pins the fused kernel's threads per instance: 64, 128, 256 or 512
     (one CTA per instance), 32 (one warp per instance, several instances per
     CTA; topologies whose supernodes are at most 32 wide), 0: library
@@ -160,6 +162,8 @@ class _Call:
         if self.fused and options.engine == "auto" and options.autotune and not options.block:
             engine, self.block = autotune.choose(self)
             self.fused = engine == "fused"
+        if not self.fused and options.autotune:
+            autotune.tune_factor(self)
         self.refine = options.refine if options.refine is not None else (0 if self.fused else 1)
 
     def _use_fused(self) -> bool:

@@ -1,4 +1,4 @@
-"""Launch-shape autotuner for the Newton engines.
+"""Launch-shape autotuners for the Newton engines.
 
 Which engine and CTA width run a batched analysis fastest depends on the
 topology and the batch: the fused persistent kernel keeps an instance on
@@ -16,6 +16,12 @@ The choice changes only speed, never the algorithm: every candidate
 computes the same Newton iterates up to rounding (the engines agree to
 1e-11 relative). For bit-for-bit repeatable results across processes, pin
 ``Options(engine=..., block=...)``, which bypasses the tuner.
+
+`tune_factor` picks the generic engine's tile shape: the CTA width (128,
+256 or 512 threads) of each elimination level's factor kernel, timed level
+by level by `vxg_tune_factor` on the Jacobian of the caller's instances,
+once per (topology, precision, batch size class). The width changes no sum's
+order, so the factors are bitwise those of the built-in size rule.
 """
 
 from __future__ import annotations
@@ -37,6 +43,7 @@ TRIAL_INSTANCES = 4096
 BLOCKS = (128, 256, 512)
 
 _cache: dict[tuple, tuple[str, int]] = {}
+_widths: dict[tuple, tuple[int, ...]] = {}
 
 
 def _bucket(batch: int) -> int:
@@ -102,5 +109,40 @@ def choose(call) -> tuple[str, int]:
     return best
 
 
+def tune_factor(call) -> tuple[int, ...]:
+    """Per-level factor CTA widths (0: fixed shape) for this call's topology,
+    precision and batch, set on the call's engine handle."""
+    eng = call.eng
+    key = (call.c.topology_key(), call.prec, _bucket(call.B))
+    applied = eng.__dict__.setdefault("factor_widths_key", {})  # precision -> key held
+    widths = _widths.get(key)
+    if widths is not None:
+        if applied.get(call.prec) != key:
+            arr = (C.c_int32 * len(widths))(*widths)
+            L.check(eng.lib.vxg_set_factor_shapes(eng.handle, call.prec, arr),
+                    "vxg_set_factor_shapes")
+            applied[call.prec] = key
+        return widths
+    n = min(call.B, TRIAL_INSTANCES)
+    dev = eng.device
+    z = torch.zeros((n, eng.S), dtype=torch.float64, device=dev)
+    data = torch.empty((n, eng.nnz), dtype=torch.float64, device=dev)
+    ws = call.ws if n == call.B else eng.workspace(n, call.prec)
+    fac = eng.factor_buffer(n, call.prec)
+    L.check(eng.lib.vxg_eval(eng.handle, n, call.params, z.data_ptr(), 0.0, 1.0, 0.0, None,
+                             call.o.gmin, None, None, data.data_ptr(), ws.data_ptr(),
+                             stream_ptr()), "vxg_eval")
+    nl = C.c_int32()
+    L.check(eng.lib.vxg_level_count(eng.handle, C.byref(nl)), "vxg_level_count")
+    out = (C.c_int32 * max(nl.value, 1))()
+    L.check(eng.lib.vxg_tune_factor(eng.handle, n, call.prec, data.data_ptr(), fac.data_ptr(),
+                                    ws.data_ptr(), out, stream_ptr()), "vxg_tune_factor")
+    widths = tuple(out[i] for i in range(nl.value))
+    _widths[key] = widths
+    applied[call.prec] = key
+    return widths
+
+
 def clear() -> None:
     _cache.clear()
+    _widths.clear()

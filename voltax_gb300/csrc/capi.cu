@@ -163,6 +163,8 @@ static void free_topo(Topo& t) {
   delete[] t.h_lv_bt_ptr;
   delete[] t.h_lv_kmax;
   delete[] t.h_lv_rmax;
+  delete[] t.h_lv_nt[0];
+  delete[] t.h_lv_nt[1];
 }
 
 constexpr long long kLongSum = 32;
@@ -603,6 +605,49 @@ int vxg_solve(const vxg_handle* h, int32_t batch, int32_t precision, const void*
   return launch_solve(h->t, batch, precision, factors, data, b, x, transpose, refine,
                       at<void>(workspace, L.xt), at<void>(workspace, L.scratch),
                       at<double>(workspace, L.r64), (cudaStream_t)stream);
+}
+
+int vxg_level_count(const vxg_handle* h, int32_t* n_levels) {
+  if (!h || !n_levels) return VXG_ERR_INVALID;
+  *n_levels = h->t.n_levels;
+  return VXG_OK;
+}
+
+int vxg_set_factor_shapes(vxg_handle* h, int32_t precision, const int32_t* widths) {
+  if (!h || (precision != VXG_F64 && precision != VXG_F32)) return VXG_ERR_INVALID;
+  Topo& t = h->t;
+  const int nl = t.n_levels;
+  if (widths)
+    for (int L = 0; L < nl; ++L)
+      if (widths[L] != 0 && widths[L] != 128 && widths[L] != 256 && widths[L] != 512)
+        return VXG_ERR_INVALID;
+  int*& tab = t.h_lv_nt[precision == VXG_F32 ? 1 : 0];
+  if (!widths) {
+    delete[] tab;
+    tab = nullptr;
+  } else {
+    if (!tab) tab = new (std::nothrow) int[nl];
+    if (!tab) return VXG_ERR_ALLOC;
+    for (int L = 0; L < nl; ++L) tab[L] = widths[L];
+  }
+  // the cached Newton graphs baked in the previous widths
+  delete_graph_cache(h->graphs);
+  h->graphs = new_graph_cache();
+  return h->graphs ? VXG_OK : VXG_ERR_ALLOC;
+}
+
+int vxg_tune_factor(vxg_handle* h, int32_t batch, int32_t precision, const double* data,
+                    void* factors, void* workspace, int32_t* widths, void* stream) {
+  if (!h || batch <= 0 || !data || !factors || !workspace) return VXG_ERR_INVALID;
+  if (precision != VXG_F64 && precision != VXG_F32) return VXG_ERR_INVALID;
+  const Layout L = layout(h->t, batch, precision);
+  std::vector<int> w((size_t)std::max(h->t.n_levels, 1), 0);
+  const int st = tune_factor(h->t, batch, precision, data, factors, at<void>(workspace, L.scratch),
+                             w.data(), (cudaStream_t)stream);
+  if (st != VXG_OK) return st;
+  if (widths)
+    for (int i = 0; i < h->t.n_levels; ++i) widths[i] = w[(size_t)i];
+  return vxg_set_factor_shapes(h, precision, w.data());
 }
 
 int vxg_spmv(const vxg_handle* h, int32_t batch, const double* data, const double* x,

@@ -279,6 +279,27 @@ static int launch_level(dim3 grid, size_t smem, const Topo& t, long long lo, T* 
 template <typename T>
 static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t s);
 
+// CTA width of level L's factor kernel (levels whose F11 fits in shared
+// memory and whose Schur product stays on the CUDA cores): the width
+// vxg_tune_factor measured fastest, else the size rule.
+template <typename T>
+static int level_width(const Topo& t, int L) {
+  if constexpr (!std::is_same<T, cplx>::value) {
+    const int* tw = t.h_lv_nt[std::is_same<T, float>::value ? 1 : 0];
+    if (tw && tw[L]) return tw[L];
+  }
+  const int kmax = t.h_lv_kmax[L];
+  return kmax > 80 ? 512 : kmax > 48 ? 256 : 128;
+}
+
+template <typename T>
+static int launch_width(int nt, dim3 grid, size_t smem, const Topo& t, long long lo, T* work,
+                        long long ws, T* scratch, long long ss, cudaStream_t s) {
+  if (nt == 512) return launch_level<T, 512, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
+  if (nt == 256) return launch_level<T, 256, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
+  return launch_level<T, 128, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
+}
+
 template <typename T>
 static int factor_impl(const Topo& t, int B, const double* data, T* work, T* scratch,
                        cudaStream_t s) {
@@ -305,51 +326,66 @@ __global__ void fill_panels_ac_kernel(int B, long long nnz, const long long* __r
   work[(long long)b * work_stride + a_pos[e]] = cplx(G[e], omega[b] * C[e]);
 }
 
+static int max_optin_smem() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return -1;
+  return v;
+}
+
+// Level L's factor kernel, one launch: the tensor-core Schur products (FP32,
+// k and r at least 64), the wide kernel (F11 left in its panel) when F11
+// does not fit in shared memory, else the tuned or size-rule CTA width.
 template <typename T>
-static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t s) {
+static int factor_level_once(const Topo& t, int L, int B, T* work, T* scratch, int max_optin,
+                             cudaStream_t s) {
   const long long ws = t.work, ss = t.max_schur;
-  int dev = 0, max_optin = 0;
-  VXG_CUDA_TRY(cudaGetDevice(&dev));
-  VXG_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  for (int L = 0; L < t.n_levels; ++L) {
-    const long long lo = t.h_lv_ptr[L], hi = t.h_lv_ptr[L + 1];
-    if (hi == lo) continue;
-    const int kmax = t.h_lv_kmax[L];
-    dim3 grid((unsigned)(hi - lo), (unsigned)B);
-    size_t smem = factor_smem_bytes(kmax, sizeof(T));
-    int st = VXG_OK;
-    bool launched = false;
-    if constexpr (std::is_same<T, float>::value) {
-      if (kmax >= kTcMinK && t.h_lv_rmax[L] >= kTcMinR) {  // Schur products on the tensor cores
-        const bool wide = factor_smem_bytes(kmax, 4, false, true) > (size_t)max_optin;
-        smem = factor_smem_bytes(kmax, 4, wide, true);
-        if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
-        st = wide ? launch_level<T, 512, true, true>(grid, smem, t, lo, work, ws, scratch, ss, s)
+  const long long lo = t.h_lv_ptr[L], hi = t.h_lv_ptr[L + 1];
+  const int kmax = t.h_lv_kmax[L];
+  const dim3 grid((unsigned)(hi - lo), (unsigned)B);
+  size_t smem = factor_smem_bytes(kmax, sizeof(T));
+  if constexpr (std::is_same<T, float>::value) {
+    if (kmax >= kTcMinK && t.h_lv_rmax[L] >= kTcMinR) {  // Schur products on the tensor cores
+      const bool wide = factor_smem_bytes(kmax, 4, false, true) > (size_t)max_optin;
+      smem = factor_smem_bytes(kmax, 4, wide, true);
+      if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+      return wide ? launch_level<T, 512, true, true>(grid, smem, t, lo, work, ws, scratch, ss, s)
                   : launch_level<T, 512, false, true>(grid, smem, t, lo, work, ws, scratch, ss,
                                                       s);
-        launched = true;
-      }
     }
-    if (launched) {
-    } else if (smem > (size_t)max_optin) {  // F11 stays in the panel
-      smem = factor_smem_bytes(kmax, sizeof(T), true);
-      if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
-      st = launch_level<T, 512, true>(grid, smem, t, lo, work, ws, scratch, ss, s);
-    } else if (kmax > 80) {
-      st = launch_level<T, 512, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
-    } else if (kmax > 48) {
-      st = launch_level<T, 256, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
-    } else {
-      st = launch_level<T, 128, false>(grid, smem, t, lo, work, ws, scratch, ss, s);
-    }
+  }
+  if (smem > (size_t)max_optin) {  // F11 stays in the panel
+    smem = factor_smem_bytes(kmax, sizeof(T), true);
+    if (smem > (size_t)max_optin) return VXG_ERR_TOO_LARGE;
+    return launch_level<T, 512, true>(grid, smem, t, lo, work, ws, scratch, ss, s);
+  }
+  return launch_width<T>(level_width<T>(t, L), grid, smem, t, lo, work, ws, scratch, ss, s);
+}
+
+// work[t] -= sum of level L's Schur block entries aimed at t.
+template <typename T>
+static int apply_level_schur(const Topo& t, int L, int B, T* work, T* scratch, cudaStream_t s) {
+  const long long tlo = t.h_lv_st_ptr[L], thi = t.h_lv_st_ptr[L + 1];
+  const long long nt = (long long)B * (thi - tlo);
+  if (nt) {
+    schur_apply_kernel<T><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(
+        B, thi - tlo, t.st_tgt + tlo, t.st_ptr + tlo, t.st_src, scratch, t.max_schur, work,
+        t.work);
+    VXG_LAUNCHED();
+  }
+  return VXG_OK;
+}
+
+template <typename T>
+static int factor_levels(const Topo& t, int B, T* work, T* scratch, cudaStream_t s) {
+  const int max_optin = max_optin_smem();
+  if (max_optin < 0) return VXG_ERR_CUDA;
+  for (int L = 0; L < t.n_levels; ++L) {
+    if (t.h_lv_ptr[L + 1] == t.h_lv_ptr[L]) continue;
+    int st = factor_level_once<T>(t, L, B, work, scratch, max_optin, s);
+    if (st == VXG_OK) st = apply_level_schur<T>(t, L, B, work, scratch, s);
     if (st != VXG_OK) return st;
-    const long long tlo = t.h_lv_st_ptr[L], thi = t.h_lv_st_ptr[L + 1];
-    const long long nt = (long long)B * (thi - tlo);
-    if (nt) {
-      schur_apply_kernel<T><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(
-          B, thi - tlo, t.st_tgt + tlo, t.st_ptr + tlo, t.st_src, scratch, ss, work, ws);
-      VXG_LAUNCHED();
-    }
   }
   return VXG_OK;
 }
@@ -364,6 +400,76 @@ int launch_factor_ac(const Topo& t, int B, const double* G, const double* C,
                                                                       omega, work, t.work);
   VXG_LAUNCHED();
   return factor_levels<cplx>(t, B, work, (cplx*)scratch, s);
+}
+
+// Each tunable level's kernel timed at 128, 256 and 512 threads (the best of
+// three launches each, CUDA events on the stream) on the panels of `data`,
+// then its Schur block applied, level by level as a factorization runs.
+// The repeated in-place launches leave the panels meaningless, which changes
+// no launch's work: the kernels' control flow and addresses depend on the
+// plan alone. widths[L] = the fastest width, or 0 for a level with a fixed
+// shape (wide, or tensor-core Schur products).
+template <typename T>
+static int tune_levels(const Topo& t, int B, const double* data, T* work, T* scratch,
+                       int* widths, cudaStream_t s) {
+  const long long ws = t.work, ss = t.max_schur;
+  VXG_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(T) * (size_t)B * ws, s));
+  const long long n = (long long)B * t.nnz;
+  if (n)
+    fill_panels_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, t.nnz, t.a_pos, data,
+                                                                        work, ws);
+  VXG_LAUNCHED();
+  const int max_optin = max_optin_smem();
+  if (max_optin < 0) return VXG_ERR_CUDA;
+  cudaEvent_t e[2] = {nullptr, nullptr};
+  int st = VXG_OK;
+  for (int q = 0; q < 2 && st == VXG_OK; ++q)
+    if (cudaEventCreate(&e[q]) != cudaSuccess) st = VXG_ERR_CUDA;
+  for (int L = 0; L < t.n_levels && st == VXG_OK; ++L) {
+    widths[L] = 0;
+    const long long lo = t.h_lv_ptr[L], hi = t.h_lv_ptr[L + 1];
+    if (hi == lo) continue;
+    const int kmax = t.h_lv_kmax[L];
+    const dim3 grid((unsigned)(hi - lo), (unsigned)B);
+    const size_t smem = factor_smem_bytes(kmax, sizeof(T));
+    const bool tc = std::is_same<T, float>::value && kmax >= kTcMinK && t.h_lv_rmax[L] >= kTcMinR;
+    if (tc || smem > (size_t)max_optin) {
+      st = factor_level_once<T>(t, L, B, work, scratch, max_optin, s);
+    } else {
+      float best = 0.f;
+      for (int nt : {128, 256, 512}) {
+        float tmin = 0.f;
+        for (int rep = 0; rep < 3 && st == VXG_OK; ++rep) {
+          float ms = 0.f;
+          if (cudaEventRecord(e[0], s) != cudaSuccess) st = VXG_ERR_CUDA;
+          if (st == VXG_OK) st = launch_width<T>(nt, grid, smem, t, lo, work, ws, scratch, ss, s);
+          if (st == VXG_OK && (cudaEventRecord(e[1], s) != cudaSuccess ||
+                               cudaEventSynchronize(e[1]) != cudaSuccess ||
+                               cudaEventElapsedTime(&ms, e[0], e[1]) != cudaSuccess))
+            st = VXG_ERR_CUDA;
+          if (rep == 0 || ms < tmin) tmin = ms;
+        }
+        if (st == VXG_OK && (widths[L] == 0 || tmin < best)) {
+          best = tmin;
+          widths[L] = nt;
+        }
+      }
+    }
+    if (st == VXG_OK) st = apply_level_schur<T>(t, L, B, work, scratch, s);
+  }
+  for (cudaEvent_t x : e)
+    if (x) cudaEventDestroy(x);
+  if (st == VXG_OK) VXG_CUDA_TRY(cudaStreamSynchronize(s));
+  return st;
+}
+
+int tune_factor(const Topo& t, int B, int precision, const double* data, void* factors,
+                void* scratch, int* widths, cudaStream_t s) {
+  if (precision == VXG_F64)
+    return tune_levels<double>(t, B, data, (double*)factors, (double*)scratch, widths, s);
+  if (precision == VXG_F32)
+    return tune_levels<float>(t, B, data, (float*)factors, (float*)scratch, widths, s);
+  return VXG_ERR_INVALID;
 }
 
 int launch_factor(const Topo& t, int B, int precision, const double* data, void* factors,

@@ -77,6 +77,9 @@ struct Topo {
   int* bt_tgt;
   long long *bt_ptr, *bt_src;
   long long max_schur, max_bord;  // largest per-level scratch
+  // CTA width of each level's factor kernel picked by vxg_tune_factor
+  // (F64, F32; 0 or a null table: the size rule)
+  int* h_lv_nt[2];
   int kmax, rmax;
   int max_m;  // largest local block (terminals + internals) over the groups
   // 16-bit tables of the fused kernel (null when some index does not fit)
@@ -101,6 +104,10 @@ void count_launches(unsigned long long n);
 char* last_error_buffer();
 GraphCache* new_graph_cache();
 void delete_graph_cache(GraphCache* c);  // this thread's vxg_last_error text (256 bytes)
+// Per-level CTA widths of the factor kernels that beat the size rule, timed
+// on `data` (writes `factors` and `scratch`; synchronizes `s`).
+int tune_factor(const Topo& t, int B, int precision, const double* data, void* factors,
+                void* scratch, int* widths, cudaStream_t s);
 }
 
 // Count one kernel launch and surface launch errors.
