@@ -324,6 +324,23 @@ int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* pa
                   int32_t direct_steps, double gmin, const vxg_newton_opts* opts,
                   double* z_out, int32_t* converged, int32_t* iters, void* stream);
 
+/* DC sweep with continuation in ONE persistent launch (dc_sweep,
+ * voltax/analysis.py:530-568): for point k = 0 .. n_points-1, parameter row
+ * `row` of device `device` of group `group` takes values[k] (device array)
+ * in every instance, and the DC operating point at time t is solved as in
+ * vxg_fused_run's dc_first (direct attempt, then the gmin stages) starting
+ * from point k-1's solution (point 0: from z0). The kernel writes the value
+ * into each instance's own copy of the parameter, so that group's rows must
+ * be per instance (batch_stride > 0) in writable device memory; they hold
+ * the last value afterwards. z_out: n_points x B x S; converged, iters:
+ * n_points x B. */
+int vxg_fused_sweep(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                    int32_t group, int32_t row, int32_t device, int32_t n_points,
+                    const double* values, double t, const double* z0, const double* gmins,
+                    int32_t gmin_steps, int32_t direct_steps, double gmin,
+                    const vxg_newton_opts* opts, double* z_out, int32_t* converged,
+                    int32_t* iters, void* stream);
+
 /* Phase timing of the fused kernel (a diagnostic; no counterpart in the
  * reference). With `cycles` != NULL (device, 8 int64, zeroed by the
  * caller), every later vxg_fused_run of the calling thread adds, summed

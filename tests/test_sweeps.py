@@ -139,3 +139,31 @@ def test_dc_sweep_schmitt_trigger_hysteresis():
     rise_thr = _crossing(vin, out_up, 0.0)
     fall_thr = -_crossing(-vin[::-1], out_dn, 0.0)
     assert 0.4 < rise_thr < 0.55 and -0.55 < fall_thr < -0.4
+
+
+@pytest.mark.gpu
+def test_dc_sweep_in_one_launch_matches_point_by_point():
+    """A swept DC source on the fused engine runs the whole continuation in
+    one persistent launch (vxg_fused_sweep); it gives the iterates of the
+    point-by-point sweep bit for bit and leaves the circuit untouched."""
+    from voltax_gb300 import _lib
+    lib = _lib.load()
+    c = _latch()
+    o = vx.Options(engine="fused")
+    vin = np.linspace(0.0, 1.2, 25)
+    vx.dc(c, options=o)  # settle the launch-shape choice
+    n0 = lib.vxg_launch_count()
+    fast = vx.dc_sweep(c, vin, "Vin", options=o)
+    launches = lib.vxg_launch_count() - n0
+    slow = vx.dc_sweep(c, vin, lambda cc, v: cc.set("Vin", value=v), options=o)
+    assert launches == 1
+    assert bool(fast.converged.all()) and torch.equal(fast.converged, slow.converged)
+    assert torch.equal(fast.iterations, slow.iterations)
+    assert torch.equal(fast.z, slow.z)
+    el, idx = c.device("Vin")
+    assert float(el.value.value.reshape(-1)[idx]) == 0.0
+    # down again from the top, continuing the upper branch
+    down_fast = vx.dc_sweep(c, vin[::-1], "Vin", guess=fast.z[-1], options=o)
+    down_slow = vx.dc_sweep(c, vin[::-1], lambda cc, v: cc.set("Vin", value=v),
+                            guess=slow.z[-1], options=o)
+    assert torch.equal(down_fast.z, down_slow.z)

@@ -83,6 +83,8 @@ SIGNATURES = {
     "vxg_fused_smem": ([P, I32, C.POINTER(C.c_size_t)], I32),
     "vxg_fused_run": ([P, I32, C.POINTER(GroupParams), I32, I32, P, P, I32, P, I32, I32, F64,
                        C.POINTER(NewtonOpts), P, P, P, P], I32),
+    "vxg_fused_sweep": ([P, I32, C.POINTER(GroupParams), I32, I32, I32, I32, P, F64, P, P, I32,
+                         I32, F64, C.POINTER(NewtonOpts), P, P, P, P], I32),
     "vxg_factor_static": ([P, I32, I32, P, P, P], I32),
     "vxg_gemm_tf32x3": ([I32, I32, I32, P, I32, P, I32, P, I32, P, P], I32),
     "vxg_fused_set_profile": ([P], I32),

@@ -507,9 +507,14 @@ def dc_sweep(circuit, values, apply, t: float = 0.0, guess=None,
 
     `apply` is a source name (its DC value is set) or ``fn(circuit, value)``.
     Returns a `Solution` whose ``t`` holds the sweep values and whose ``z``
-    has the sweep axis first. Each point is one Newton launch on the GPU,
-    warm-started from the previous state left on the device."""
+    has the sweep axis first. A DC source swept on the fused engine runs the
+    whole sweep in one persistent launch (`vxg_fused_sweep`); otherwise each
+    point is one Newton launch, warm-started from the previous state left on
+    the device."""
     if isinstance(apply, str):
+        swept = _device_sweep(circuit, values, apply, t, guess, options)
+        if swept is not None:
+            return swept
         device = apply
         apply = lambda c, v: c.set(device, value=v)  # noqa: E731
     vals = torch.as_tensor(np.array(values, dtype=np.float64))  # a copy: any strides
@@ -523,6 +528,62 @@ def dc_sweep(circuit, values, apply, t: float = 0.0, guess=None,
         its.append(sol.iterations)
     return Solution(vals, torch.stack(zs), torch.stack(oks), circuit.layout,
                     torch.stack(its))
+
+
+def _device_sweep(circuit, values, name: str, t, guess, options: Options):
+    """`dc_sweep` of the DC value of source `name` in one launch: the fused
+    kernel writes each point's value into a private per-instance copy of the
+    source group's parameter rows and solves from the previous point. None
+    when that path does not apply (not a constant-valued source, the generic
+    engine, or a parameter that needs a gradient): the caller then sweeps
+    point by point."""
+    from .elements import _Source
+    from .signals import Constant
+    try:
+        gname, idx = circuit.layout.device(name)
+    except KeyError:
+        return None
+    el = circuit.elements[gname]
+    if not isinstance(el, _Source) or not isinstance(el.value, Constant):
+        return None
+    vals = np.array(values, dtype=np.float64).reshape(-1)
+    if vals.size == 0:
+        return None
+    call = _Call(circuit, options)
+    if not call.fused or any(r.requires_grad for r in _flat_rows(call)):
+        return None
+    eng, o = call.eng, call.o
+    S, B = eng.S, call.B
+    dev = eng.device
+    gi = eng.tables.group_names.index(gname)
+    packed = call.keep[gi]  # (rows, 1 or B, n)
+    rows_n, _, n = packed.shape
+    own = packed.expand(rows_n, B, n).clone()  # written by the kernel
+    call.keep.append(own)
+    call.params[gi] = L.GroupParams(own.data_ptr(), B * n, n)
+    if guess is None:
+        z0 = torch.zeros((B, S), dtype=torch.float64, device=dev)
+    else:
+        z0 = torch.as_tensor(guess, dtype=torch.float64, device=dev)
+        z0 = z0.reshape(-1, S).expand(B, S).contiguous()
+    K = vals.size
+    vals_d = torch.as_tensor(vals, device=dev)
+    gmins = np.concatenate([[o.gmin], np.logspace(np.log10(o.gmin_start), np.log10(o.gmin),
+                                                  o.gmin_steps)])
+    gm_d = torch.as_tensor(gmins, dtype=torch.float64, device=dev)
+    z_out = torch.empty((K, B, S), dtype=torch.float64, device=dev)
+    conv = torch.empty((K, B), dtype=torch.int32, device=dev)
+    iters = torch.empty((K, B), dtype=torch.int32, device=dev)
+    nat = o.native(refine=call.refine)
+    nat.block = call.block
+    L.check(eng.lib.vxg_fused_sweep(
+        eng.handle, B, call.params, gi, 0, idx, K, vals_d.data_ptr(), float(t), z0.data_ptr(),
+        gm_d.data_ptr(), o.gmin_steps, o.direct_steps, o.gmin, C.byref(nat), z_out.data_ptr(),
+        conv.data_ptr(), iters.data_ptr(), stream_ptr()), "vxg_fused_sweep")
+    conv = conv.bool()
+    if circuit.batch == 1:
+        z_out, conv, iters = z_out[:, 0], conv[:, 0], iters[:, 0]
+    return Solution(torch.as_tensor(vals), z_out, conv, circuit.layout, iters)
 
 
 def time_grid(circuit, t_stop: float, dt_max: float, dt_min: float | None = None,

@@ -92,23 +92,15 @@ extern "C" int vxg_fused_smem(const vxg_handle* h, int32_t precision, size_t* by
   return fused_eligible(h->t, precision, bytes);
 }
 
-extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
-                             int32_t mode, int32_t n_t, const double* ts, const double* z0,
-                             int32_t dc_first, const double* gmins, int32_t gmin_steps,
-                             int32_t direct_steps, double gmin, const vxg_newton_opts* o,
-                             double* z_out, int32_t* converged, int32_t* iters, void* stream) {
-  if (!h || batch <= 0 || !params || n_t <= 0 || !ts || !z0 || !z_out || !converged ||
-      !iters || !o || mode < 0 || mode > 2 || (n_t > 1 && mode == VXG_MODE_DC) ||
-      (dc_first && gmin_steps > 0 && !gmins) || o->max_steps < 0 || o->refine < 0 ||
-      (o->precision != VXG_F64 && o->precision != VXG_F32))
-    return VXG_ERR_INVALID;
-  const Topo& t = h->t;
+// The persistent launch of vxg_fused_run and vxg_fused_sweep: tables,
+// options and the CTA width (the caller's, an autotuned choice, else wider
+// CTAs when few instances or few resident CTAs per SM leave warps idle).
+static int launch_args(const Topo& t, int batch, const vxg_group_params* params,
+                       const vxg_newton_opts* o, FusedArgs& a, cudaStream_t s) {
   size_t smem = 0;
   int first_global = B_COUNT, staged = 0;
   int st = fused_eligible(t, o->precision, &smem, &first_global, &staged);
   if (st) return st;
-  FusedArgs a;
-  std::memset(&a, 0, sizeof(a));
   a.first_global = first_global;
   a.staged = staged;
   a.gt = make_table(t, params);
@@ -151,30 +143,15 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
   a.blob = t.d_blob;
   a.bo = t.blob;
   a.B = batch;
-  a.mode = mode;
-  a.n_t = n_t;
   a.max_steps = o->max_steps;
   a.refine = o->refine;
-  a.dc_first = dc_first;
-  a.gmin_steps = gmin_steps;
-  a.direct_steps = direct_steps;
   a.rtol = o->rtol;
   a.atol = o->atol;
   a.max_dv = o->max_dv;
-  a.gmin = gmin;
-  a.ts = ts;
-  a.gmins = gmins;
-  a.z0 = z0;
-  a.z_out = z_out;
-  a.conv = converged;
-  a.iters = iters;
   a.phase_clk = t_phase_clk;
-  cudaStream_t s = (cudaStream_t)stream;
   int dev = 0, sms = 0;
   VXG_CUDA_TRY(cudaGetDevice(&dev));
   VXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  // CTA width: the caller's (an autotuned choice), else wider CTAs when few
-  // instances or few resident CTAs per SM leave warps idle
   int nt = o->block;
   if (nt == 0) {
     int smem_sm = 0;
@@ -192,4 +169,71 @@ extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group
     case 512: return f32 ? launch_fused<float, 512>(a, s) : launch_fused<double, 512>(a, s);
     default: return VXG_ERR_INVALID;
   }
+}
+
+static bool opts_ok(const vxg_newton_opts* o) {
+  return o && o->max_steps >= 0 && o->refine >= 0 &&
+         (o->precision == VXG_F64 || o->precision == VXG_F32);
+}
+
+extern "C" int vxg_fused_run(const vxg_handle* h, int32_t batch, const vxg_group_params* params,
+                             int32_t mode, int32_t n_t, const double* ts, const double* z0,
+                             int32_t dc_first, const double* gmins, int32_t gmin_steps,
+                             int32_t direct_steps, double gmin, const vxg_newton_opts* o,
+                             double* z_out, int32_t* converged, int32_t* iters, void* stream) {
+  if (!h || batch <= 0 || !params || n_t <= 0 || !ts || !z0 || !z_out || !converged ||
+      !iters || !opts_ok(o) || mode < 0 || mode > 2 || (n_t > 1 && mode == VXG_MODE_DC) ||
+      (dc_first && gmin_steps > 0 && !gmins))
+    return VXG_ERR_INVALID;
+  FusedArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = mode;
+  a.n_t = n_t;
+  a.dc_first = dc_first;
+  a.gmin_steps = gmin_steps;
+  a.direct_steps = direct_steps;
+  a.gmin = gmin;
+  a.ts = ts;
+  a.gmins = gmins;
+  a.z0 = z0;
+  a.z_out = z_out;
+  a.conv = converged;
+  a.iters = iters;
+  return launch_args(h->t, batch, params, o, a, (cudaStream_t)stream);
+}
+
+extern "C" int vxg_fused_sweep(const vxg_handle* h, int32_t batch,
+                               const vxg_group_params* params, int32_t group, int32_t row,
+                               int32_t device, int32_t n_points, const double* values, double t,
+                               const double* z0, const double* gmins, int32_t gmin_steps,
+                               int32_t direct_steps, double gmin, const vxg_newton_opts* o,
+                               double* z_out, int32_t* converged, int32_t* iters,
+                               void* stream) {
+  if (!h || batch <= 0 || !params || n_points <= 0 || !values || !z0 || !z_out ||
+      !converged || !iters || !opts_ok(o) || (gmin_steps > 0 && !gmins))
+    return VXG_ERR_INVALID;
+  const Topo& tp = h->t;
+  if (group < 0 || group >= tp.n_groups || row < 0 || row >= tp.groups[group].n_params ||
+      device < 0 || device >= tp.groups[group].n || !params[group].params ||
+      params[group].batch_stride <= 0)
+    return VXG_ERR_INVALID;
+  FusedArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = VXG_MODE_DC;
+  a.n_t = n_points;
+  a.dc_first = 1;
+  a.gmin_steps = gmin_steps;
+  a.direct_steps = direct_steps;
+  a.gmin = gmin;
+  a.gmins = gmins;
+  a.z0 = z0;
+  a.z_out = z_out;
+  a.conv = converged;
+  a.iters = iters;
+  a.sweep_vals = values;
+  a.sweep_slot = const_cast<double*>(params[group].params) + row * params[group].row_stride +
+                 device;
+  a.sweep_stride = params[group].batch_stride;
+  a.sweep_t = t;
+  return launch_args(tp, batch, params, o, a, (cudaStream_t)stream);
 }

@@ -60,6 +60,14 @@ struct FusedArgs {
   double* z_out;
   int* conv;
   int* iters;
+  // DC sweep (vxg_fused_sweep; sweep_vals null otherwise): before point n,
+  // instance b writes sweep_vals[n] to sweep_slot[b * sweep_stride], its
+  // own copy of the swept parameter, then solves DC at sweep_t from point
+  // n-1's solution
+  const double* sweep_vals;
+  double* sweep_slot;
+  long long sweep_stride;
+  double sweep_t;
   // phase timing (a diagnostic, normally null): SM clock cycles of each CTA
   // per phase, summed over CTAs -- eval, assemble, factor, solve, update,
   // and the whole kernel -- see vxg_fused_set_profile
@@ -1057,6 +1065,25 @@ struct Instance {
     return ok && scale == 1.0;
   }
 
+  // DC at time t from the current state (voltax/analysis.py:236-266): the
+  // direct attempt, then on failure the gmin stages restarted from `restart`.
+  __device__ __forceinline__ int dc_solve(double t, const double* restart, int* iters_out) {
+    const int direct = A.gmin_steps > 0 ? A.direct_steps : A.max_steps;
+    int it = 0;
+    int ok = newton(VXG_MODE_DC, t, 0.0, A.gmin, direct, &it);
+    if (!ok && A.gmin_steps > 0) {
+      for (int i = tid(); i < A.S; i += GT) z[i] = restart[i];
+      sync();
+      for (int s = 1; s <= A.gmin_steps; ++s) {
+        int its = 0;
+        ok = newton(VXG_MODE_DC, t, 0.0, A.gmins[s], A.max_steps, &its);
+        it += its;
+      }
+    }
+    *iters_out = it;
+    return ok;
+  }
+
   __device__ int newton(int mode, double t, double t_prev, double gmin, int max_steps,
                         int* iters_out) {
     const bool dc = mode == VXG_MODE_DC;
@@ -1143,48 +1170,45 @@ __device__ __forceinline__ void bind(Instance<T, NT, kWarp>& I, unsigned char* b
 // the DC operating point (direct attempt, then gmin stepping restarting from
 // z0), then one Newton solve per time point.
 template <typename T, int NT, bool kWarp>
-__device__ void run_instances(const FusedArgs& A, Instance<T, NT, kWarp>& I, int first,
-                              int stride) {
+__device__ __forceinline__ void run_instances(const FusedArgs& A, Instance<T, NT, kWarp>& I,
+                                              int first, int stride) {
   using G = Instance<T, NT, kWarp>;
   const long long BS = (long long)A.B * A.S;
   for (int b = first; b < A.B; b += stride) {
     I.b = b;
     for (int i = G::tid(); i < A.S; i += G::GT) I.z[i] = A.z0[(long long)b * A.S + i];
     G::sync();
-    int ok = 1, it = 0;
-    if (A.dc_first) {
-      const int direct = A.gmin_steps > 0 ? A.direct_steps : A.max_steps;
-      ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmin, direct, &it);
-      if (!ok && A.gmin_steps > 0) {
-        for (int i = G::tid(); i < A.S; i += G::GT) I.z[i] = A.z0[(long long)b * A.S + i];
-        G::sync();
-        for (int s = 1; s <= A.gmin_steps; ++s) {
-          int its = 0;
-          ok = I.newton(VXG_MODE_DC, A.ts[0], 0.0, A.gmins[s], A.max_steps, &its);
-          it += its;
+    // Point n is a DC solve (every point of a sweep; point 0 of a transient
+    // when dc_first) or a time step; one call site each, so that the Newton
+    // body is inlined at three places only.
+    const bool sweep = A.sweep_vals != nullptr;
+    for (int n = 0; n < A.n_t; ++n) {
+      int ok = 1, it = 0;
+      if (sweep || n == 0) {
+        if (sweep) {
+          if (G::tid() == 0) A.sweep_slot[(long long)b * A.sweep_stride] = A.sweep_vals[n];
+          G::sync();  // the group's evaluations read the value after this barrier
         }
+        if (sweep || A.dc_first)
+          ok = I.dc_solve(sweep ? A.sweep_t : A.ts[0],
+                          n == 0 ? A.z0 + (long long)b * A.S
+                                 : A.z_out + (long long)(n - 1) * BS + (long long)b * A.S,
+                          &it);
+      } else {
+        const double tp = A.ts[n - 1], t = A.ts[n];
+        if (A.mode == VXG_MODE_TRAP) {  // f(z_prev, t_prev); q(z_prev) comes from iteration 0
+          I.eval(I.z, tp, 1.0, 0.0, true, false, false);
+          G::sync();
+          I.assemble_res(I.fp, nullptr);
+          G::sync();
+        }
+        ok = I.newton(A.mode, t, tp, A.gmin, A.max_steps, &it);
       }
-    }
-    for (int i = G::tid(); i < A.S; i += G::GT) A.z_out[(long long)b * A.S + i] = I.z[i];
-    if (G::tid() == 0) {
-      A.conv[b] = ok;
-      A.iters[b] = it;
-    }
-    for (int n = 1; n < A.n_t; ++n) {
-      const double tp = A.ts[n - 1], t = A.ts[n];
-      if (A.mode == VXG_MODE_TRAP) {  // f(z_prev, t_prev); q(z_prev) comes from iteration 0
-        I.eval(I.z, tp, 1.0, 0.0, true, false, false);
-        G::sync();
-        I.assemble_res(I.fp, nullptr);
-        G::sync();
-      }
-      int its = 0;
-      const int okn = I.newton(A.mode, t, tp, A.gmin, A.max_steps, &its);
       for (int i = G::tid(); i < A.S; i += G::GT)
         A.z_out[(long long)n * BS + (long long)b * A.S + i] = I.z[i];
       if (G::tid() == 0) {
-        A.conv[(long long)n * A.B + b] = okn;
-        A.iters[(long long)n * A.B + b] = its;
+        A.conv[(long long)n * A.B + b] = ok;
+        A.iters[(long long)n * A.B + b] = it;
       }
     }
     G::sync();
