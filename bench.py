@@ -520,12 +520,20 @@ class GPU:
             e1.record()
             self.barrier()
             ms.append(e0.elapsed_time(e1))
-        t = float(np.sum(ms)) / 1e3
-        if self.dist is not None:
-            tt = torch.tensor([t], device=self.dev)
-            self.dist.all_reduce(tt, op=self.dist.ReduceOp.MAX)
-            t = float(tt)
-        return t
+        return max_over_ranks(self.dist, float(np.sum(ms)) / 1e3, self.dev)
+
+
+def max_over_ranks(dist, seconds: float, device) -> float:
+    """The job's time: the largest of the ranks' `seconds` (an all-reduce
+    MAX over the process group; the value itself with no group). Replicas
+    process fixed work each, so the aggregate rate is ranks x per-rank work
+    over this time."""
+    if dist is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
 
 
 # FP64 work of the fused kernel's chosen form per Newton iteration of one
