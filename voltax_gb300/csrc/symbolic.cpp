@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -98,6 +99,53 @@ Vec pivot_groups(i64 S, i64 n, const i64* ua, const i64* ub, i64* G_out) {
   return gid;
 }
 
+// Runs fn(i, state) for i in [0, n) on up to VXS_THREADS threads (default:
+// the hardware's, at most 8), each thread with its own default-constructed
+// State; the first error is rethrown here.
+template <typename State, typename Fn>
+void parallel_for(i64 n, Fn&& fn) {
+  i64 want = (i64)std::thread::hardware_concurrency();
+  if (want <= 0) want = 1;
+  want = std::min<i64>(want, 8);
+  if (const char* env = std::getenv("VXS_THREADS")) {
+    const long v = std::strtol(env, nullptr, 10);
+    if (v > 0) want = v;
+  }
+  const i64 nthreads = std::max<i64>(1, std::min(want, n));
+  std::atomic<i64> next{0};
+  std::atomic<bool> failed{false};
+  std::mutex mu;
+  int code = VXS_OK;
+  std::string msg;
+  auto worker = [&] {
+    State st;
+    for (;;) {
+      const i64 i = next.fetch_add(1);
+      if (i >= n || failed.load()) return;
+      try {
+        fn(i, st);
+      } catch (const Error& e) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!failed.exchange(true)) code = e.code, msg = e.msg;
+      } catch (const std::bad_alloc&) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!failed.exchange(true)) code = VXS_ERR_NOMEM, msg = "out of host memory";
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (i64 t = 1; t < nthreads; ++t) {
+    try {
+      pool.emplace_back(worker);
+    } catch (const std::system_error&) {
+      break;  // fewer threads: the calling thread takes the remaining items
+    }
+  }
+  worker();
+  for (std::thread& t : pool) t.join();
+  if (failed.load()) fail(code, msg);
+}
+
 // ---------------------------------------------------------------------------
 // Nested dissection of the group graph (voltax/sparse.py:308-378).
 // ---------------------------------------------------------------------------
@@ -105,12 +153,12 @@ struct Dissection {
   const Csr& adj;
   const Vec& w;
   i64 leaf;
-  Vec loc;     // global vertex -> index in the current set, or -1
+  Vec& loc;    // global vertex -> index in the current set, or -1 (shared by workers
+               // on disjoint vertex sets)
   Vec dist, lab, queue;
   std::vector<std::pair<Vec, i64>> nodes;  // (vertex set, parent) in creation order
 
-  Dissection(const Csr& a, const Vec& wt, i64 lf)
-      : adj(a), w(wt), leaf(lf), loc(a.rows(), -1) {}
+  Dissection(const Csr& a, const Vec& wt, i64 lf, Vec& lc) : adj(a), w(wt), leaf(lf), loc(lc) {}
 
   // BFS distances inside the current set from local vertex `start`.
   void bfs(const Vec& verts, i64 start) {
@@ -161,17 +209,12 @@ struct Dissection {
     return ncomp;
   }
 
-  void run(const std::vector<char>& last) {
-    i64 G = adj.rows();
-    i64 top = -1;
-    Vec lastv, rest;
-    for (i64 g = 0; g < G; ++g) (last[g] ? lastv : rest).push_back(g);
-    if (!lastv.empty()) {
-      nodes.emplace_back(std::move(lastv), -1);
-      top = 0;
-    }
+  // Dissects `first` (parent `par`) and every set it splits into, depth
+  // first from one stack, appending (set, parent) to `nodes`; parents of
+  // the sets created here are indices into `nodes`.
+  void dissect(Vec first, i64 par0) {
     std::vector<std::pair<Vec, i64>> stack;
-    stack.emplace_back(std::move(rest), top);
+    stack.emplace_back(std::move(first), par0);
     while (!stack.empty()) {
       Vec verts = std::move(stack.back().first);
       i64 par = stack.back().second;
@@ -252,6 +295,47 @@ struct Dissection {
       nodes.emplace_back(std::move(sep), par);
       stack.emplace_back(std::move(low), me);
       stack.emplace_back(std::move(high), me);
+    }
+  }
+
+  // The high-degree groups (`last`) form the root set; the rest is
+  // dissected. Its connected components (the segments of a batch of
+  // independent circuits) are independent subtrees: they are dissected on
+  // the thread pool and appended in the order one stack visits them (the
+  // last component first), so the result is that of the sequential run.
+  void run(const std::vector<char>& last) {
+    i64 G = adj.rows();
+    i64 top = -1;
+    Vec lastv, rest;
+    for (i64 g = 0; g < G; ++g) (last[g] ? lastv : rest).push_back(g);
+    if (!lastv.empty()) {
+      nodes.emplace_back(std::move(lastv), -1);
+      top = 0;
+    }
+    const i64 n = (i64)rest.size();
+    if (n == 0) return;
+    for (i64 i = 0; i < n; ++i) loc[rest[i]] = i;
+    const i64 ncomp = components(rest);
+    if (ncomp <= 1) {
+      for (i64 v : rest) loc[v] = -1;
+      dissect(std::move(rest), top);
+      return;
+    }
+    std::vector<Vec> parts(ncomp);
+    for (i64 i = 0; i < n; ++i) parts[lab[i]].push_back(rest[i]);
+    for (i64 v : rest) loc[v] = -1;
+    constexpr i64 kRoot = -2;  // "the parent of this component" while apart
+    std::vector<std::vector<std::pair<Vec, i64>>> sub(ncomp);
+    parallel_for<std::unique_ptr<Dissection>>(
+        ncomp, [&](i64 c, std::unique_ptr<Dissection>& wk) {
+          if (!wk) wk.reset(new Dissection(adj, w, leaf, loc));
+          wk->nodes.clear();
+          wk->dissect(std::move(parts[(size_t)c]), kRoot);
+          sub[(size_t)c] = std::move(wk->nodes);
+        });
+    for (i64 c = ncomp - 1; c >= 0; --c) {
+      const i64 off = (i64)nodes.size();
+      for (auto& [set, p] : sub[(size_t)c]) nodes.emplace_back(std::move(set), p == kRoot ? top : p + off);
     }
   }
 
@@ -399,50 +483,10 @@ struct LevelOut {
   i64 schur_len = 0, bord_len = 0;
 };
 
-// Runs fn(level, scratch) for every level on up to VXS_THREADS threads
-// (default: the hardware's, at most 8); the first error is rethrown here.
+// Runs fn(level, scratch) for every level on up to VXS_THREADS threads.
 template <typename Fn>
 void run_levels(i64 nlev, Fn&& fn) {
-  i64 want = (i64)std::thread::hardware_concurrency();
-  if (want <= 0) want = 1;
-  want = std::min<i64>(want, 8);
-  if (const char* env = std::getenv("VXS_THREADS")) {
-    const long v = std::strtol(env, nullptr, 10);
-    if (v > 0) want = v;
-  }
-  const i64 nthreads = std::max<i64>(1, std::min(want, nlev));
-  std::atomic<i64> next{0};
-  std::atomic<bool> failed{false};
-  std::mutex mu;
-  int code = VXS_OK;
-  std::string msg;
-  auto worker = [&] {
-    GatherScratch w;
-    for (;;) {
-      const i64 lv = next.fetch_add(1);
-      if (lv >= nlev || failed.load()) return;
-      try {
-        fn(lv, w);
-      } catch (const Error& e) {
-        std::lock_guard<std::mutex> g(mu);
-        if (!failed.exchange(true)) code = e.code, msg = e.msg;
-      } catch (const std::bad_alloc&) {
-        std::lock_guard<std::mutex> g(mu);
-        if (!failed.exchange(true)) code = VXS_ERR_NOMEM, msg = "out of host memory";
-      }
-    }
-  };
-  std::vector<std::thread> pool;
-  for (i64 t = 1; t < nthreads; ++t) {
-    try {
-      pool.emplace_back(worker);
-    } catch (const std::system_error&) {
-      break;  // fewer threads: the calling thread takes the remaining levels
-    }
-  }
-  worker();
-  for (std::thread& t : pool) t.join();
-  if (failed.load()) fail(code, msg);
+  parallel_for<GatherScratch>(nlev, fn);
 }
 
 
@@ -502,7 +546,8 @@ void build(Plan& P, i64 S, const i64* indptr, const i64* indices, i64 n_unions,
   std::vector<Vec> qsets;
   Vec parents;
   {
-    Dissection nd(Q, w, leaf);
+    Vec loc(G, -1);
+    Dissection nd(Q, w, leaf, loc);
     nd.run(last);
     nd.postorder(qsets, parents);
   }
