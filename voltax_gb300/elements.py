@@ -97,7 +97,16 @@ class Element:
         return len(self.nodes)
 
     def node_array(self) -> np.ndarray:
-        return np.asarray(self.nodes, dtype=np.int64).reshape(self.size, -1)
+        """The node table as a read-only ``(N, T)`` int64 array, converted
+        once per node table (a copy made by `with_nodes` that keeps the
+        table keeps the array)."""
+        held = self.__dict__.get("_node_table")
+        if held is not None and held[0] is self.nodes:
+            return held[1]
+        table = np.asarray(self.nodes, dtype=np.int64).reshape(self.size, -1)
+        table.setflags(write=False)
+        self.__dict__["_node_table"] = (self.nodes, table)
+        return table
 
     def with_nodes(self, nodes) -> "Element":
         new = object.__new__(type(self))

@@ -22,6 +22,7 @@ All draws use ``numpy.random.default_rng(seed)``.
 from __future__ import annotations
 
 import functools
+import itertools
 
 import numpy as np
 import torch
@@ -98,18 +99,23 @@ def _grids(sides, seeds, sigma: float, sink_max: float, vpad: float, prefixes):
         off += len(order)
     cat = np.concatenate
     gnd = lambda a: np.stack([a, np.full_like(a, -1)], 1)  # noqa: E731
-    pads = cat(v_nodes)
-    groups, devices = {}, {}
+    tables = {"Resistor": cat(r_nodes), "CurrentSource": gnd(cat(i_nodes)),
+              "VoltageSource": gnd(cat(v_nodes))}
+    groups, devices = {}, []
     for gname, make, members in (
-            ("Resistor", lambda: Resistor(cat(r_nodes).tolist(), cat(r_val)), r_names),
-            ("CurrentSource", lambda: CurrentSource(gnd(cat(i_nodes)).tolist(), cat(i_val)),
-             i_names),
-            ("VoltageSource", lambda: VoltageSource(gnd(pads).tolist(),
-                                                    np.full(len(pads), float(vpad))), v_names)):
+            ("Resistor", lambda t: Resistor(t.tolist(), cat(r_val)), r_names),
+            ("CurrentSource", lambda t: CurrentSource(t.tolist(), cat(i_val)), i_names),
+            ("VoltageSource", lambda t: VoltageSource(t.tolist(), np.full(len(t), float(vpad))),
+             v_names)):
         if members:
-            groups[gname] = make()
-            devices.update((name, (gname, i)) for i, name in enumerate(members))
-    return Circuit(groups, tuple(names), devices), seg
+            table = tables[gname]
+            el = make(table)
+            table.setflags(write=False)
+            el.__dict__["_node_table"] = (el.nodes, table)  # the array node_array() returns
+            groups[gname] = el
+            # the (device, group, index) triples a builder's name map lays out
+            devices.append(tuple(zip(members, itertools.repeat(gname), range(len(members)))))
+    return Circuit(groups, tuple(names), tuple(itertools.chain.from_iterable(devices))), seg
 
 
 def power_grid(n: int = 100, seed: int = 0, sigma: float = 0.3,
