@@ -86,9 +86,14 @@ class Structure:
 def positions(st: Structure, rows, cols) -> np.ndarray:
     """Positions of ``(rows, cols)`` in the pattern; ``nnz`` where either is
     ground (-1). Raises if an entry is missing (voltax/sparse.py:136-147)."""
-    rows, cols = np.broadcast_arrays(np.asarray(rows), np.asarray(cols))
     keys = st.rows.astype(np.int64) * st.size + st.indices
-    want = rows.astype(np.int64) * st.size + cols
+    return _positions_in(keys, st.size, rows, cols)
+
+
+def _positions_in(keys: np.ndarray, S: int, rows, cols) -> np.ndarray:
+    """`positions` against the sorted entry keys ``row * S + col``."""
+    rows, cols = np.broadcast_arrays(np.asarray(rows), np.asarray(cols))
+    want = rows.astype(np.int64) * S + cols
     pos = np.searchsorted(keys, want)
     ok = (rows >= 0) & (cols >= 0)
     hit = np.where(ok, keys[np.minimum(pos, len(keys) - 1)] == want, True)
@@ -97,9 +102,27 @@ def positions(st: Structure, rows, cols) -> np.ndarray:
     return np.where(ok, pos, len(keys)).astype(np.int32)
 
 
+# Node tables of the circuit whose structure is being built, by the identity
+# of their node tuples: the topology key carries the tuples, the elements
+# already hold them as arrays (`Element.node_array`).
+_NODE_TABLES: dict = {}
+
+
 def structure(circuit, leaf: int | None = None) -> Structure:
     """The cached `Structure` of `circuit`'s topology."""
-    return _structure(circuit.topology_key(), LEAF_SIZE if leaf is None else leaf)
+    _NODE_TABLES.update({id(el.nodes): (el.nodes, el.node_array())
+                         for el in circuit.elements.values() if el.size})
+    try:
+        return _structure(circuit.topology_key(), LEAF_SIZE if leaf is None else leaf)
+    finally:
+        _NODE_TABLES.clear()
+
+
+def _node_table(nodes, n: int) -> np.ndarray:
+    held = _NODE_TABLES.get(id(nodes))
+    if held is not None and held[0] is nodes:
+        return held[1]
+    return np.asarray(nodes, dtype=np.int64).reshape(n, -1)
 
 
 @functools.lru_cache(maxsize=512)
@@ -118,7 +141,7 @@ def build_structure(S: int, nv: int, offsets: dict, groups, leaf: int = LEAF_SIZ
         n, k, off = offsets[name]
         if n == 0:
             continue
-        idx = np.asarray(nodes, dtype=np.int64).reshape(n, -1)
+        idx = _node_table(nodes, n)
         allv = np.concatenate([idx, np.arange(off, off + n * k).reshape(n, k)], 1)
         devices.append((name, allv, idx.shape[1], local))
         blocks = allv if local else allv.reshape(1, -1)
@@ -137,7 +160,7 @@ def build_structure(S: int, nv: int, offsets: dict, groups, leaf: int = LEAF_SIZ
     stamps = []
     for name, allv, _, local in devices:
         blocks = allv if local else allv.reshape(1, -1)
-        pos = positions(st, blocks[:, :, None], blocks[:, None, :])
+        pos = _positions_in(uniq, S, blocks[:, :, None], blocks[:, None, :])
         stamps.append((name, pos if local else pos[0], local))
     object.__setattr__(st, "stamps", tuple(stamps))
     return st
