@@ -156,6 +156,15 @@ def test_take_moves_fields_out_of_the_plan():
         assert lib.vxs_plan_take(h, 14, a.ctypes.data) == 0
         assert lib.vxs_plan_len(h, 14) == 0
         assert a.min() >= 0
+        # a level-table field (kept in per-level pieces) moves out the same way
+        for field in (23, 24):  # ST_PTR, ST_SRC
+            n = lib.vxs_plan_len(h, field)
+            b = np.empty(n, np.int64)
+            assert lib.vxs_plan_copy(h, field, b.ctypes.data) == 0
+            c = np.empty(n, np.int64)
+            assert lib.vxs_plan_take(h, field, c.ctypes.data) == 0
+            assert np.array_equal(b, c) and lib.vxs_plan_len(h, field) == 0
+            assert lib.vxs_plan_copy(h, field, None) == 0
     finally:
         lib.vxs_plan_destroy(h)
 

@@ -380,9 +380,50 @@ struct Dissection {
 // ---------------------------------------------------------------------------
 // The plan.
 // ---------------------------------------------------------------------------
+// One elimination level's launch tables (ends are local CSR ends), and
+// where its Schur and border sources start in the concatenated ST_SRC and
+// BT_SRC.
+struct LevelOut {
+  Vec sn, schur_off, bord_off, st_tgt, st_end, st_src, bt_tgt, bt_end, bt_src;
+  i64 schur_len = 0, bord_len = 0;
+  i64 st_base = 0, bt_base = 0;
+};
+
+// The plan's fields. The per-level launch tables (LV_SN, LV_SCHUR_OFF,
+// LV_BORD_OFF and the ST_* / BT_* gathers) stay in their levels' pieces
+// (`lv`) and are concatenated only by the copy into the caller's array,
+// level by level on the thread pool: the plan never holds a second,
+// concatenated copy of its largest fields.
 struct Plan {
   Vec f[VXS_N_FIELDS];
+  std::vector<LevelOut> lv;
+  uint32_t taken = 0;  // pieced fields already moved out (bit per field)
 };
+
+bool pieced(int field) {
+  switch (field) {
+    case VXS_LV_SN: case VXS_LV_SCHUR_OFF: case VXS_LV_BORD_OFF: case VXS_ST_TGT:
+    case VXS_ST_PTR: case VXS_ST_SRC: case VXS_BT_TGT: case VXS_BT_PTR: case VXS_BT_SRC:
+      return true;
+    default:
+      return false;
+  }
+}
+
+// A level's piece of a pieced field (the CSR pointer fields: its local ends).
+Vec& piece(LevelOut& o, int field) {
+  switch (field) {
+    case VXS_LV_SN: return o.sn;
+    case VXS_LV_SCHUR_OFF: return o.schur_off;
+    case VXS_LV_BORD_OFF: return o.bord_off;
+    case VXS_ST_TGT: return o.st_tgt;
+    case VXS_ST_PTR: return o.st_end;
+    case VXS_ST_SRC: return o.st_src;
+    case VXS_BT_TGT: return o.bt_tgt;
+    case VXS_BT_PTR: return o.bt_end;
+    default: return o.bt_src;
+  }
+}
 
 i64 key3(i64 k, i64 r) { return k * k * k + k * k * r + k * r * r; }
 
@@ -476,12 +517,6 @@ void gather(GatherScratch& w, i64 n_targets, Vec& tgt, Vec& end, Vec& src) {
     emit([&](i64 i) { return w.key_a[i]; }, [&](i64 i) { return w.src_a[i]; });
   }
 }
-
-// One elimination level's launch tables (ends are local CSR ends).
-struct LevelOut {
-  Vec sn, schur_off, bord_off, st_tgt, st_end, st_src, bt_tgt, bt_end, bt_src;
-  i64 schur_len = 0, bord_len = 0;
-};
 
 // Runs fn(level, scratch) for every level on up to VXS_THREADS threads.
 template <typename Fn>
@@ -707,61 +742,26 @@ void build(Plan& P, i64 S, const i64* indptr, const i64* indices, i64 n_unions,
   run_levels(nlev, [&](i64 lv, GatherScratch& w) { build_level(lv, w, outs[lv]); });
 
   Vec& lv_ptr = P.f[VXS_LV_PTR];
-  Vec& lv_sn = P.f[VXS_LV_SN];
-  Vec& lv_schur_off = P.f[VXS_LV_SCHUR_OFF];
-  Vec& lv_bord_off = P.f[VXS_LV_BORD_OFF];
   Vec& lv_schur_len = P.f[VXS_LV_SCHUR_LEN];
   Vec& lv_bord_len = P.f[VXS_LV_BORD_LEN];
   Vec& lv_st_ptr = P.f[VXS_LV_ST_PTR];
-  Vec& st_tgt = P.f[VXS_ST_TGT];
-  Vec& st_ptr = P.f[VXS_ST_PTR];
-  Vec& st_src = P.f[VXS_ST_SRC];
   Vec& lv_bt_ptr = P.f[VXS_LV_BT_PTR];
-  Vec& bt_tgt = P.f[VXS_BT_TGT];
-  Vec& bt_ptr = P.f[VXS_BT_PTR];
-  Vec& bt_src = P.f[VXS_BT_SRC];
-  i64 n_st = 0, n_ss = 0, n_bt = 0, n_bs = 0;
-  for (const LevelOut& o : outs) {
-    n_st += (i64)o.st_tgt.size();
-    n_ss += (i64)o.st_src.size();
-    n_bt += (i64)o.bt_tgt.size();
-    n_bs += (i64)o.bt_src.size();
-  }
-  lv_sn.reserve(nsn);
-  st_tgt.reserve(n_st);
-  st_ptr.reserve(n_st + 1);
-  st_src.reserve(n_ss);
-  bt_tgt.reserve(n_bt);
-  bt_ptr.reserve(n_bt + 1);
-  bt_src.reserve(n_bs);
   lv_ptr.assign(1, 0);
   lv_st_ptr.assign(1, 0);
   lv_bt_ptr.assign(1, 0);
-  st_ptr.assign(1, 0);
-  bt_ptr.assign(1, 0);
-  auto append = [](Vec& dst, Vec& src) {
-    dst.insert(dst.end(), src.begin(), src.end());
-    Vec().swap(src);
-  };
-  for (LevelOut& o : outs) {  // level order; each level freed once copied
-    append(lv_sn, o.sn);
-    append(lv_schur_off, o.schur_off);
-    append(lv_bord_off, o.bord_off);
-    const i64 sbase = (i64)st_src.size(), bbase = (i64)bt_src.size();
-    for (i64 e : o.st_end) st_ptr.push_back(sbase + e);
-    for (i64 e : o.bt_end) bt_ptr.push_back(bbase + e);
-    Vec().swap(o.st_end);
-    Vec().swap(o.bt_end);
-    append(st_tgt, o.st_tgt);
-    append(st_src, o.st_src);
-    append(bt_tgt, o.bt_tgt);
-    append(bt_src, o.bt_src);
-    lv_ptr.push_back((i64)lv_sn.size());
+  i64 n_ss = 0, n_bs = 0;
+  for (LevelOut& o : outs) {  // level order
+    o.st_base = n_ss;
+    o.bt_base = n_bs;
+    n_ss += (i64)o.st_src.size();
+    n_bs += (i64)o.bt_src.size();
+    lv_ptr.push_back(lv_ptr.back() + (i64)o.sn.size());
     lv_schur_len.push_back(o.schur_len);
     lv_bord_len.push_back(o.bord_len);
-    lv_st_ptr.push_back((i64)st_tgt.size());
-    lv_bt_ptr.push_back((i64)bt_tgt.size());
+    lv_st_ptr.push_back(lv_st_ptr.back() + (i64)o.st_tgt.size());
+    lv_bt_ptr.push_back(lv_bt_ptr.back() + (i64)o.bt_tgt.size());
   }
+  P.lv = std::move(outs);
 
   P.f[VXS_GID] = std::move(gid);
   P.f[VXS_PARENT] = std::move(parents);
@@ -803,7 +803,11 @@ int vxs_plan_create(int64_t S, const int64_t* indptr, const int64_t* indices,
 
 int64_t vxs_plan_len(const vxs_plan* p, int32_t field) {
   if (!p || field < 0 || field >= VXS_N_FIELDS) return -1;
-  return (int64_t)p->p.f[field].size();
+  if (!pieced(field)) return (int64_t)p->p.f[field].size();
+  if ((p->p.taken >> field) & 1u) return 0;
+  int64_t n = (field == VXS_ST_PTR || field == VXS_BT_PTR) ? 1 : 0;
+  for (const LevelOut& o : p->p.lv) n += (int64_t)piece(const_cast<LevelOut&>(o), field).size();
+  return n;
 }
 
 int vxs_plan_copy(const vxs_plan* p, int32_t field, int64_t* dst) {
@@ -811,20 +815,51 @@ int vxs_plan_copy(const vxs_plan* p, int32_t field, int64_t* dst) {
     g_error = "unknown plan field";
     return VXS_ERR_INVALID;
   }
-  const Vec& v = p->p.f[field];
-  if (!v.empty()) {
-    if (!dst) {
-      g_error = "null destination";
-      return VXS_ERR_INVALID;
-    }
-    std::memcpy(dst, v.data(), v.size() * sizeof(int64_t));
+  if (vxs_plan_len(p, field) > 0 && !dst) {
+    g_error = "null destination";
+    return VXS_ERR_INVALID;
+  }
+  if (!pieced(field)) {
+    const Vec& v = p->p.f[field];
+    if (!v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(int64_t));
+    return VXS_OK;
+  }
+  if ((p->p.taken >> field) & 1u) return VXS_OK;  // already moved out: nothing left
+  // each level's piece at its offset; a pointer field's local ends shifted
+  // by where the level's sources start
+  const bool ends = field == VXS_ST_PTR || field == VXS_BT_PTR;
+  std::vector<LevelOut>& lv = const_cast<std::vector<LevelOut>&>(p->p.lv);
+  const i64 nlev = (i64)lv.size();
+  Vec off(nlev + 1, ends ? 1 : 0);
+  for (i64 L = 0; L < nlev; ++L) off[L + 1] = off[L] + (i64)piece(lv[L], field).size();
+  if (ends) dst[0] = 0;
+  try {
+    parallel_for<char>(nlev, [&](i64 L, char&) {
+      const Vec& v = piece(lv[L], field);
+      int64_t* out = dst + off[L];
+      if (ends) {
+        const i64 base = field == VXS_ST_PTR ? lv[L].st_base : lv[L].bt_base;
+        for (size_t i = 0; i < v.size(); ++i) out[i] = base + v[i];
+      } else if (!v.empty()) {
+        std::memcpy(out, v.data(), v.size() * sizeof(int64_t));
+      }
+    });
+  } catch (const Error& e) {
+    g_error = e.msg;
+    return e.code;
   }
   return VXS_OK;
 }
 
 int vxs_plan_take(vxs_plan* p, int32_t field, int64_t* dst) {
   const int rc = vxs_plan_copy(p, field, dst);
-  if (rc == VXS_OK) Vec().swap(p->p.f[field]);
+  if (rc == VXS_OK) {
+    if (pieced(field)) {
+      for (LevelOut& o : p->p.lv) Vec().swap(piece(o, field));
+      p->p.taken |= 1u << field;
+    } else
+      Vec().swap(p->p.f[field]);
+  }
   return rc;
 }
 
