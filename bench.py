@@ -539,17 +539,17 @@ def max_over_ranks(dist, seconds: float, device) -> float:
 # FP64 work of the fused kernel's chosen form per Newton iteration of one
 # 4-bit mirror-adder instance: 2 DFMA + DADD + DMUL thread instructions that
 # ncu counted on the 512-instance x 21-point launch (fused_kernel<float,128>,
-# profiles/fused_kernel_adder_mc512.md), 2.962e9 FLOP, divided by that
+# the committed ncu summary of that launch), 2.96e9 FLOP, divided by that
 # launch's 95,827 Newton iterations. It is fixed by the algorithm (the same
 # device equations, residual and update every iteration), so it is the
 # roofline's per-unit work; the FP64 peak is the hardware rate ncu reports
 # (2 DFMA per cycle per SM) at the SM clock sampled during the run.
 FUSED_FP64_FLOP_PER_ITER = {"adder_mc": 30_907.0}
-FUSED_NCU = {"source": "profiles/fused_kernel_adder_mc512.md", "issue_active_pct": 21.2,
-             "fp64_pipe_active_pct": 33.8, "warps_eligible_per_scheduler_cycle": 0.24,
-             "top_stalls_per_issue": {"barrier": 5.92, "short_scoreboard": 4.21,
-                                      "wait": 3.27},
-             "dram_bytes_per_launch_512x21": 5.88e6}
+FUSED_NCU = {"source": "profiles/fused_kernel_adder_mc512.md", "issue_active_pct": 21.1,
+             "fp64_pipe_active_pct": 32.3, "warps_eligible_per_scheduler_cycle": 0.24,
+             "top_stalls_per_issue": {"barrier": 6.04, "short_scoreboard": 4.17,
+                                      "wait": 3.20},
+             "dram_bytes_per_launch_512x21": 5.89e6}
 
 
 def measure_circuit(g, a, w, instances, n_t, steps, warmup, cpu=None, full=True):
