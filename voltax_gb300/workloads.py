@@ -102,10 +102,11 @@ def _grids(sides, seeds, sigma: float, sink_max: float, vpad: float, prefixes):
     tables = {"Resistor": cat(r_nodes), "CurrentSource": gnd(cat(i_nodes)),
               "VoltageSource": gnd(cat(v_nodes))}
     groups, devices = {}, []
+    rows = lambda t: tuple(zip(*t.T.tolist()))  # noqa: E731  (node tuples, made by zip)
     for gname, make, members in (
-            ("Resistor", lambda t: Resistor(t.tolist(), cat(r_val)), r_names),
-            ("CurrentSource", lambda t: CurrentSource(t.tolist(), cat(i_val)), i_names),
-            ("VoltageSource", lambda t: VoltageSource(t.tolist(), np.full(len(t), float(vpad))),
+            ("Resistor", lambda t: Resistor(rows(t), cat(r_val)), r_names),
+            ("CurrentSource", lambda t: CurrentSource(rows(t), cat(i_val)), i_names),
+            ("VoltageSource", lambda t: VoltageSource(rows(t), np.full(len(t), float(vpad))),
              v_names)):
         if members:
             table = tables[gname]
