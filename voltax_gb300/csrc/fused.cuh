@@ -1124,7 +1124,7 @@ struct Instance {
 };
 
 // Resident CTAs per SM the register allocation is sized for. FP32 with
-// 128-thread CTAs: six (85 registers a thread; on the 4096-instance adder
+// 128-thread CTAs: six (80 registers a thread; on the 4096-instance adder
 // 2.63 M solves/s against 2.57 M with five and 2.14 M with four, the extra
 // spills of the smaller budget notwithstanding). FP64, whose spills grow
 // faster, and larger blocks: 640 threads per SM (five 128-thread CTAs, two
