@@ -70,6 +70,27 @@ def _grid_arrays(n: int, rng, sigma: float, sink_max: float):
     return order, rank[ends], rank[ids.ravel()], rank[pads], g, sinks
 
 
+class _Names:
+    """Name strings shared by the grids of one batch (freed with it): the
+    ``n{i}_{j}`` site names of each side, and ``R0, R1, ...`` style counters."""
+
+    def __init__(self):
+        self._sites: dict[int, tuple[str, ...]] = {}
+        self._numbered: dict[str, list[str]] = {}
+
+    def sites(self, n: int) -> tuple[str, ...]:
+        got = self._sites.get(n)
+        if got is None:
+            got = self._sites[n] = tuple(f"n{q // n}_{q % n}" for q in range(n * n))
+        return got
+
+    def numbered(self, letter: str, count: int) -> list[str]:
+        have = self._numbered.setdefault(letter, [])
+        if len(have) < count:
+            have.extend(f"{letter}{q}" for q in range(len(have), count))
+        return have[:count]
+
+
 def _grids(sides, seeds, sigma: float, sink_max: float, vpad: float, prefixes):
     """Grids as one circuit, built from arrays: the node numbering, device
     names, groups and parameters of adding every segment, sink and pad to a
@@ -83,19 +104,22 @@ def _grids(sides, seeds, sigma: float, sink_max: float, vpad: float, prefixes):
     r_val, i_val = [], []
     r_names, i_names, v_names = [], [], []
     off = 0
+    known = _Names()
     for k, (n, seed, pre) in enumerate(zip(sides, seeds, prefixes)):
+        n = int(n)
         order, ends, sink_at, pad_at, g, sinks = _grid_arrays(
-            int(n), np.random.default_rng(seed), sigma, sink_max)
-        names += [f"{pre}n{q // n}_{q % n}" for q in order]
+            n, np.random.default_rng(seed), sigma, sink_max)
+        site = known.sites(n)
+        names += map(pre.__add__, (site[q] for q in order.tolist()))
         seg += [k] * len(order)
         r_nodes.append(ends + off)
         r_val.append(1.0 / g)
         i_nodes.append(sink_at + off)
         i_val.append(sinks)
         v_nodes.append(pad_at + off)
-        r_names += [f"{pre}R{q}" for q in range(len(ends))]
-        i_names += [f"{pre}I{q}" for q in range(len(sinks))]
-        v_names += [f"{pre}Vpad{q}" for q in range(len(pad_at))]
+        r_names += map(pre.__add__, known.numbered("R", len(ends)))
+        i_names += map(pre.__add__, known.numbered("I", len(sinks)))
+        v_names += map(pre.__add__, known.numbered("Vpad", len(pad_at)))
         off += len(order)
     cat = np.concatenate
     gnd = lambda a: np.stack([a, np.full_like(a, -1)], 1)  # noqa: E731
